@@ -1,0 +1,291 @@
+"""ctypes binding of libedfmm.so (declared in include/edfmm.h).
+
+The library is the only compute path of this package: if it is missing, or
+no CUDA device is visible, every entry point raises instead of falling back
+to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libedfmm.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "edfmm.h")
+
+EDFMM_OK = 0
+EDFMM_ERR_ARG = -1
+EDFMM_ERR_CUDA = -2
+EDFMM_ERR_ALLOC = -3
+EDFMM_ERR_UNSUPPORTED = -4
+EDFMM_ERR_STATE = -5
+EDFMM_F32 = 0
+EDFMM_F64 = 1
+EDFMM_REFERENCE_PAIR_ORDER = 1
+EDFMM_NO_FARFIELD = 2
+EDFMM_NO_NEARFIELD = 4
+
+
+class EdfmmError(RuntimeError):
+    """A libedfmm call returned a non-zero status."""
+
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where} failed with status {code}: {message}")
+        self.code = code
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int64),
+        ("n_nodes", C.c_int64),
+        ("n_leaves", C.c_int64),
+        ("n_p2p_pairs", C.c_int64),
+        ("n_m2l_pairs", C.c_int64),
+        ("p2p_interactions", C.c_int64),
+        ("max_level", C.c_int32),
+        ("depth_warnings", C.c_int32),
+        ("dtype", C.c_int32),
+        ("expansion_order", C.c_int32),
+        ("leaf_size", C.c_int32),
+        ("max_depth", C.c_int32),
+        ("mac_theta", C.c_double),
+    ]
+
+
+_lib = None
+_lock = threading.Lock()
+_vp = C.c_void_p
+
+
+def _declare(L):
+    i32, i64, dbl = C.c_int, C.c_int64, C.c_double
+    sig = {
+        "edfmm_last_error": (C.c_char_p, []),
+        "edfmm_version": (C.c_char_p, []),
+        "edfmm_launch_count": (i64, []),
+        "edfmm_plan_create": (i32, [_vp, i64, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
+        "edfmm_plan_destroy": (i32, [_vp]),
+        "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
+        "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
+        "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
+        "edfmm_plan_export_tree": (i32, [_vp] * 11),
+        "edfmm_plan_export_lists": (i32, [_vp, _vp, _vp, _vp]),
+        "edfmm_plan_matvec": (i32, [_vp, _vp, _vp, _vp, dbl, _vp, i32, _vp]),
+        "edfmm_plan_set_charges": (i32, [_vp, _vp, _vp]),
+        "edfmm_plan_p2m": (i32, [_vp, _vp]),
+        "edfmm_plan_m2m": (i32, [_vp, _vp]),
+        "edfmm_plan_m2l": (i32, [_vp, i32, _vp]),
+        "edfmm_plan_l2l": (i32, [_vp, _vp]),
+        "edfmm_plan_l2p": (i32, [_vp, _vp, _vp]),
+        "edfmm_plan_p2p": (i32, [_vp, _vp, _vp]),
+        "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
+        "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def load_library(require_cuda: bool = True):
+    """Load libedfmm.so; raise if it is missing or (by default) CUDA is absent."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"libedfmm.so not found at {LIB_PATH}; build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` (nvcc, sm_103a)"
+                )
+            L = C.CDLL(LIB_PATH)
+            _declare(L)
+            _lib = L
+    if require_cuda and not torch.cuda.is_available():
+        raise RuntimeError("electrodrive_gb300 requires a CUDA device (no CPU fallback)")
+    return _lib
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/edfmm.h."""
+    with open(HEADER_PATH) as f:
+        txt = f.read()
+    return sorted(set(re.findall(r"\b(edfmm_[a-z0-9_]+)\s*\(", txt)))
+
+
+def check(rc: int, where: str):
+    if rc != EDFMM_OK:
+        msg = _lib.edfmm_last_error().decode() if _lib is not None else ""
+        raise EdfmmError(rc, where, msg)
+
+
+def ptr(t: torch.Tensor | None):
+    return None if t is None else _vp(t.data_ptr())
+
+
+def stream_handle(device=None):
+    return _vp(torch.cuda.current_stream(device).cuda_stream)
+
+
+def dtype_code(dt: torch.dtype) -> int:
+    if dt == torch.float32:
+        return EDFMM_F32
+    if dt == torch.float64:
+        return EDFMM_F64
+    raise ValueError(f"unsupported dtype {dt}; expected float32 or float64")
+
+
+def launch_count() -> int:
+    return int(load_library(require_cuda=False).edfmm_launch_count())
+
+
+def measure_fp32_peak(iters: int = 20000) -> float:
+    """FP32 FMA throughput of the current device, TFLOP/s."""
+    L = load_library()
+    out = C.c_double()
+    check(L.edfmm_measure_fp32_peak(int(iters), stream_handle(), C.byref(out)), "edfmm_measure_fp32_peak")
+    return float(out.value)
+
+
+class Plan:
+    """Owns an edfmm_plan: device octree + interaction lists + expansion buffers."""
+
+    def __init__(self, points: torch.Tensor, *, leaf_size: int = 64, max_depth: int = 32,
+                 mac_theta: float = 0.5, expansion_order: int = 8):
+        L = load_library()
+        if points.ndim != 2 or points.shape[-1] != 3:
+            raise ValueError(f"points must have shape (N, 3), got {tuple(points.shape)}")
+        if not points.is_cuda:
+            raise ValueError("Plan expects CUDA points")
+        pts = points.contiguous()
+        self.device = pts.device
+        self.dtype = pts.dtype
+        h = _vp()
+        with torch.cuda.device(self.device):
+            rc = L.edfmm_plan_create(ptr(pts), pts.shape[0], dtype_code(pts.dtype), int(leaf_size), int(max_depth),
+                                     float(mac_theta), int(expansion_order), stream_handle(self.device), C.byref(h))
+        check(rc, "edfmm_plan_create")
+        self._h = h
+        self._lib = L
+        info = PlanInfo()
+        check(L.edfmm_plan_get_info(h, C.byref(info)), "edfmm_plan_get_info")
+        self.info = info
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.edfmm_plan_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _refresh_info(self):
+        info = PlanInfo()
+        check(self._lib.edfmm_plan_get_info(self._h, C.byref(info)), "edfmm_plan_get_info")
+        self.info = info
+
+    def rebuild_lists(self, mac_theta: float):
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_rebuild_lists(self._h, float(mac_theta), stream_handle(self.device)),
+                  "edfmm_plan_rebuild_lists")
+        self._refresh_info()
+
+    def set_order(self, p: int):
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_set_order(self._h, int(p), stream_handle(self.device)), "edfmm_plan_set_order")
+        self._refresh_info()
+
+    # ---------------------------------------------------------------- exports
+    def export_tree(self):
+        i = self.info
+        dev, dt = self.device, self.dtype
+        M, N = i.n_nodes, i.n_points
+        out = dict(
+            index_map=torch.empty(N, dtype=torch.int64, device=dev),
+            node_centers=torch.empty(M, 3, dtype=dt, device=dev),
+            node_half_extents=torch.empty(M, 3, dtype=dt, device=dev),
+            node_radii=torch.empty(M, dtype=dt, device=dev),
+            node_levels=torch.empty(M, dtype=torch.int32, device=dev),
+            node_parents=torch.empty(M, dtype=torch.int64, device=dev),
+            node_children=torch.empty(M, 8, dtype=torch.int64, device=dev),
+            node_ranges=torch.empty(M, 2, dtype=torch.int64, device=dev),
+            node_is_leaf=torch.empty(M, dtype=torch.bool, device=dev),
+        )
+        with torch.cuda.device(dev):
+            check(self._lib.edfmm_plan_export_tree(
+                self._h, ptr(out["index_map"]), ptr(out["node_centers"]), ptr(out["node_half_extents"]),
+                ptr(out["node_radii"]), ptr(out["node_levels"]), ptr(out["node_parents"]), ptr(out["node_children"]),
+                ptr(out["node_ranges"]), ptr(out["node_is_leaf"]), stream_handle(dev)), "edfmm_plan_export_tree")
+        return out
+
+    def export_lists(self):
+        dev = self.device
+        p2p = torch.empty(self.info.n_p2p_pairs, 2, dtype=torch.int64, device=dev)
+        m2l = torch.empty(self.info.n_m2l_pairs, 2, dtype=torch.int64, device=dev)
+        with torch.cuda.device(dev):
+            check(self._lib.edfmm_plan_export_lists(self._h, ptr(p2p), ptr(m2l), stream_handle(dev)),
+                  "edfmm_plan_export_lists")
+        return p2p, m2l
+
+    def expansions(self):
+        nc = (self.info.expansion_order + 1) * (self.info.expansion_order + 2) // 2
+        cdt = torch.complex64 if self.dtype == torch.float32 else torch.complex128
+        Mx = torch.empty(self.info.n_nodes, nc, dtype=cdt, device=self.device)
+        Lx = torch.empty(self.info.n_nodes, nc, dtype=cdt, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_get_expansions(self._h, ptr(Mx), ptr(Lx), stream_handle(self.device)),
+                  "edfmm_plan_get_expansions")
+        return Mx, Lx
+
+    # ---------------------------------------------------------------- compute
+    def _check_vec(self, t: torch.Tensor, name: str):
+        if t.device != self.device or t.dtype != self.dtype or t.shape != (self.info.n_points,):
+            raise ValueError(f"{name} must be a ({self.info.n_points},) {self.dtype} tensor on {self.device}, "
+                             f"got {tuple(t.shape)} {t.dtype} on {t.device}")
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+
+    def matvec(self, sigma, areas, self_integrals=None, *, k_e: float = 1.0, out=None, flags: int = 0):
+        self._check_vec(sigma, "sigma")
+        self._check_vec(areas, "areas")
+        if self_integrals is not None:
+            self._check_vec(self_integrals, "self_integrals")
+        if out is None:
+            out = torch.empty_like(sigma)
+        else:
+            self._check_vec(out, "out")
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_matvec(self._h, ptr(sigma), ptr(areas), ptr(self_integrals), float(k_e),
+                                              ptr(out), int(flags), stream_handle(self.device)), "edfmm_plan_matvec")
+        return out
+
+    def set_charges(self, charges):
+        self._check_vec(charges, "charges")
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_set_charges(self._h, ptr(charges), stream_handle(self.device)),
+                  "edfmm_plan_set_charges")
+
+    def stage(self, name: str, *args):
+        fn = getattr(self._lib, f"edfmm_plan_{name}")
+        with torch.cuda.device(self.device):
+            check(fn(self._h, *args, stream_handle(self.device)), f"edfmm_plan_{name}")
+
+    def p2p(self):
+        out = torch.empty(self.info.n_points, dtype=self.dtype, device=self.device)
+        self.stage("p2p", ptr(out))
+        return out
+
+    def l2p(self):
+        out = torch.empty(self.info.n_points, dtype=self.dtype, device=self.device)
+        self.stage("l2p", ptr(out))
+        return out

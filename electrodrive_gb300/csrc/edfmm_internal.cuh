@@ -1,0 +1,205 @@
+// Internal declarations shared by the libedfmm translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/edfmm.h"
+
+namespace edfmm {
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+void count_launch(int n = 1);
+
+#define EDFMM_CUDA_TRY(expr)                                                                  \
+    do {                                                                                      \
+        cudaError_t _e = (expr);                                                              \
+        if (_e != cudaSuccess)                                                                \
+            return ::edfmm::fail(EDFMM_ERR_CUDA, std::string(#expr " failed: ") +             \
+                                                     cudaGetErrorString(_e));                 \
+    } while (0)
+
+#define EDFMM_LAUNCH_CHECK(name)                                                              \
+    do {                                                                                      \
+        ::edfmm::count_launch();                                                              \
+        cudaError_t _e = cudaGetLastError();                                                  \
+        if (_e != cudaSuccess)                                                                \
+            return ::edfmm::fail(EDFMM_ERR_CUDA, std::string("launch of " name " failed: ") + \
+                                                     cudaGetErrorString(_e));                 \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffer (owning)
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            bytes = o.bytes;
+            o.p = nullptr;
+            o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    // grows (never shrinks); contents are not preserved
+    int reserve(size_t nbytes) {
+        if (nbytes <= bytes && p) return EDFMM_OK;
+        release();
+        size_t want = nbytes ? nbytes : 16;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(EDFMM_ERR_ALLOC, std::string("cudaMalloc of ") + std::to_string(want) +
+                                             " bytes failed: " + cudaGetErrorString(e));
+        }
+        bytes = want;
+        return EDFMM_OK;
+    }
+    template <class U> U *as() const { return static_cast<U *>(p); }
+};
+
+// typed view of a buffer (a free function, so no `template` keyword is needed
+// inside templates)
+template <class U> inline U *dptr(const DevBuf &b) { return static_cast<U *>(b.p); }
+
+// ---------------------------------------------------------------------------
+// primitives (scan.cu)
+// ---------------------------------------------------------------------------
+// Exclusive prefix sum of n int32 counts into int32 offsets; the grand total
+// is written to *total_dev (int64) if non-null.  tmp must hold scan_tmp_bytes(n).
+size_t scan_tmp_bytes(int64_t n);
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, int64_t *total_dev, void *tmp,
+                   cudaStream_t s);
+
+// Sort every CSR row of `vals` ascending (rows given by offsets[0..rows]).
+// tmp must hold sort_rows_tmp_bytes(...) for the longest rows.
+int sort_csr_rows(const int32_t *offsets, int32_t *vals, int64_t rows, int64_t max_row_len,
+                  cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// tree + lists (tree.cu, lists.cu)
+// ---------------------------------------------------------------------------
+template <typename T> struct Vec4 {};
+template <> struct Vec4<float> {
+    using type = float4;
+};
+template <> struct Vec4<double> {
+    using type = double4;
+};
+
+// Device-resident tree in DFS pre-order (the reference's node numbering).
+struct DevTree {
+    int dtype = EDFMM_F32;
+    int64_t n_points = 0;
+    int64_t n_nodes = 0;
+    int64_t n_leaves = 0;
+    int max_level = 0;
+    int depth_warnings = 0;
+    DevBuf pts;        // T4 per point, tree order: (x, y, z, charge)
+    DevBuf index_map;  // int32, tree position -> original index
+    DevBuf center;     // T4 per node: (cx, cy, cz, radius)
+    DevBuf half;       // T4 per node: (hx, hy, hz, expansion scale a)
+    DevBuf range;      // int2 per node: [start, end)
+    DevBuf parent;     // int32
+    DevBuf children;   // int32 x 8
+    DevBuf level;      // int32
+    DevBuf is_leaf;    // uint8
+    DevBuf leaves;     // int32 ids of leaf nodes (ascending)
+    std::vector<int32_t> level_offsets;  // host: level l nodes = level_nodes[off[l], off[l+1])
+    DevBuf level_nodes;                  // int32 node ids grouped by level
+};
+
+int tree_build(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth,
+               DevTree &tree, cudaStream_t s);
+
+struct DevLists {
+    int64_t n_p2p = 0, n_m2l = 0;
+    int64_t p2p_interactions = 0;
+    int64_t max_p2p_row = 0, max_m2l_row = 0;
+    DevBuf p2p_off, p2p_src;  // CSR by target, sources ascending
+    DevBuf m2l_off, m2l_src;
+    // transposed M2L CSR (rows = listed sources), built on demand for the
+    // reference's swapped pair order
+    bool have_m2l_swapped = false;
+    DevBuf m2l_swapped_off, m2l_swapped_src;
+};
+
+int lists_build(const DevTree &tree, double theta, DevLists &lists, cudaStream_t s);
+int lists_build_swapped(const DevTree &tree, DevLists &lists, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// FMM stages (farfield.cu, nearfield.cu)
+// ---------------------------------------------------------------------------
+inline int num_coeffs(int p) { return (p + 1) * (p + 2) / 2; }
+
+// M2L pairs whose source radius exceeds 256x the target radius, as CSR rows
+// by target (FP32 plans only; empty for uniform trees).
+struct ExtremeRows {
+    bool built = false;
+    int64_t n_pairs = 0, n_rows = 0;
+    DevBuf off, src, rows;
+};
+
+struct FmmBuffers {
+    int p = 8;
+    int nc = 45;
+    int nc_pad = 46;  // per-node stride in complex numbers (even: 16-byte rows for float)
+    DevBuf multipoles;  // complex T, n_nodes x nc_pad
+    DevBuf locals;      // complex T, n_nodes x nc_pad
+    ExtremeRows extreme, extreme_swapped;
+};
+
+int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaStream_t s);
+int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
+int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
+int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s);
+int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
+
+struct NearArgs {
+    const void *sigma = nullptr;      // original order (nullable)
+    const void *areas = nullptr;      // original order (nullable)
+    const void *self_int = nullptr;   // original order (nullable)
+    double k_e = 1.0;
+    void *out = nullptr;              // original order if scatter, else tree order
+    bool scatter = false;             // write out[index_map[i]] with k_e, self term, clamp
+    bool near = true;                 // include P2P
+    bool far = true;                  // include L2P
+};
+int run_p2p_l2p(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
+                const NearArgs &args, cudaStream_t s);
+int upload_tables();
+
+}  // namespace edfmm
+
+struct edfmm_plan {
+    edfmm::DevTree tree;
+    edfmm::DevLists lists;
+    edfmm::FmmBuffers fmm;
+    double mac_theta = 0.5;
+    int leaf_size = 64;
+    int max_depth = 32;
+    int device = 0;
+};

@@ -1,0 +1,700 @@
+// Far-field stages of the FMM: P2M, M2M, M2L, L2L.
+//
+// Coefficients are stored per node as (p+1)(p+2)/2 complex numbers (m >= 0),
+// scaled by the node's expansion radius a (the tight-box radius, floored at
+// 2^-40 of the root radius):  Mhat_n^m = M_n^m / a^n,  Lhat_n^m = L_n^m a^n.
+// This keeps every coefficient O(1) in FP32 at any tree depth.
+//
+// M2L (the dominant stage) is organised so that one lane owns one
+// (target, source) pair at a time and keeps the whole translation in
+// registers: the source multipole (scaled by (a_M/a_L)^k), the accumulator
+// for the 45 target coefficients (p = 8) and one column of irregular
+// harmonics of v = (c_L - c_M) / a_L, generated by recurrence.  A warp walks
+// one target's row of the interaction list; the 32 partial sums are reduced
+// with shuffles, so the result is deterministic.  With this scaling
+//   Lhat_n^m = (-1)^(n+m) / a_L  sum_pairs sum_{k,l} Mhat_k^l (a_M/a_L)^k I_{n+k}^{l-m}(v),
+// which is exact algebra; pairs whose source radius exceeds 256x the target's
+// (only in strongly adaptive trees) would overflow (a_M/a_L)^k in FP32 and are
+// instead translated by a shared-memory kernel using
+//   Lhat_n^m = (-1)^(n+m) / a_L  (a_L/a_M)^(n+1) sum_{k,l} Mhat_k^l I_{n+k}^{l-m}((c_L - c_M)/a_M).
+// FP64 plans use that kernel for every pair.
+#include <algorithm>
+
+#include "edfmm_internal.cuh"
+#include "harmonics.cuh"
+
+namespace edfmm {
+
+namespace {
+
+constexpr float kExtremeRatio = 256.0f;
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+__device__ __forceinline__ void coef_nm(int c, int &n, int &m) {
+    n = 0;
+    while ((n + 1) * (n + 2) / 2 <= c) ++n;
+    m = c - n * (n + 1) / 2;
+}
+
+// ---------------------------------------------------------------------------
+// charges
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_set_charges(typename Vec4<T>::type *pts, const int32_t *__restrict__ idx, int64_t n,
+                              const T *__restrict__ a, const T *__restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = idx[i];
+    pts[i].w = b ? a[o] * b[o] : a[o];
+}
+
+// ---------------------------------------------------------------------------
+// P2M: warp per leaf, lanes over points
+// ---------------------------------------------------------------------------
+template <typename T, int P>
+__global__ void __launch_bounds__(128) k_p2m(const int32_t *__restrict__ leaves, int64_t n_leaves,
+                                             const typename Vec4<T>::type *__restrict__ pts,
+                                             const typename Vec4<T>::type *__restrict__ center,
+                                             const typename Vec4<T>::type *__restrict__ half, const int2 *range,
+                                             Cplx<T> *Mexp, int nc_pad) {
+    constexpr int NC = ncoef(P);
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n_leaves) return;
+    const int leaf = leaves[w];
+    const typename Vec4<T>::type c = center[leaf];
+    const T ia = (T)1 / half[leaf].w;
+    const int2 rg = range[leaf];
+    T accr[NC], acci[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) accr[k] = acci[k] = (T)0;
+    for (int i = rg.x + lane; i < rg.y; i += 32) {
+        const typename Vec4<T>::type p = pts[i];
+        T Rr[NC], Ri[NC];
+        regular_harmonics<T, P>((p.x - c.x) * ia, (p.y - c.y) * ia, (p.z - c.z) * ia, Rr, Ri);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            accr[k] += p.w * Rr[k];
+            acci[k] -= p.w * Ri[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            accr[k] += __shfl_xor_sync(0xffffffffu, accr[k], o);
+            acci[k] += __shfl_xor_sync(0xffffffffu, acci[k], o);
+        }
+    }
+    Cplx<T> *out = Mexp + (int64_t)leaf * nc_pad;
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+        if ((k & 31) == lane) out[k] = Cplx<T>{accr[k], acci[k]};
+}
+
+// ---------------------------------------------------------------------------
+// M2M: warp per internal node of one level, lanes over output coefficients
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_m2m(const int32_t *__restrict__ nodes, int n_nodes,
+                                             const uint8_t *__restrict__ is_leaf, const int32_t *__restrict__ children,
+                                             const typename Vec4<T>::type *__restrict__ center,
+                                             const typename Vec4<T>::type *__restrict__ half, Cplx<T> *Mexp, int p,
+                                             int nc_pad) {
+    __shared__ Cplx<T> sR[4][ncoef(kPMax)], sM[4][ncoef(kPMax)];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 4 + wl;
+    if (w >= n_nodes) return;
+    const int node = nodes[w];
+    if (is_leaf[node]) return;
+    const int nc = ncoef(p);
+    const typename Vec4<T>::type cp = center[node];
+    const T aP = half[node].w, iaP = (T)1 / aP;
+    Cplx<T> acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int o = 0; o < 8; ++o) {
+        const int ch = children[8 * node + o];
+        if (ch < 0) continue;
+        const typename Vec4<T>::type cc = center[ch];
+        const T ratio = half[ch].w * iaP;
+        if (lane == 0) regular_harmonics_rt<T>((cc.x - cp.x) * iaP, (cc.y - cp.y) * iaP, (cc.z - cp.z) * iaP, p, sR[wl]);
+        for (int k = lane; k < nc; k += 32) {
+            int n, m;
+            coef_nm(k, n, m);
+            T sc = (T)1;
+            for (int e = 0; e < n; ++e) sc *= ratio;
+            Cplx<T> v = Mexp[(int64_t)ch * nc_pad + k];
+            sM[wl][k] = Cplx<T>{v.re * sc, v.im * sc};
+        }
+        __syncwarp();
+        for (int q = 0; q < 3; ++q) {
+            const int k = lane + 32 * q;
+            if (k >= nc) break;
+            int n, m;
+            coef_nm(k, n, m);
+            Cplx<T> a = acc[q];
+            for (int kk = 0; kk <= n; ++kk) {
+                const int j = n - kk;
+                for (int l = -kk; l <= kk; ++l) {
+                    const int u = m - l;
+                    if (u < -j || u > j) continue;
+                    Cplx<T> r = harm_at(sR[wl], kk, l);
+                    Cplx<T> mm = harm_at(sM[wl], j, u);
+                    // conj(r) * mm
+                    a.re += r.re * mm.re + r.im * mm.im;
+                    a.im += r.re * mm.im - r.im * mm.re;
+                }
+            }
+            acc[q] = a;
+        }
+        __syncwarp();
+    }
+    for (int q = 0; q < 3; ++q) {
+        const int k = lane + 32 * q;
+        if (k < nc) Mexp[(int64_t)node * nc_pad + k] = acc[q];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// M2L fast path (FP32, compile-time order)
+// ---------------------------------------------------------------------------
+// Output split for the register budget: at high order the 45 accumulators,
+// the 45 source coefficients and one harmonics column do not fit in 255
+// registers together, so the target coefficients are divided by m-column
+// into two sets of nearly equal work (greedy on the per-column cost P+1-m)
+// and each set is computed by its own pass.  SET 0 = all columns.
+template <int P> __host__ __device__ constexpr bool m_in_set(int m, int set) {
+    if (set == 0) return true;
+    int wa = 0, wb = 0;
+    bool in_a = false;
+    for (int mm = 0; mm <= P; ++mm) {
+        const int w = P + 1 - mm;
+        const bool a = wa <= wb;
+        if (a)
+            wa += w;
+        else
+            wb += w;
+        if (mm == m) in_a = a;
+    }
+    return set == 1 ? in_a : !in_a;
+}
+template <int P> constexpr int m2l_passes() { return P >= 7 ? 2 : 1; }
+
+// One column mu of irregular harmonics and every (l, m) block that uses it;
+// mu is a template parameter so each column is straight-line code with
+// constant register indices.
+template <int P, int SET, int MU>
+__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float vx,
+                                           float vy, float vz, float ir2, float &dr, float &di, float (&Ar)[ncoef(P)],
+                                           float (&Ai)[ncoef(P)]) {
+    if constexpr (MU > 0) {
+        const float s = -(float)(2 * MU - 1) * ir2;
+        const float nr = s * (vx * dr - vy * di);
+        const float ni = s * (vx * di + vy * dr);
+        dr = nr;
+        di = ni;
+    }
+    float cr[2 * P + 1], ci[2 * P + 1];  // I_j^mu at [j], j >= mu
+#pragma unroll
+    for (int j = 0; j <= 2 * P; ++j) {
+        if (j == MU) {
+            cr[j] = dr;
+            ci[j] = di;
+        } else if (j == MU + 1) {
+            const float a = (float)(2 * j - 1) * vz * ir2;
+            cr[j] = a * cr[j - 1];
+            ci[j] = a * ci[j - 1];
+        } else if (j > MU + 1) {
+            const float a = (float)(2 * j - 1) * vz;
+            const float b = (float)((j - 1 + MU) * (j - 1 - MU));
+            cr[j] = (a * cr[j - 1] - b * cr[j - 2]) * ir2;
+            ci[j] = (a * ci[j - 1] - b * ci[j - 2]) * ir2;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m <= P; ++m) {
+        if (!m_in_set<P>(m, SET)) continue;
+#pragma unroll
+        for (int n = 0; n <= P; ++n) {
+#pragma unroll
+            for (int k = 0; k <= P; ++k) {
+                const int j = n + k;
+                // (l, m) with l - m = +mu, l >= 0
+                {
+                    const int l = m + MU;
+                    if (l <= P && n >= m && k >= l) {
+                        Ar[tri(n, m)] += mr[tri(k, l)] * cr[j] - mi[tri(k, l)] * ci[j];
+                        Ai[tri(n, m)] += mr[tri(k, l)] * ci[j] + mi[tri(k, l)] * cr[j];
+                    }
+                }
+                // (l, m) with l - m = -mu: I^{-mu} = (-1)^mu conj(I^mu)
+                if (MU > 0) {
+                    const int l = m - MU;
+                    const int al = l < 0 ? -l : l;
+                    if (al <= P && n >= m && k >= al) {
+                        const float xr = mr[tri(k, al)], xi = mi[tri(k, al)];
+                        if (l >= 0) {
+                            // (-1)^mu M conj(I)
+                            if (MU & 1) {
+                                Ar[tri(n, m)] -= xr * cr[j] + xi * ci[j];
+                                Ai[tri(n, m)] -= xi * cr[j] - xr * ci[j];
+                            } else {
+                                Ar[tri(n, m)] += xr * cr[j] + xi * ci[j];
+                                Ai[tri(n, m)] += xi * cr[j] - xr * ci[j];
+                            }
+                        } else {
+                            // (-1)^l conj(M) (-1)^mu conj(I) = (-1)^m conj(M I)
+                            if (m & 1) {
+                                Ar[tri(n, m)] -= xr * cr[j] - xi * ci[j];
+                                Ai[tri(n, m)] += xr * ci[j] + xi * cr[j];
+                            } else {
+                                Ar[tri(n, m)] += xr * cr[j] - xi * ci[j];
+                                Ai[tri(n, m)] -= xr * ci[j] + xi * cr[j];
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if constexpr (MU < 2 * P) m2l_column<P, SET, MU + 1>(mr, mi, vx, vy, vz, ir2, dr, di, Ar, Ai);
+}
+
+template <int P, int SET>
+__device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, float c, float vx, float vy, float vz,
+                                               float (&Ar)[ncoef(P)], float (&Ai)[ncoef(P)]) {
+    constexpr int NC = ncoef(P);
+    float mr[NC], mi[NC];
+#pragma unroll
+    for (int q = 0; q < (NC + 1) / 2; ++q) {
+        const float4 v = __ldg(M4 + q);
+        mr[2 * q] = v.x;
+        mi[2 * q] = v.y;
+        if (2 * q + 1 < NC) {
+            mr[2 * q + 1] = v.z;
+            mi[2 * q + 1] = v.w;
+        }
+    }
+    {
+        float ck = c;
+#pragma unroll
+        for (int k = 1; k <= P; ++k) {
+#pragma unroll
+            for (int l = 0; l <= P; ++l) {
+                if (l <= k) {
+                    mr[tri(k, l)] *= ck;
+                    mi[tri(k, l)] *= ck;
+                }
+            }
+            ck *= c;
+        }
+    }
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    const float ir2 = __frcp_rn(r2);
+    float dr = rsqrtf(r2), di = 0.0f;  // I_mu^mu, advanced column by column
+    m2l_column<P, SET, 0>(mr, mi, vx, vy, vz, ir2, dr, di, Ar, Ai);
+}
+
+template <int P, int SET>
+__global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
+                                                  const int32_t *__restrict__ src, const float4 *__restrict__ center,
+                                                  const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
+                                                  float2 *__restrict__ Lexp, int nc_pad) {
+    constexpr int NC = ncoef(P);
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= n_nodes) return;
+    const float4 ct = center[t];
+    const float aL = half[t].w;
+    const float iaL = 1.0f / aL;
+    float Ar[NC], Ai[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) Ar[k] = Ai[k] = 0.0f;
+    const int e = off[t + 1];
+    for (int k = off[t] + lane; k < e; k += 32) {
+        const int s = __ldg(src + k);
+        const float4 cs = __ldg(center + s);
+        const float c = __ldg(&half[s].w) * iaL;
+        if (c > kExtremeRatio) continue;  // translated by k_m2l_generic
+        m2l_accumulate<P, SET>(reinterpret_cast<const float4 *>(Mexp + (int64_t)s * nc_pad), c, (ct.x - cs.x) * iaL,
+                               (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL, Ar, Ai);
+    }
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > n || !m_in_set<P>(m, SET)) continue;
+            const int k = tri(n, m);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Ar[k] += __shfl_xor_sync(0xffffffffu, Ar[k], o);
+                Ai[k] += __shfl_xor_sync(0xffffffffu, Ai[k], o);
+            }
+        }
+    }
+    float2 *out = Lexp + t * nc_pad;
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > n || !m_in_set<P>(m, SET)) continue;
+            const int k = tri(n, m);
+            if ((k & 31) == lane) {
+                const float s = ((n + m) & 1) ? -iaL : iaL;
+                out[k] = make_float2(s * Ar[k], s * Ai[k]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// M2L generic path: any precision / order; warp per target row, lanes over
+// harmonics columns and output coefficients, operands in shared memory.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32_t *__restrict__ row_ids,
+                                                     const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+                                                     const typename Vec4<T>::type *__restrict__ center,
+                                                     const typename Vec4<T>::type *__restrict__ half,
+                                                     const Cplx<T> *__restrict__ Mexp, Cplx<T> *Lexp, int p, int nc_pad,
+                                                     int accumulate) {
+    __shared__ Cplx<T> sI[4][ncoef(2 * kPMax)];
+    __shared__ Cplx<T> sM[4][ncoef(kPMax)];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * 4 + wl;
+    if (w >= n_rows) return;
+    const int t = row_ids ? row_ids[w] : (int)w;
+    const int nc = ncoef(p);
+    const typename Vec4<T>::type ct = center[t];
+    const T aL = half[t].w;
+    Cplx<T> acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int k = off[t]; k < off[t + 1]; ++k) {
+        const int s = src[k];
+        const typename Vec4<T>::type cs = center[s];
+        const T aM = half[s].w, iaM = (T)1 / aM, f = aL * iaM;
+        const T vx = (ct.x - cs.x) * iaM, vy = (ct.y - cs.y) * iaM, vz = (ct.z - cs.z) * iaM;
+        const T r2 = vx * vx + vy * vy + vz * vz, ir2 = (T)1 / r2;
+        if (lane <= 2 * p) {
+            const int mu = lane;
+            T dr = (T)1 / sqrt(r2), di = (T)0;
+            for (int i = 1; i <= mu; ++i) {
+                const T sc = -(T)(2 * i - 1) * ir2;
+                const T nr = sc * (vx * dr - vy * di), ni = sc * (vx * di + vy * dr);
+                dr = nr;
+                di = ni;
+            }
+            sI[wl][tri(mu, mu)] = Cplx<T>{dr, di};
+            T pr = dr, pi = di, qr = 0, qi = 0;
+            for (int j = mu + 1; j <= 2 * p; ++j) {
+                const T a = (T)(2 * j - 1) * vz, b = (T)((j - 1 + mu) * (j - 1 - mu));
+                const T nr = (a * pr - b * qr) * ir2, ni = (a * pi - b * qi) * ir2;
+                sI[wl][tri(j, mu)] = Cplx<T>{nr, ni};
+                qr = pr;
+                qi = pi;
+                pr = nr;
+                pi = ni;
+            }
+        }
+        for (int c = lane; c < nc; c += 32) sM[wl][c] = Mexp[(int64_t)s * nc_pad + c];
+        __syncwarp();
+        for (int q = 0; q < 3; ++q) {
+            const int c = lane + 32 * q;
+            if (c >= nc) break;
+            int n, m;
+            coef_nm(c, n, m);
+            Cplx<T> sacc{0, 0};
+            for (int kk = 0; kk <= p; ++kk)
+                for (int l = -kk; l <= kk; ++l) {
+                    Cplx<T> v = cmul(harm_at(sM[wl], kk, l), harm_at(sI[wl], n + kk, l - m));
+                    sacc.re += v.re;
+                    sacc.im += v.im;
+                }
+            T fn = f;
+            for (int e = 0; e < n; ++e) fn *= f;
+            acc[q].re += fn * sacc.re;
+            acc[q].im += fn * sacc.im;
+        }
+        __syncwarp();
+    }
+    const T iaL = (T)1 / aL;
+    for (int q = 0; q < 3; ++q) {
+        const int c = lane + 32 * q;
+        if (c >= nc) break;
+        int n, m;
+        coef_nm(c, n, m);
+        const T sg = ((n + m) & 1) ? -iaL : iaL;
+        Cplx<T> v{sg * acc[q].re, sg * acc[q].im};
+        Cplx<T> *o = Lexp + (int64_t)t * nc_pad + c;
+        if (accumulate) {
+            v.re += o->re;
+            v.im += o->im;
+        }
+        *o = v;
+    }
+}
+
+// extreme pairs (source radius > 256x target radius) as a CSR by target
+__global__ void k_extreme_flags(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *half,
+                                int32_t *row_cnt) {
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= n_nodes) return;
+    const float iaL = 1.0f / half[t].w;
+    int c = 0;
+    for (int k = off[t] + lane; k < off[t + 1]; k += 32) c += (half[src[k]].w * iaL > kExtremeRatio) ? 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) row_cnt[t] = c;
+}
+__global__ void k_extreme_fill(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *half,
+                               const int32_t *eoff, int32_t *esrc) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_nodes) return;
+    const float iaL = 1.0f / half[t].w;
+    int j = eoff[t];
+    for (int k = off[t]; k < off[t + 1]; ++k)
+        if (half[src[k]].w * iaL > kExtremeRatio) esrc[j++] = src[k];
+}
+__global__ void k_set_last(int32_t *off, int64_t rows, const int64_t *total) { off[rows] = (int32_t)*total; }
+__global__ void k_nonempty_rows(int64_t n_nodes, const int32_t *cnt, const int32_t *pos, int32_t *rows) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_nodes && cnt[t] > 0) rows[pos[t]] = (int32_t)t;
+}
+__global__ void k_flag_nonzero(int64_t n, const int32_t *cnt, int32_t *flag) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) flag[t] = cnt[t] > 0;
+}
+
+// ---------------------------------------------------------------------------
+// L2L: warp per node of one level (level >= 1)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_l2l(const int32_t *__restrict__ nodes, int n_nodes,
+                                             const int32_t *__restrict__ parent,
+                                             const typename Vec4<T>::type *__restrict__ center,
+                                             const typename Vec4<T>::type *__restrict__ half, Cplx<T> *Lexp, int p,
+                                             int nc_pad) {
+    __shared__ Cplx<T> sR[4][ncoef(kPMax)], sL[4][ncoef(kPMax)];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 4 + wl;
+    if (w >= n_nodes) return;
+    const int node = nodes[w];
+    const int par = parent[node];
+    const int nc = ncoef(p);
+    const typename Vec4<T>::type cc = center[node], cp = center[par];
+    const T aP = half[par].w, iaP = (T)1 / aP, ratio = half[node].w * iaP;
+    if (lane == 0) regular_harmonics_rt<T>((cc.x - cp.x) * iaP, (cc.y - cp.y) * iaP, (cc.z - cp.z) * iaP, p, sR[wl]);
+    for (int k = lane; k < nc; k += 32) sL[wl][k] = Lexp[(int64_t)par * nc_pad + k];
+    __syncwarp();
+    for (int q = 0; q < 3; ++q) {
+        const int c = lane + 32 * q;
+        if (c >= nc) break;
+        int j, u;
+        coef_nm(c, j, u);
+        Cplx<T> a{0, 0};
+        for (int kk = 0; kk + j <= p; ++kk)
+            for (int l = -kk; l <= kk; ++l) {
+                const int nn = j + kk, mm = u + l;
+                if (mm < -nn || mm > nn) continue;
+                Cplx<T> v = cmul(harm_at(sL[wl], nn, mm), harm_at(sR[wl], kk, l));
+                a.re += v.re;
+                a.im += v.im;
+            }
+        T sc = (T)1;
+        for (int e = 0; e < j; ++e) sc *= ratio;
+        Cplx<T> *o = Lexp + (int64_t)node * nc_pad + c;
+        o->re += sc * a.re;
+        o->im += sc * a.im;
+    }
+}
+
+template <typename T> int p2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    if (tree.n_leaves == 0) return EDFMM_OK;
+    const unsigned grid = nblk(tree.n_leaves * 32, 128);
+#define EDFMM_P2M_CASE(PP)                                                                                          \
+    case PP:                                                                                                        \
+        k_p2m<T, PP><<<grid, 128, 0, s>>>(dptr<int32_t>(tree.leaves), tree.n_leaves, dptr<T4>(tree.pts),              \
+                                          dptr<T4>(tree.center), dptr<T4>(tree.half), dptr<int2>(tree.range),          \
+                                          dptr<Cplx<T>>(buf.multipoles), buf.nc_pad);                                \
+        break;
+    switch (buf.p) {
+        EDFMM_P2M_CASE(1)
+        EDFMM_P2M_CASE(2)
+        EDFMM_P2M_CASE(3)
+        EDFMM_P2M_CASE(4)
+        EDFMM_P2M_CASE(5)
+        EDFMM_P2M_CASE(6)
+        EDFMM_P2M_CASE(7)
+        EDFMM_P2M_CASE(8)
+        EDFMM_P2M_CASE(9)
+        EDFMM_P2M_CASE(10)
+        default:
+            return fail(EDFMM_ERR_UNSUPPORTED, "expansion order out of range");
+    }
+#undef EDFMM_P2M_CASE
+    EDFMM_LAUNCH_CHECK("k_p2m");
+    return EDFMM_OK;
+}
+
+template <typename T> int m2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    for (int lev = tree.max_level - 1; lev >= 0; --lev) {
+        const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
+        if (hi <= lo) continue;
+        k_m2m<T><<<nblk(hi - lo, 4), 128, 0, s>>>(dptr<int32_t>(tree.level_nodes) + lo, hi - lo, dptr<uint8_t>(tree.is_leaf),
+                                                  dptr<int32_t>(tree.children), dptr<T4>(tree.center), dptr<T4>(tree.half),
+                                                  dptr<Cplx<T>>(buf.multipoles), buf.p, buf.nc_pad);
+        EDFMM_LAUNCH_CHECK("k_m2m");
+    }
+    return EDFMM_OK;
+}
+
+template <typename T> int l2l_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    for (int lev = 1; lev <= tree.max_level; ++lev) {
+        const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
+        if (hi <= lo) continue;
+        k_l2l<T><<<nblk(hi - lo, 4), 128, 0, s>>>(dptr<int32_t>(tree.level_nodes) + lo, hi - lo, dptr<int32_t>(tree.parent),
+                                                  dptr<T4>(tree.center), dptr<T4>(tree.half), dptr<Cplx<T>>(buf.locals),
+                                                  buf.p, buf.nc_pad);
+        EDFMM_LAUNCH_CHECK("k_l2l");
+    }
+    return EDFMM_OK;
+}
+
+// extreme-pair CSR for one orientation (float plans only)
+int build_extreme(const DevTree &tree, const int32_t *off, const int32_t *src, ExtremeRows &ext, cudaStream_t s) {
+    int rc;
+    const int64_t M = tree.n_nodes;
+    DevBuf cnt, tmp, total, flag, pos;
+    if ((rc = cnt.reserve(sizeof(int32_t) * M)) || (rc = ext.off.reserve(sizeof(int32_t) * (M + 1))) ||
+        (rc = tmp.reserve(scan_tmp_bytes(M))) || (rc = total.reserve(sizeof(int64_t))))
+        return rc;
+    k_extreme_flags<<<nblk(M * 32, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<int32_t>(cnt));
+    EDFMM_LAUNCH_CHECK("k_extreme_flags");
+    if ((rc = scan_exclusive(dptr<int32_t>(cnt), dptr<int32_t>(ext.off), M, dptr<int64_t>(total), tmp.p, s))) return rc;
+    k_set_last<<<1, 1, 0, s>>>(dptr<int32_t>(ext.off), M, dptr<int64_t>(total));
+    EDFMM_LAUNCH_CHECK("k_set_last");
+    int64_t n_ext = 0;
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(&n_ext, total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    ext.n_pairs = n_ext;
+    ext.n_rows = 0;
+    ext.built = true;
+    if (n_ext == 0) return EDFMM_OK;
+    if ((rc = ext.src.reserve(sizeof(int32_t) * n_ext)) || (rc = flag.reserve(sizeof(int32_t) * M)) ||
+        (rc = pos.reserve(sizeof(int32_t) * M)) || (rc = ext.rows.reserve(sizeof(int32_t) * M)))
+        return rc;
+    k_extreme_fill<<<nblk(M, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<int32_t>(ext.off),
+                                                 dptr<int32_t>(ext.src));
+    EDFMM_LAUNCH_CHECK("k_extreme_fill");
+    k_flag_nonzero<<<nblk(M, 256), 256, 0, s>>>(M, dptr<int32_t>(cnt), dptr<int32_t>(flag));
+    EDFMM_LAUNCH_CHECK("k_flag_nonzero");
+    if ((rc = scan_exclusive(dptr<int32_t>(flag), dptr<int32_t>(pos), M, dptr<int64_t>(total), tmp.p, s))) return rc;
+    k_nonempty_rows<<<nblk(M, 256), 256, 0, s>>>(M, dptr<int32_t>(cnt), dptr<int32_t>(pos), dptr<int32_t>(ext.rows));
+    EDFMM_LAUNCH_CHECK("k_nonempty_rows");
+    int64_t nr = 0;
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(&nr, total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    ext.n_rows = nr;
+    return EDFMM_OK;
+}
+
+template <int P>
+void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const float4 *cen,
+                     const float4 *hal, const float2 *Mx, float2 *Lx, int nc_pad, cudaStream_t s) {
+    if constexpr (m2l_passes<P>() == 1) {
+        k_m2l_fast<P, 0><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+    } else {
+        k_m2l_fast<P, 1><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        count_launch();
+        k_m2l_fast<P, 2><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+    }
+}
+
+template <typename T>
+int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    const int64_t M = tree.n_nodes;
+    if (M == 0) return EDFMM_OK;
+    const int32_t *off = swapped ? dptr<int32_t>(lists.m2l_swapped_off) : dptr<int32_t>(lists.m2l_off);
+    const int32_t *src = swapped ? dptr<int32_t>(lists.m2l_swapped_src) : dptr<int32_t>(lists.m2l_src);
+    if (sizeof(T) == 8) {
+        k_m2l_generic<T><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, dptr<T4>(tree.center), dptr<T4>(tree.half),
+                                                    dptr<Cplx<T>>(buf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p,
+                                                    buf.nc_pad, 0);
+        EDFMM_LAUNCH_CHECK("k_m2l_generic");
+        return EDFMM_OK;
+    }
+    const unsigned grid = nblk(M * 32, 128);
+    const float4 *cen = dptr<float4>(tree.center), *hal = dptr<float4>(tree.half);
+    const float2 *Mx = dptr<float2>(buf.multipoles);
+    float2 *Lx = dptr<float2>(buf.locals);
+#define EDFMM_M2L_CASE(PP)                                                          \
+    case PP:                                                                        \
+        launch_m2l_fast<PP>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);    \
+        break;
+    switch (buf.p) {
+        EDFMM_M2L_CASE(1)
+        EDFMM_M2L_CASE(2)
+        EDFMM_M2L_CASE(3)
+        EDFMM_M2L_CASE(4)
+        EDFMM_M2L_CASE(5)
+        EDFMM_M2L_CASE(6)
+        EDFMM_M2L_CASE(7)
+        EDFMM_M2L_CASE(8)
+        default:
+            // orders above 8 would not fit the register-resident formulation
+            k_m2l_generic<float><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, cen, hal, dptr<Cplx<float>>(buf.multipoles),
+                                                            dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 0);
+            EDFMM_LAUNCH_CHECK("k_m2l_generic");
+            return EDFMM_OK;
+    }
+#undef EDFMM_M2L_CASE
+    EDFMM_LAUNCH_CHECK("k_m2l_fast");
+    ExtremeRows &ext = swapped ? buf.extreme_swapped : buf.extreme;
+    if (!ext.built) {
+        int rc = build_extreme(tree, off, src, ext, s);
+        if (rc) return rc;
+    }
+    if (ext.n_pairs > 0) {
+        k_m2l_generic<float><<<nblk(ext.n_rows, 4), 128, 0, s>>>(
+            ext.n_rows, dptr<int32_t>(ext.rows), dptr<int32_t>(ext.off), dptr<int32_t>(ext.src), cen, hal,
+            dptr<Cplx<float>>(buf.multipoles), dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 1);
+        EDFMM_LAUNCH_CHECK("k_m2l_generic");
+    }
+    return EDFMM_OK;
+}
+
+}  // namespace
+
+int set_charges(const DevTree &tree, const void *a, const void *b, cudaStream_t s) {
+    if (tree.n_points == 0) return EDFMM_OK;
+    if (tree.dtype == EDFMM_F64)
+        k_set_charges<double><<<nblk(tree.n_points, 256), 256, 0, s>>>(dptr<double4>(tree.pts), dptr<int32_t>(tree.index_map),
+                                                                      tree.n_points, static_cast<const double *>(a),
+                                                                      static_cast<const double *>(b));
+    else
+        k_set_charges<float><<<nblk(tree.n_points, 256), 256, 0, s>>>(dptr<float4>(tree.pts), dptr<int32_t>(tree.index_map),
+                                                                     tree.n_points, static_cast<const float *>(a),
+                                                                     static_cast<const float *>(b));
+    EDFMM_LAUNCH_CHECK("k_set_charges");
+    return EDFMM_OK;
+}
+
+int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? p2m_impl<double>(tree, buf, s) : p2m_impl<float>(tree, buf, s);
+}
+int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? m2m_impl<double>(tree, buf, s) : m2m_impl<float>(tree, buf, s);
+}
+int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? m2l_impl<double>(tree, lists, buf, swapped, s)
+                                   : m2l_impl<float>(tree, lists, buf, swapped, s);
+}
+int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? l2l_impl<double>(tree, buf, s) : l2l_impl<float>(tree, buf, s);
+}
+
+}  // namespace edfmm

@@ -1,0 +1,245 @@
+// Near field (P2P) fused with the local-expansion evaluation (L2P) and the
+// matvec epilogue.
+//
+// One warp owns one target leaf: each lane holds one target point (two when
+// the leaf has more than 32 points).  Source leaves of the target's P2P row
+// are staged 32 points at a time in shared memory as (x, y, z, q) and read by
+// broadcast, so every 16-byte load feeds 32 (or 64) interactions.  The kernel
+// is the reference's kernels_cpu.py:83-153 contribution
+//     q_s / max(|x_t - x_s|, eps)   (eps = machine epsilon of the dtype)
+// evaluated as q_s * rsqrt(max(r^2, eps^2)), with the diagonal dropped only
+// inside the self leaf pair.  The same warp then evaluates the leaf's local
+// expansion at its points and, for a full matvec, applies the epilogue of
+// bem_fmm.py:718-749 (K_E, original order, self term, non-finite -> 0), so
+// each output is written exactly once.
+#include <cfloat>
+
+#include "edfmm_internal.cuh"
+#include "harmonics.cuh"
+
+namespace edfmm {
+
+namespace {
+
+__constant__ float c_rdiv_f[kPMax + 1][kPMax + 1];
+__constant__ double c_rdiv_d[kPMax + 1][kPMax + 1];
+
+template <typename T> __device__ __forceinline__ T rdiv(int n, int m);
+template <> __device__ __forceinline__ float rdiv<float>(int n, int m) { return c_rdiv_f[n][m]; }
+template <> __device__ __forceinline__ double rdiv<double>(int n, int m) { return c_rdiv_d[n][m]; }
+
+__device__ __forceinline__ float inv_dist(float r2, float eps2) { return rsqrtf(fmaxf(r2, eps2)); }
+__device__ __forceinline__ double inv_dist(double r2, double eps2) { return rsqrt(fmax(r2, eps2)); }
+
+// Re sum_{n,m} L_n^m R_n^m(x, y, z) over m in [-n, n]
+template <typename T>
+__device__ __forceinline__ T l2p_point(const Cplx<T> *L, int p, T x, T y, T z) {
+    const T r2 = x * x + y * y + z * z;
+    T acc = (T)0, dr = (T)1, di = (T)0;
+    for (int m = 0; m <= p; ++m) {
+        if (m > 0) {
+            const T s = -(T)0.5 * rdiv<T>(m, 0) * (T)m;  // -1 / (2m): rdiv(m, 0) = 1 / m^2
+            const T nr = s * (x * dr - y * di), ni = s * (x * di + y * dr);
+            dr = nr;
+            di = ni;
+        }
+        const T w = m == 0 ? (T)1 : (T)2;
+        T pr = dr, pi = di, qr = (T)0, qi = (T)0;
+        Cplx<T> lv = L[tri(m, m)];
+        T col = lv.re * pr - lv.im * pi;
+        for (int n = m + 1; n <= p; ++n) {
+            const T d = rdiv<T>(n, m);
+            const T c1 = (T)(2 * n - 1) * z;
+            const T nr = (c1 * pr - r2 * qr) * d, ni = (c1 * pi - r2 * qi) * d;
+            lv = L[tri(n, m)];
+            col += lv.re * nr - lv.im * ni;
+            qr = pr;
+            qi = pi;
+            pr = nr;
+            pi = ni;
+        }
+        acc += w * col;
+    }
+    return acc;
+}
+
+template <typename T> struct NearParams {
+    const int32_t *leaves;
+    int64_t n_leaves;
+    const int32_t *off;
+    const int32_t *src;
+    const typename Vec4<T>::type *pts;
+    const int2 *range;
+    const typename Vec4<T>::type *center;
+    const typename Vec4<T>::type *half;
+    const Cplx<T> *Lexp;
+    int p;
+    int nc_pad;
+    T eps2;
+    int near;
+    int far;
+    // epilogue
+    int scatter;
+    const int32_t *index_map;
+    const T *sigma;
+    const T *areas;
+    const T *self_int;
+    T k_e;
+    T *out;
+};
+
+template <typename T, int TPL, bool SELF>
+__device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *sp, int cnt, int sbase,
+                                                 const typename Vec4<T>::type (&x)[2], const int (&ti)[2], T eps2,
+                                                 T (&acc)[2]) {
+#pragma unroll 8
+    for (int j = 0; j < cnt; ++j) {
+        const typename Vec4<T>::type q = sp[j];
+#pragma unroll
+        for (int u = 0; u < TPL; ++u) {
+            const T dx = x[u].x - q.x, dy = x[u].y - q.y, dz = x[u].z - q.z;
+            T inv = inv_dist(dx * dx + dy * dy + dz * dz, eps2);
+            if (SELF && sbase + j == ti[u]) inv = (T)0;
+            acc[u] += q.w * inv;
+        }
+    }
+}
+
+template <typename T, int TPL>
+__device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb, int te, typename Vec4<T>::type *sp,
+                                           const Cplx<T> *sL) {
+    using T4 = typename Vec4<T>::type;
+    const int lane = threadIdx.x & 31;
+    T4 x[2];
+    int ti[2];
+    bool valid[2];
+    T acc[2] = {(T)0, (T)0};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        ti[u] = tb + lane + 32 * u;
+        valid[u] = u < TPL && ti[u] < te;
+        x[u] = valid[u] ? P.pts[ti[u]] : P.pts[tb];
+    }
+    if (P.near) {
+        const int e = P.off[t + 1];
+        for (int k = P.off[t]; k < e; ++k) {
+            const int s = P.src[k];
+            const int2 sr = P.range[s];
+            for (int sb = sr.x; sb < sr.y; sb += 32) {
+                const int cnt = min(32, sr.y - sb);
+                __syncwarp();
+                if (lane < cnt) sp[lane] = P.pts[sb + lane];
+                __syncwarp();
+                if (s == t)
+                    accumulate_chunk<T, TPL, true>(sp, cnt, sb, x, ti, P.eps2, acc);
+                else
+                    accumulate_chunk<T, TPL, false>(sp, cnt, sb, x, ti, P.eps2, acc);
+            }
+        }
+    }
+    T4 c;
+    T ia = (T)1;
+    if (P.far) {
+        c = P.center[t];
+        ia = (T)1 / P.half[t].w;
+    }
+#pragma unroll
+    for (int u = 0; u < TPL; ++u) {
+        if (!valid[u]) continue;
+        T v = acc[u];
+        if (P.far) v += l2p_point<T>(sL, P.p, (x[u].x - c.x) * ia, (x[u].y - c.y) * ia, (x[u].z - c.z) * ia);
+        if (P.scatter) {
+            const int o = P.index_map[ti[u]];
+            v = v * P.k_e;
+            if (P.self_int) v += P.self_int[o] * P.sigma[o] * P.areas[o];
+            if (!isfinite(v)) v = (T)0;
+            P.out[o] = v;
+        } else {
+            P.out[ti[u]] = v;
+        }
+    }
+}
+
+template <typename T> __global__ void __launch_bounds__(128) k_p2p_l2p(const NearParams<T> P) {
+    using T4 = typename Vec4<T>::type;
+    __shared__ T4 sp[4][32];
+    __shared__ Cplx<T> sL[4][ncoef(kPMax)];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * 4 + wl;
+    if (w >= P.n_leaves) return;
+    const int t = P.leaves[w];
+    if (P.far) {
+        const int nc = ncoef(P.p);
+        for (int k = lane; k < nc; k += 32) sL[wl][k] = P.Lexp[(int64_t)t * P.nc_pad + k];
+        __syncwarp();
+    }
+    const int2 rg = P.range[t];
+    if (rg.y - rg.x <= 32) {
+        leaf_block<T, 1>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
+    } else {
+        for (int tb = rg.x; tb < rg.y; tb += 64) leaf_block<T, 2>(P, t, tb, min(rg.y, tb + 64), sp[wl], sL[wl]);
+    }
+}
+
+}  // namespace
+
+// 1 / ((n + m)(n - m)) tables (1 / n^2 at m = 0); __constant__ data lives in
+// each device context, so every plan creation uploads it on its device.
+int upload_tables() {
+    float hf[kPMax + 1][kPMax + 1];
+    double hd[kPMax + 1][kPMax + 1];
+    for (int n = 0; n <= kPMax; ++n)
+        for (int m = 0; m <= kPMax; ++m) {
+            int d = (n + m) * (n - m);
+            if (m == 0 && n > 0) d = n * n;
+            hd[n][m] = d != 0 ? 1.0 / d : 0.0;
+            hf[n][m] = (float)hd[n][m];
+        }
+    EDFMM_CUDA_TRY(cudaMemcpyToSymbol(c_rdiv_f, hf, sizeof(hf)));
+    EDFMM_CUDA_TRY(cudaMemcpyToSymbol(c_rdiv_d, hd, sizeof(hd)));
+    return EDFMM_OK;
+}
+
+namespace {
+
+template <typename T>
+int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf, const NearArgs &a, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    if (tree.n_leaves == 0) return EDFMM_OK;
+    NearParams<T> P;
+    P.leaves = dptr<int32_t>(tree.leaves);
+    P.n_leaves = tree.n_leaves;
+    P.off = dptr<int32_t>(lists.p2p_off);
+    P.src = dptr<int32_t>(lists.p2p_src);
+    P.pts = dptr<T4>(tree.pts);
+    P.range = dptr<int2>(tree.range);
+    P.center = dptr<T4>(tree.center);
+    P.half = dptr<T4>(tree.half);
+    P.Lexp = dptr<Cplx<T>>(buf.locals);
+    P.p = buf.p;
+    P.nc_pad = buf.nc_pad;
+    const T eps = sizeof(T) == 8 ? (T)DBL_EPSILON : (T)FLT_EPSILON;
+    P.eps2 = eps * eps;
+    P.near = a.near ? 1 : 0;
+    P.far = a.far ? 1 : 0;
+    P.scatter = a.scatter ? 1 : 0;
+    P.index_map = dptr<int32_t>(tree.index_map);
+    P.sigma = static_cast<const T *>(a.sigma);
+    P.areas = static_cast<const T *>(a.areas);
+    P.self_int = static_cast<const T *>(a.self_int);
+    P.k_e = (T)a.k_e;
+    P.out = static_cast<T *>(a.out);
+    k_p2p_l2p<T><<<(unsigned)((tree.n_leaves + 3) / 4), 128, 0, s>>>(P);
+    EDFMM_LAUNCH_CHECK("k_p2p_l2p");
+    return EDFMM_OK;
+}
+
+}  // namespace
+
+int run_p2p_l2p(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf, const NearArgs &args,
+                cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? near_impl<double>(tree, lists, buf, args, s)
+                                   : near_impl<float>(tree, lists, buf, args, s);
+}
+
+}  // namespace edfmm

@@ -1,0 +1,337 @@
+// C ABI of libedfmm: plan life cycle, exports and the matvec pipeline.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "edfmm_internal.cuh"
+#include "harmonics.cuh"
+
+namespace edfmm {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
+
+inline cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <typename T>
+__global__ void k_export_tree(int64_t M, int64_t N, const int32_t *idx, const typename Vec4<T>::type *center,
+                              const typename Vec4<T>::type *half, const int2 *range, const int32_t *parent,
+                              const int32_t *children, const int32_t *level, const uint8_t *leaf, int64_t *o_idx,
+                              T *o_c, T *o_h, T *o_r, int32_t *o_lev, int64_t *o_par, int64_t *o_ch, int64_t *o_rng,
+                              uint8_t *o_leaf) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o_idx && i < N) o_idx[i] = idx[i];
+    if (i >= M) return;
+    typename Vec4<T>::type c = center[i], h = half[i];
+    if (o_c) {
+        o_c[3 * i] = c.x;
+        o_c[3 * i + 1] = c.y;
+        o_c[3 * i + 2] = c.z;
+    }
+    if (o_h) {
+        o_h[3 * i] = h.x;
+        o_h[3 * i + 1] = h.y;
+        o_h[3 * i + 2] = h.z;
+    }
+    if (o_r) o_r[i] = c.w;
+    if (o_lev) o_lev[i] = level[i];
+    if (o_par) o_par[i] = parent[i];
+    if (o_ch)
+        for (int o = 0; o < 8; ++o) o_ch[8 * i + o] = children[8 * i + o];
+    if (o_rng) {
+        o_rng[2 * i] = range[i].x;
+        o_rng[2 * i + 1] = range[i].y;
+    }
+    if (o_leaf) o_leaf[i] = leaf[i];
+}
+
+__global__ void k_export_pairs(int64_t rows, const int32_t *off, const int32_t *src, int64_t *out) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.y + threadIdx.y;
+    if (r >= rows) return;
+    for (int k = off[r] + threadIdx.x; k < off[r + 1]; k += blockDim.x) {
+        out[2 * (int64_t)k] = src[k];
+        out[2 * (int64_t)k + 1] = r;
+    }
+}
+
+template <typename T>
+__global__ void k_export_coeffs(int64_t M, int nc, int nc_pad, const Cplx<T> *in, Cplx<T> *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * nc) return;
+    int64_t node = i / nc;
+    int c = (int)(i % nc);
+    out[i] = in[node * nc_pad + c];
+}
+
+int check_plan(const edfmm_plan *p) {
+    if (!p) return fail(EDFMM_ERR_ARG, "plan is NULL");
+    return EDFMM_OK;
+}
+
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+}  // namespace edfmm
+
+using namespace edfmm;
+
+extern "C" {
+
+const char *edfmm_last_error(void) { return g_last_error.c_str(); }
+
+const char *edfmm_version(void) { return "edfmm 0.1 (sm_103a)"; }
+
+int64_t edfmm_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth, double mac_theta,
+                      int expansion_order, void *stream, edfmm_plan **plan_out) {
+    if (!plan_out) return fail(EDFMM_ERR_ARG, "plan_out is NULL");
+    *plan_out = nullptr;
+    if (n < 0) return fail(EDFMM_ERR_ARG, "n must be >= 0");
+    if (n > 0 && !points_dev) return fail(EDFMM_ERR_ARG, "points_dev is NULL");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (leaf_size <= 0) return fail(EDFMM_ERR_ARG, "leaf_size must be positive");
+    if (max_depth <= 0 || max_depth > 64) return fail(EDFMM_ERR_ARG, "max_depth must be in [1, 64]");
+    if (!(mac_theta > 0.0 && mac_theta < 1.0)) return fail(EDFMM_ERR_ARG, "mac_theta must be in (0, 1)");
+    if (expansion_order < 1 || expansion_order > 10)
+        return fail(EDFMM_ERR_UNSUPPORTED, "expansion_order must be in [1, 10]");
+    int rc = upload_tables();
+    if (rc) return rc;
+    edfmm_plan *p = new edfmm_plan();
+    cudaGetDevice(&p->device);
+    p->mac_theta = mac_theta;
+    p->leaf_size = leaf_size;
+    p->max_depth = max_depth;
+    cudaStream_t s = S(stream);
+    rc = tree_build(points_dev, n, dtype, leaf_size, max_depth, p->tree, s);
+    if (!rc) rc = lists_build(p->tree, mac_theta, p->lists, s);
+    if (!rc) {
+        p->fmm.p = expansion_order;
+        p->fmm.nc = num_coeffs(expansion_order);
+        p->fmm.nc_pad = (p->fmm.nc + 1) & ~1;
+        size_t esz = (dtype == EDFMM_F64 ? 16 : 8) * (size_t)p->fmm.nc_pad * (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
+        rc = p->fmm.multipoles.reserve(esz);
+        if (!rc) rc = p->fmm.locals.reserve(esz);
+        if (!rc) {
+            cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("plan set-up: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *plan_out = p;
+    return EDFMM_OK;
+}
+
+int edfmm_plan_destroy(edfmm_plan *plan) {
+    delete plan;
+    return EDFMM_OK;
+}
+
+int edfmm_plan_rebuild_lists(edfmm_plan *p, double mac_theta, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (!(mac_theta > 0.0 && mac_theta < 1.0)) return fail(EDFMM_ERR_ARG, "mac_theta must be in (0, 1)");
+    if (mac_theta == p->mac_theta) return EDFMM_OK;
+    if (int rc = lists_build(p->tree, mac_theta, p->lists, S(stream))) return rc;
+    p->mac_theta = mac_theta;
+    p->fmm.extreme = ExtremeRows();
+    p->fmm.extreme_swapped = ExtremeRows();
+    return EDFMM_OK;
+}
+
+int edfmm_plan_set_order(edfmm_plan *p, int expansion_order, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (expansion_order < 1 || expansion_order > 10)
+        return fail(EDFMM_ERR_UNSUPPORTED, "expansion_order must be in [1, 10]");
+    if (expansion_order == p->fmm.p) return EDFMM_OK;
+    cudaStream_t s = S(stream);
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    p->fmm.p = expansion_order;
+    p->fmm.nc = num_coeffs(expansion_order);
+    p->fmm.nc_pad = (p->fmm.nc + 1) & ~1;
+    size_t esz = (p->tree.dtype == EDFMM_F64 ? 16 : 8) * (size_t)p->fmm.nc_pad *
+                 (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
+    p->fmm.multipoles.release();
+    p->fmm.locals.release();
+    int rc = p->fmm.multipoles.reserve(esz);
+    if (!rc) rc = p->fmm.locals.reserve(esz);
+    if (rc) return rc;
+    EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s));
+    EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.locals.p, 0, esz, s));
+    return EDFMM_OK;
+}
+
+int edfmm_plan_get_info(const edfmm_plan *p, edfmm_plan_info *info) {
+    if (int rc = check_plan(p)) return rc;
+    if (!info) return fail(EDFMM_ERR_ARG, "info is NULL");
+    std::memset(info, 0, sizeof(*info));
+    info->n_points = p->tree.n_points;
+    info->n_nodes = p->tree.n_nodes;
+    info->n_leaves = p->tree.n_leaves;
+    info->n_p2p_pairs = p->lists.n_p2p;
+    info->n_m2l_pairs = p->lists.n_m2l;
+    info->p2p_interactions = p->lists.p2p_interactions;
+    info->max_level = p->tree.max_level;
+    info->depth_warnings = p->tree.depth_warnings;
+    info->dtype = p->tree.dtype;
+    info->expansion_order = p->fmm.p;
+    info->leaf_size = p->leaf_size;
+    info->max_depth = p->max_depth;
+    info->mac_theta = p->mac_theta;
+    return EDFMM_OK;
+}
+
+int edfmm_plan_export_tree(const edfmm_plan *p, int64_t *index_map, void *centers, void *half_extents, void *radii,
+                           int32_t *levels, int64_t *parents, int64_t *children, int64_t *ranges, uint8_t *is_leaf,
+                           void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    const DevTree &t = p->tree;
+    int64_t n = std::max(t.n_nodes, t.n_points);
+    if (n == 0) return EDFMM_OK;
+    if (t.dtype == EDFMM_F64)
+        k_export_tree<double><<<nblk(n, 256), 256, 0, S(stream)>>>(
+            t.n_nodes, t.n_points, dptr<int32_t>(t.index_map), dptr<double4>(t.center), dptr<double4>(t.half),
+            dptr<int2>(t.range), dptr<int32_t>(t.parent), dptr<int32_t>(t.children), dptr<int32_t>(t.level),
+            dptr<uint8_t>(t.is_leaf), index_map, static_cast<double *>(centers), static_cast<double *>(half_extents),
+            static_cast<double *>(radii), levels, parents, children, ranges, is_leaf);
+    else
+        k_export_tree<float><<<nblk(n, 256), 256, 0, S(stream)>>>(
+            t.n_nodes, t.n_points, dptr<int32_t>(t.index_map), dptr<float4>(t.center), dptr<float4>(t.half),
+            dptr<int2>(t.range), dptr<int32_t>(t.parent), dptr<int32_t>(t.children), dptr<int32_t>(t.level),
+            dptr<uint8_t>(t.is_leaf), index_map, static_cast<float *>(centers), static_cast<float *>(half_extents),
+            static_cast<float *>(radii), levels, parents, children, ranges, is_leaf);
+    EDFMM_LAUNCH_CHECK("k_export_tree");
+    return EDFMM_OK;
+}
+
+int edfmm_plan_export_lists(const edfmm_plan *p, int64_t *p2p_pairs, int64_t *m2l_pairs, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    const int64_t M = p->tree.n_nodes;
+    if (M == 0) return EDFMM_OK;
+    dim3 blk(32, 8);
+    if (p2p_pairs && p->lists.n_p2p > 0) {
+        k_export_pairs<<<nblk(M, 8), blk, 0, S(stream)>>>(M, dptr<int32_t>(p->lists.p2p_off),
+                                                           dptr<int32_t>(p->lists.p2p_src), p2p_pairs);
+        EDFMM_LAUNCH_CHECK("k_export_pairs");
+    }
+    if (m2l_pairs && p->lists.n_m2l > 0) {
+        k_export_pairs<<<nblk(M, 8), blk, 0, S(stream)>>>(M, dptr<int32_t>(p->lists.m2l_off),
+                                                           dptr<int32_t>(p->lists.m2l_src), m2l_pairs);
+        EDFMM_LAUNCH_CHECK("k_export_pairs");
+    }
+    return EDFMM_OK;
+}
+
+int edfmm_plan_get_expansions(const edfmm_plan *p, void *multipoles, void *locals, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    const int64_t M = p->tree.n_nodes;
+    const int nc = p->fmm.nc;
+    if (M == 0) return EDFMM_OK;
+    for (int k = 0; k < 2; ++k) {
+        void *dst = k == 0 ? multipoles : locals;
+        if (!dst) continue;
+        const DevBuf &src = k == 0 ? p->fmm.multipoles : p->fmm.locals;
+        if (p->tree.dtype == EDFMM_F64)
+            k_export_coeffs<double><<<nblk(M * nc, 256), 256, 0, S(stream)>>>(M, nc, p->fmm.nc_pad, dptr<Cplx<double>>(src),
+                                                                              static_cast<Cplx<double> *>(dst));
+        else
+            k_export_coeffs<float><<<nblk(M * nc, 256), 256, 0, S(stream)>>>(M, nc, p->fmm.nc_pad, dptr<Cplx<float>>(src),
+                                                                             static_cast<Cplx<float> *>(dst));
+        EDFMM_LAUNCH_CHECK("k_export_coeffs");
+    }
+    return EDFMM_OK;
+}
+
+int edfmm_plan_set_charges(edfmm_plan *p, const void *charges, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (p->tree.n_points > 0 && !charges) return fail(EDFMM_ERR_ARG, "charges is NULL");
+    return set_charges(p->tree, charges, nullptr, S(stream));
+}
+
+int edfmm_plan_p2m(edfmm_plan *p, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    return run_p2m(p->tree, p->fmm, S(stream));
+}
+
+int edfmm_plan_m2m(edfmm_plan *p, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    return run_m2m(p->tree, p->fmm, S(stream));
+}
+
+int edfmm_plan_m2l(edfmm_plan *p, int flags, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    const bool swapped = (flags & EDFMM_REFERENCE_PAIR_ORDER) != 0;
+    if (swapped) {
+        if (int rc = lists_build_swapped(p->tree, p->lists, S(stream))) return rc;
+    }
+    return run_m2l(p->tree, p->lists, p->fmm, swapped, S(stream));
+}
+
+int edfmm_plan_l2l(edfmm_plan *p, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    return run_l2l(p->tree, p->fmm, S(stream));
+}
+
+int edfmm_plan_l2p(edfmm_plan *p, void *phi_far_tree, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (p->tree.n_points > 0 && !phi_far_tree) return fail(EDFMM_ERR_ARG, "output is NULL");
+    NearArgs a;
+    a.out = phi_far_tree;
+    a.near = false;
+    a.far = true;
+    return run_p2p_l2p(p->tree, p->lists, p->fmm, a, S(stream));
+}
+
+int edfmm_plan_p2p(edfmm_plan *p, void *phi_near_tree, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (p->tree.n_points > 0 && !phi_near_tree) return fail(EDFMM_ERR_ARG, "output is NULL");
+    NearArgs a;
+    a.out = phi_near_tree;
+    a.near = true;
+    a.far = false;
+    return run_p2p_l2p(p->tree, p->lists, p->fmm, a, S(stream));
+}
+
+int edfmm_plan_matvec(edfmm_plan *p, const void *sigma, const void *areas, const void *self_integrals, double k_e,
+                      void *out, int flags, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (p->tree.n_points == 0) return EDFMM_OK;
+    if (!sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "sigma, areas and out must be non-NULL");
+    cudaStream_t s = S(stream);
+    const bool far = (flags & EDFMM_NO_FARFIELD) == 0;
+    const bool near = (flags & EDFMM_NO_NEARFIELD) == 0;
+    const bool swapped = (flags & EDFMM_REFERENCE_PAIR_ORDER) != 0;
+    int rc;
+    if (swapped && (rc = lists_build_swapped(p->tree, p->lists, s))) return rc;
+    if ((rc = set_charges(p->tree, sigma, areas, s))) return rc;
+    if (far) {
+        if ((rc = run_p2m(p->tree, p->fmm, s)) || (rc = run_m2m(p->tree, p->fmm, s)) ||
+            (rc = run_m2l(p->tree, p->lists, p->fmm, swapped, s)) || (rc = run_l2l(p->tree, p->fmm, s)))
+            return rc;
+    }
+    NearArgs a;
+    a.sigma = sigma;
+    a.areas = areas;
+    a.self_int = self_integrals;
+    a.k_e = k_e;
+    a.out = out;
+    a.scatter = true;
+    a.near = near;
+    a.far = far;
+    return run_p2p_l2p(p->tree, p->lists, p->fmm, a, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,179 @@
+/*
+ * edfmm.h -- C ABI of the GB300-native FMM-accelerated Laplace single-layer
+ * BEM operator (libedfmm.so).
+ *
+ * Conventions
+ *   - Every pointer argument named *_dev is a device pointer on the current
+ *     CUDA device; host pointers are named *_host.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     All work is stream-ordered; functions that must size device buffers from
+ *     device results (plan creation) synchronise `stream` internally.
+ *   - `dtype` is EDFMM_F32 or EDFMM_F64 and applies to every floating-point
+ *     array of the call.
+ *   - Return value: EDFMM_OK (0), a negative code for argument / CUDA /
+ *     allocation errors, or a positive code for a numerical condition.
+ *     edfmm_last_error() returns a human-readable message for the calling
+ *     thread's most recent failure.
+ *
+ * Each entry point cites the reference interface it replaces (paths inside
+ * the reference project).
+ */
+#ifndef EDFMM_H
+#define EDFMM_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define EDFMM_API __attribute__((visibility("default")))
+#else
+#define EDFMM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDFMM_OK 0
+#define EDFMM_ERR_ARG (-1)
+#define EDFMM_ERR_CUDA (-2)
+#define EDFMM_ERR_ALLOC (-3)
+#define EDFMM_ERR_UNSUPPORTED (-4)
+#define EDFMM_ERR_STATE (-5)
+
+#define EDFMM_F32 0
+#define EDFMM_F64 1
+
+/* matvec flags */
+#define EDFMM_REFERENCE_PAIR_ORDER 1 /* apply listed (src, tgt) M2L pairs as L[src] += T M[tgt],
+                                        the reference's unpacking (multipole_operators.py:1671) */
+#define EDFMM_NO_FARFIELD 2          /* near field only (P2P) */
+#define EDFMM_NO_NEARFIELD 4         /* far field only (P2M..L2P) */
+
+typedef struct edfmm_plan edfmm_plan;
+
+typedef struct {
+    int64_t n_points;
+    int64_t n_nodes;
+    int64_t n_leaves;
+    int64_t n_p2p_pairs;
+    int64_t n_m2l_pairs;
+    int64_t p2p_interactions;  /* sum over P2P pairs of n_src * n_tgt */
+    int32_t max_level;
+    int32_t depth_warnings;    /* leaves cut by max_depth above leaf_size (tree.py:899-908) */
+    int32_t dtype;
+    int32_t expansion_order;
+    int32_t leaf_size;
+    int32_t max_depth;
+    double mac_theta;
+} edfmm_plan_info;
+
+/* Thread-local description of the most recent failure. */
+EDFMM_API const char *edfmm_last_error(void);
+
+/* Library version string. */
+EDFMM_API const char *edfmm_version(void);
+
+/*
+ * Build the adaptive octree and the dual-tree interaction lists on the GPU
+ * and allocate every buffer a matvec needs.  Replaces the geometry set-up of
+ * LaplaceFmm3D.__init__ (electrodrive/fmm3d/bem_fmm.py:127-302), i.e.
+ * build_fmm_tree (electrodrive/fmm3d/tree.py:968-1050) followed by
+ * build_interaction_lists (electrodrive/fmm3d/interaction_lists.py:531-577).
+ * points_dev: (n, 3) row-major in `dtype`.  Tree and lists are bit-identical
+ * to the reference's for the same inputs.
+ */
+EDFMM_API int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth,
+                      double mac_theta, int expansion_order, void *stream, edfmm_plan **plan_out);
+
+EDFMM_API int edfmm_plan_destroy(edfmm_plan *plan);
+
+/*
+ * Rebuild the interaction lists of an existing plan for another MAC
+ * parameter (build_interaction_lists(tree, tree, mac_theta=...),
+ * electrodrive/fmm3d/interaction_lists.py:531-577).
+ */
+EDFMM_API int edfmm_plan_rebuild_lists(edfmm_plan *plan, double mac_theta, void *stream);
+
+/*
+ * Change the expansion order p (FmmConfig.expansion_order,
+ * electrodrive/fmm3d/config.py:90-106); reallocates the expansion buffers.
+ */
+EDFMM_API int edfmm_plan_set_order(edfmm_plan *plan, int expansion_order, void *stream);
+
+EDFMM_API int edfmm_plan_get_info(const edfmm_plan *plan, edfmm_plan_info *info_out);
+
+/*
+ * Copy the tree into caller buffers in the reference's SoA layout
+ * (FmmTree._build_soa, electrodrive/fmm3d/tree.py:286-348).  Any pointer may
+ * be NULL.  Float arrays are in the plan dtype; centers/half_extents (M,3),
+ * children (M,8) with -1 for a missing child, ranges (M,2) [start, end).
+ */
+EDFMM_API int edfmm_plan_export_tree(const edfmm_plan *plan, int64_t *index_map_dev, void *centers_dev,
+                           void *half_extents_dev, void *radii_dev, int32_t *levels_dev,
+                           int64_t *parents_dev, int64_t *children_dev, int64_t *ranges_dev,
+                           uint8_t *is_leaf_dev, void *stream);
+
+/*
+ * Copy the interaction lists as (src, tgt) pairs sorted by (tgt, src), the
+ * InteractionLists.p2p_pairs / m2l_pairs order
+ * (electrodrive/fmm3d/interaction_lists.py:474-485).  Either pointer may be NULL.
+ */
+EDFMM_API int edfmm_plan_export_lists(const edfmm_plan *plan, int64_t *p2p_pairs_dev, int64_t *m2l_pairs_dev,
+                            void *stream);
+
+/*
+ * The single-layer operator, LaplaceFmm3D.matvec
+ * (electrodrive/fmm3d/bem_fmm.py:760-885, GPU body :596-754):
+ *   q = sigma * areas; V = k_e * (phi_far + phi_near) in original order;
+ *   V += self_integrals * sigma * areas when self_integrals_dev != NULL;
+ *   non-finite entries of V -> 0.
+ * sigma/areas/self_integrals/out: (n,) original order, plan dtype.
+ * Allocates nothing; safe to call repeatedly on the same stream.
+ */
+EDFMM_API int edfmm_plan_matvec(edfmm_plan *plan, const void *sigma_dev, const void *areas_dev,
+                      const void *self_integrals_dev, double k_e, void *out_dev, int flags,
+                      void *stream);
+
+/*
+ * Stage entry points on the plan's own expansion buffers, mirroring the
+ * tree-level operators p2m / m2m / m2l / l2l / l2p
+ * (electrodrive/fmm3d/multipole_operators.py:1520-1765) and the near field
+ * apply_p2p_gpu (electrodrive/fmm3d/kernels_gpu.py:242-274).
+ * charges_dev: (n,) in ORIGINAL order.  phi_*_tree_dev: (n,) in TREE order,
+ * pure 1/r kernel (no k_e).
+ */
+EDFMM_API int edfmm_plan_set_charges(edfmm_plan *plan, const void *charges_dev, void *stream);
+EDFMM_API int edfmm_plan_p2m(edfmm_plan *plan, void *stream);
+EDFMM_API int edfmm_plan_m2m(edfmm_plan *plan, void *stream);
+EDFMM_API int edfmm_plan_m2l(edfmm_plan *plan, int flags, void *stream);
+EDFMM_API int edfmm_plan_l2l(edfmm_plan *plan, void *stream);
+EDFMM_API int edfmm_plan_l2p(edfmm_plan *plan, void *phi_far_tree_dev, void *stream);
+EDFMM_API int edfmm_plan_p2p(edfmm_plan *plan, void *phi_near_tree_dev, void *stream);
+
+/*
+ * Expansion coefficients, packed (n_nodes, (p+1)(p+2)/2) complex (re, im
+ * interleaved, plan dtype), m >= 0 only, index (n, m) -> n(n+1)/2 + m.
+ * Coefficients use complex solid harmonics with the Condon-Shortley phase,
+ * scaled by the node radius a: Mhat_n^m = M_n^m / a^n, Lhat_n^m = L_n^m a^n.
+ */
+EDFMM_API int edfmm_plan_get_expansions(const edfmm_plan *plan, void *multipoles_dev, void *locals_dev,
+                              void *stream);
+
+/*
+ * Number of the library's own kernel launches issued since load (all
+ * threads).  Used by benchmarks to report launches inside a timed region.
+ */
+EDFMM_API int64_t edfmm_launch_count(void);
+
+/*
+ * Measured FP32 FMA throughput of the current device in TFLOP/s (an FMA
+ * counts as 2 flops): the roofline denominator of the FP32-bound FMM stages.
+ * No counterpart in the reference (it has no GPU kernels for the FMM).
+ */
+EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EDFMM_H */

@@ -1,0 +1,144 @@
+"""Write the golden fixtures in this folder by running the reference itself.
+
+Run in a checkout where the reference project is importable, e.g.::
+
+    REFERENCE_ROOT=/root/reference python tests/golden/make_golden.py
+
+Nothing at test time imports the reference; the tests read only the .npz
+files written here.  Each fixture records which reference routine produced
+it (paths inside the reference project):
+
+* ``tree_*.npz``   -- ``electrodrive/fmm3d/tree.py:968`` ``build_fmm_tree`` SoA
+  and ``electrodrive/fmm3d/interaction_lists.py:531`` ``build_interaction_lists``
+  pairs, plus ``electrodrive/fmm3d/kernels_cpu.py:183`` ``apply_p2p_cpu_tiled``
+  potentials for seeded charges.
+* ``fmm_*.npz``    -- ``electrodrive/fmm3d/bem_fmm.py:888``
+  ``make_laplace_fmm_backend(...).matvec`` (CPU) next to
+  ``electrodrive/core/bem_kernel.py:558`` ``bem_matvec_gpu(backend="torch_tiled")``.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+sys.path.insert(0, REF)
+os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
+sys.dont_write_bytecode = True
+
+import torch  # noqa: E402
+
+from electrodrive.fmm3d.tree import build_fmm_tree  # noqa: E402
+from electrodrive.fmm3d.interaction_lists import build_interaction_lists  # noqa: E402
+from electrodrive.fmm3d.kernels_cpu import apply_p2p_cpu_tiled  # noqa: E402
+
+
+def gen_points(kind: str, n: int, seed: int, dtype) -> torch.Tensor:
+    g = torch.Generator().manual_seed(seed)
+    if kind == "uniform":
+        p = torch.rand(n, 3, generator=g, dtype=torch.float64)
+    elif kind == "clusters":
+        # two tight Gaussian clusters plus a sparse uniform background
+        a = 0.02 * torch.randn(n // 2, 3, generator=g, dtype=torch.float64) + 0.25
+        b = 0.05 * torch.randn(n // 3, 3, generator=g, dtype=torch.float64) + torch.tensor([0.8, 0.7, 0.3], dtype=torch.float64)
+        c = torch.rand(n - a.shape[0] - b.shape[0], 3, generator=g, dtype=torch.float64)
+        p = torch.cat([a, b, c])
+    elif kind == "lattice":
+        # many points exactly on splitting planes and duplicated coordinates
+        k = int(round(n ** (1.0 / 3.0))) + 1
+        ix = torch.randint(0, k, (n, 3), generator=g)
+        p = ix.to(torch.float64) / (k - 1)
+    elif kind == "coincident":
+        # blocks of exactly coincident points (degenerate boxes)
+        base = torch.rand(n // 40 + 1, 3, generator=g, dtype=torch.float64)
+        p = base.repeat_interleave(40, dim=0)[:n].clone()
+        p[::7] += 1e-9  # some nearly coincident
+    elif kind == "sphere":
+        v = torch.randn(n, 3, generator=g, dtype=torch.float64)
+        p = v / v.norm(dim=1, keepdim=True)
+    else:
+        raise ValueError(kind)
+    return p.to(dtype)
+
+
+def save_tree_case(name, kind, n, seed, dtype, leaf, theta, max_depth=32):
+    pts = gen_points(kind, n, seed, dtype)
+    t0 = time.time()
+    tree = build_fmm_tree(pts, leaf_size=leaf, max_depth=max_depth)
+    lists = build_interaction_lists(tree, tree, mac_theta=theta)
+    g = torch.Generator().manual_seed(seed + 100)
+    q = (2 * torch.rand(n, generator=g, dtype=torch.float64) - 1).to(dtype)
+    q_tree = tree.map_to_tree_order(q)
+    res = apply_p2p_cpu_tiled(tree, tree, q_tree, lists)
+    p2p = np.asarray(lists.p2p_pairs, dtype=np.int32).reshape(-1, 2)
+    m2l = np.asarray(lists.m2l_pairs, dtype=np.int32).reshape(-1, 2)
+    np.savez_compressed(
+        os.path.join(HERE, f"tree_{name}.npz"),
+        kind=kind, n=n, seed=seed, leaf_size=leaf, max_depth=max_depth, theta=theta,
+        dtype=str(dtype).replace("torch.", ""),
+        points=pts.numpy(),
+        charges=q.numpy(),
+        index_map=tree.index_map.numpy().astype(np.int32),
+        node_centers=tree.node_centers.numpy(),
+        node_half_extents=tree.node_half_extents.numpy(),
+        node_radii=tree.node_radii.numpy(),
+        node_levels=tree.node_levels.numpy(),
+        node_parents=tree.node_parents.numpy().astype(np.int32),
+        node_children=tree.node_children.numpy().astype(np.int32),
+        node_ranges=tree.node_ranges.numpy().astype(np.int32),
+        node_is_leaf=tree.node_is_leaf.numpy(),
+        p2p_pairs=p2p,
+        m2l_pairs=m2l,
+        p2p_potential_tree=res.potential.numpy(),
+        p2p_n_interactions=res.n_interactions,
+    )
+    print(f"tree_{name}: N={n} nodes={tree.n_nodes} p2p={len(p2p)} m2l={len(m2l)} ({time.time() - t0:.1f}s)")
+
+
+def save_fmm_case(name, n, seed, dtype, leaf, theta, p):
+    from electrodrive.fmm3d.bem_fmm import make_laplace_fmm_backend
+    from electrodrive.core.bem_kernel import bem_matvec_gpu
+
+    pts = gen_points("uniform", n, seed, dtype)
+    g = torch.Generator().manual_seed(seed + 200)
+    sigma = (2 * torch.rand(n, generator=g, dtype=torch.float64) - 1).to(dtype)
+    areas = (0.5 + torch.rand(n, generator=g, dtype=torch.float64)).to(dtype) * 1e-3
+    self_int = (torch.rand(n, generator=g, dtype=torch.float64) * 1e10).to(dtype)
+    t0 = time.time()
+    fmm = make_laplace_fmm_backend(pts, areas, max_leaf_size=leaf, theta=theta, expansion_order=p, backend="cpu")
+    v_fmm = fmm.matvec(sigma=sigma, src_centroids=pts, areas=areas, tile_size=1024, self_integrals=self_int)
+    t1 = time.time()
+    v_dense = bem_matvec_gpu(sigma, pts, areas, tile_size=1024, self_integrals=self_int, backend="torch_tiled")
+    np.savez_compressed(
+        os.path.join(HERE, f"fmm_{name}.npz"),
+        n=n, seed=seed, leaf_size=leaf, theta=theta, p=p, dtype=str(dtype).replace("torch.", ""),
+        points=pts.numpy(), sigma=sigma.numpy(), areas=areas.numpy(), self_integrals=self_int.numpy(),
+        v_fmm_reference=v_fmm.numpy(), v_dense_reference=v_dense.numpy(),
+        reference_seconds_per_matvec=t1 - t0,
+    )
+    rel = float((v_fmm - v_dense).norm() / v_dense.norm())
+    print(f"fmm_{name}: N={n} ref-FMM vs dense rel-L2 {rel:.3e} ({t1 - t0:.1f}s per matvec incl. setup)")
+
+
+def main():
+    which = sys.argv[1:] or ["trees", "fmm"]
+    if "trees" in which:
+        save_tree_case("uniform4096_f32", "uniform", 4096, 0, torch.float32, 64, 0.5)
+        save_tree_case("clusters3000_f32", "clusters", 3000, 1, torch.float32, 32, 0.5)
+        save_tree_case("lattice2000_f32", "lattice", 2000, 2, torch.float32, 16, 0.5)
+        save_tree_case("coincident1200_f32", "coincident", 1200, 3, torch.float32, 8, 0.5)
+        save_tree_case("sphere2500_f64", "sphere", 2500, 4, torch.float64, 24, 0.6)
+        save_tree_case("uniform1500_theta03_f32", "uniform", 1500, 5, torch.float32, 20, 0.3)
+        save_tree_case("deep_maxdepth3_f32", "clusters", 2000, 6, torch.float32, 4, 0.5, max_depth=3)
+        save_tree_case("tiny5_f32", "uniform", 5, 7, torch.float32, 64, 0.5)
+    if "fmm" in which:
+        save_fmm_case("uniform512_f32", 512, 10, torch.float32, 64, 0.5, 8)
+        save_fmm_case("uniform1024_f32", 1024, 11, torch.float32, 64, 0.5, 8)
+
+
+if __name__ == "__main__":
+    main()
