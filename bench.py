@@ -290,7 +290,7 @@ def main():
 
             idx = torch.randperm(n, generator=torch.Generator().manual_seed(3))[:256].numpy()
             d = O.direct(pts.numpy(), q.double().numpy(), idx)
-            got = v.double().numpy()[idx]
+            got = v.double().numpy()[idx] / O.K_E  # the public operator includes K_E
             err = float(np.linalg.norm(got - d) / np.linalg.norm(d))
         except Exception:
             pass

@@ -371,8 +371,14 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
     for (int k = off[t]; k < off[t + 1]; ++k) {
         const int s = src[k];
         const typename Vec4<T>::type cs = center[s];
-        const T aM = half[s].w, iaM = (T)1 / aM, f = aL * iaM;
-        const T vx = (ct.x - cs.x) * iaM, vy = (ct.y - cs.y) * iaM, vz = (ct.z - cs.z) * iaM;
+        // Scale by the larger of the two radii so that every ratio is <= 1:
+        //  source scale: A_n += (a_L/a_M)^(n+1) sum Mhat_k I_{n+k}(t / a_M)
+        //  target scale: A_n += sum Mhat_k (a_M/a_L)^k I_{n+k}(t / a_L)
+        const T aM = half[s].w;
+        const bool by_src = aM >= aL;
+        const T ia = (T)1 / (by_src ? aM : aL);
+        const T f = by_src ? aL / aM : aM / aL;
+        const T vx = (ct.x - cs.x) * ia, vy = (ct.y - cs.y) * ia, vz = (ct.z - cs.z) * ia;
         const T r2 = vx * vx + vy * vy + vz * vz, ir2 = (T)1 / r2;
         if (lane <= 2 * p) {
             const int mu = lane;
@@ -395,7 +401,18 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
                 pi = ni;
             }
         }
-        for (int c = lane; c < nc; c += 32) sM[wl][c] = Mexp[(int64_t)s * nc_pad + c];
+        for (int c = lane; c < nc; c += 32) {
+            Cplx<T> mv = Mexp[(int64_t)s * nc_pad + c];
+            if (!by_src) {
+                int n, m;
+                coef_nm(c, n, m);
+                T fk = (T)1;
+                for (int e = 0; e < n; ++e) fk *= f;
+                mv.re *= fk;
+                mv.im *= fk;
+            }
+            sM[wl][c] = mv;
+        }
         __syncwarp();
         for (int q = 0; q < 3; ++q) {
             const int c = lane + 32 * q;
@@ -409,8 +426,11 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
                     sacc.re += v.re;
                     sacc.im += v.im;
                 }
-            T fn = f;
-            for (int e = 0; e < n; ++e) fn *= f;
+            T fn = (T)1;
+            if (by_src) {
+                fn = f;
+                for (int e = 0; e < n; ++e) fn *= f;
+            }
             acc[q].re += fn * sacc.re;
             acc[q].im += fn * sacc.im;
         }
