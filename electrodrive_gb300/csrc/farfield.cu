@@ -180,35 +180,32 @@ template <int P> __host__ __device__ constexpr bool m_in_set(int m, int set) {
 }
 template <int P> constexpr int m2l_passes() { return P >= 7 ? 2 : 1; }
 
-// One column mu of irregular harmonics and every (l, m) block that uses it;
-// mu is a template parameter so each column is straight-line code with
-// constant register indices.
+// The fast M2L factors the azimuth out of the translation.  With
+// v = (c_L - c_M) / a_L = (s cos phi, s sin phi, z) and the irregular
+// harmonics R_j^mu := I_j^mu(s, 0, z) (real: the recurrence with y = 0),
+//   I_j^mu(v) = e^{i mu phi} R_j^mu,   R_j^{-mu} = (-1)^mu R_j^mu,
+// so, with the source rotated, Mt_k^l = Mhat_k^l (a_M/a_L)^k e^{i l phi},
+//   S_n^m = sum_{k,l} Mt_k^l R_{n+k}^{l-m}   (real coefficients)
+//   A_n^m += e^{-i m phi} S_n^m,   Lhat_n^m = (-1)^(n+m) A_n^m / a_L.
+// Each term is a real x complex multiply-add (2 FMAs, against 4 for the
+// unfactored complex contraction), and the harmonics columns are real.
+// One column mu is generated at a time (template recursion: constant
+// register indices) and applied to every (l, m) block that uses it.
 template <int P, int SET, int MU>
-__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float vx,
-                                           float vy, float vz, float ir2, float &dr, float &di, float (&Ar)[ncoef(P)],
-                                           float (&Ai)[ncoef(P)]) {
-    if constexpr (MU > 0) {
-        const float s = -(float)(2 * MU - 1) * ir2;
-        const float nr = s * (vx * dr - vy * di);
-        const float ni = s * (vx * di + vy * dr);
-        dr = nr;
-        di = ni;
-    }
-    float cr[2 * P + 1], ci[2 * P + 1];  // I_j^mu at [j], j >= mu
+__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float s,
+                                           float z, float ir2, float &diag, float (&Sr)[ncoef(P)],
+                                           float (&Si)[ncoef(P)]) {
+    if constexpr (MU > 0) diag *= -(float)(2 * MU - 1) * s * ir2;  // R_mu^mu
+    float c[2 * P + 1];                                            // R_j^mu at [j], j >= mu
 #pragma unroll
     for (int j = 0; j <= 2 * P; ++j) {
         if (j == MU) {
-            cr[j] = dr;
-            ci[j] = di;
+            c[j] = diag;
         } else if (j == MU + 1) {
-            const float a = (float)(2 * j - 1) * vz * ir2;
-            cr[j] = a * cr[j - 1];
-            ci[j] = a * ci[j - 1];
+            c[j] = ((float)(2 * j - 1) * z * ir2) * c[j - 1];
         } else if (j > MU + 1) {
-            const float a = (float)(2 * j - 1) * vz;
             const float b = (float)((j - 1 + MU) * (j - 1 - MU));
-            cr[j] = (a * cr[j - 1] - b * cr[j - 2]) * ir2;
-            ci[j] = (a * ci[j - 1] - b * ci[j - 2]) * ir2;
+            c[j] = ((float)(2 * j - 1) * z * c[j - 1] - b * c[j - 2]) * ir2;
         }
     }
 #pragma unroll
@@ -219,37 +216,36 @@ __device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const fl
 #pragma unroll
             for (int k = 0; k <= P; ++k) {
                 const int j = n + k;
-                // (l, m) with l - m = +mu, l >= 0
+                // l - m = +mu, l >= 0:  Mt_k^l R^mu
                 {
                     const int l = m + MU;
                     if (l <= P && n >= m && k >= l) {
-                        Ar[tri(n, m)] += mr[tri(k, l)] * cr[j] - mi[tri(k, l)] * ci[j];
-                        Ai[tri(n, m)] += mr[tri(k, l)] * ci[j] + mi[tri(k, l)] * cr[j];
+                        Sr[tri(n, m)] += mr[tri(k, l)] * c[j];
+                        Si[tri(n, m)] += mi[tri(k, l)] * c[j];
                     }
                 }
-                // (l, m) with l - m = -mu: I^{-mu} = (-1)^mu conj(I^mu)
+                // l - m = -mu: R^{-mu} = (-1)^mu R^mu
                 if (MU > 0) {
                     const int l = m - MU;
                     const int al = l < 0 ? -l : l;
                     if (al <= P && n >= m && k >= al) {
-                        const float xr = mr[tri(k, al)], xi = mi[tri(k, al)];
                         if (l >= 0) {
-                            // (-1)^mu M conj(I)
+                            // (-1)^mu Mt_k^l R
                             if (MU & 1) {
-                                Ar[tri(n, m)] -= xr * cr[j] + xi * ci[j];
-                                Ai[tri(n, m)] -= xi * cr[j] - xr * ci[j];
+                                Sr[tri(n, m)] -= mr[tri(k, al)] * c[j];
+                                Si[tri(n, m)] -= mi[tri(k, al)] * c[j];
                             } else {
-                                Ar[tri(n, m)] += xr * cr[j] + xi * ci[j];
-                                Ai[tri(n, m)] += xi * cr[j] - xr * ci[j];
+                                Sr[tri(n, m)] += mr[tri(k, al)] * c[j];
+                                Si[tri(n, m)] += mi[tri(k, al)] * c[j];
                             }
                         } else {
-                            // (-1)^l conj(M) (-1)^mu conj(I) = (-1)^m conj(M I)
+                            // Mt_k^l = (-1)^|l| conj(Mt_k^|l|): (-1)^m conj(Mt) R
                             if (m & 1) {
-                                Ar[tri(n, m)] -= xr * cr[j] - xi * ci[j];
-                                Ai[tri(n, m)] += xr * ci[j] + xi * cr[j];
+                                Sr[tri(n, m)] -= mr[tri(k, al)] * c[j];
+                                Si[tri(n, m)] += mi[tri(k, al)] * c[j];
                             } else {
-                                Ar[tri(n, m)] += xr * cr[j] - xi * ci[j];
-                                Ai[tri(n, m)] -= xr * ci[j] + xi * cr[j];
+                                Sr[tri(n, m)] += mr[tri(k, al)] * c[j];
+                                Si[tri(n, m)] -= mi[tri(k, al)] * c[j];
                             }
                         }
                     }
@@ -257,13 +253,24 @@ __device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const fl
             }
         }
     }
-    if constexpr (MU < 2 * P) m2l_column<P, SET, MU + 1>(mr, mi, vx, vy, vz, ir2, dr, di, Ar, Ai);
+    if constexpr (MU < 2 * P) m2l_column<P, SET, MU + 1>(mr, mi, s, z, ir2, diag, Sr, Si);
 }
 
 template <int P, int SET>
 __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, float c, float vx, float vy, float vz,
                                                float (&Ar)[ncoef(P)], float (&Ai)[ncoef(P)]) {
     constexpr int NC = ncoef(P);
+    const float s2 = vx * vx + vy * vy;
+    const float r2 = s2 + vz * vz;
+    const float ir2 = __frcp_rn(r2);
+    const float s = sqrtf(s2);
+    float ec = 1.0f, es = 0.0f;  // e^{i phi}
+    if (s2 > 0.0f) {
+        const float is = 1.0f / s;
+        ec = vx * is;
+        es = vy * is;
+    }
+    // rotated, rescaled source coefficients
     float mr[NC], mi[NC];
 #pragma unroll
     for (int q = 0; q < (NC + 1) / 2; ++q) {
@@ -276,23 +283,50 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
         }
     }
     {
-        float ck = c;
+        float wr = 1.0f, wi = 0.0f;  // e^{i l phi}
 #pragma unroll
-        for (int k = 1; k <= P; ++k) {
-#pragma unroll
-            for (int l = 0; l <= P; ++l) {
-                if (l <= k) {
-                    mr[tri(k, l)] *= ck;
-                    mi[tri(k, l)] *= ck;
-                }
+        for (int l = 0; l <= P; ++l) {
+            if (l > 0) {
+                const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+                wr = nr;
+                wi = ni;
             }
-            ck *= c;
+            float ck = 1.0f;
+#pragma unroll
+            for (int k = 0; k <= P; ++k) {
+                if (k >= l) {
+                    const float fr = wr * ck, fi = wi * ck;
+                    const float xr = mr[tri(k, l)], xi = mi[tri(k, l)];
+                    mr[tri(k, l)] = xr * fr - xi * fi;
+                    mi[tri(k, l)] = xr * fi + xi * fr;
+                }
+                ck *= c;
+            }
         }
     }
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    const float ir2 = __frcp_rn(r2);
-    float dr = rsqrtf(r2), di = 0.0f;  // I_mu^mu, advanced column by column
-    m2l_column<P, SET, 0>(mr, mi, vx, vy, vz, ir2, dr, di, Ar, Ai);
+    float Sr[NC], Si[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
+    float diag = sqrtf(ir2);  // R_0^0 = 1 / |v|
+    m2l_column<P, SET, 0>(mr, mi, s, vz, ir2, diag, Sr, Si);
+    // rotate back: A_n^m += e^{-i m phi} S_n^m
+    float wr = 1.0f, wi = 0.0f;
+#pragma unroll
+    for (int m = 0; m <= P; ++m) {
+        if (m > 0) {
+            const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+            wr = nr;
+            wi = ni;
+        }
+        if (!m_in_set<P>(m, SET)) continue;
+#pragma unroll
+        for (int n = 0; n <= P; ++n) {
+            if (n < m) continue;
+            const float xr = Sr[tri(n, m)], xi = Si[tri(n, m)];
+            Ar[tri(n, m)] += xr * wr + xi * wi;
+            Ai[tri(n, m)] += xi * wr - xr * wi;
+        }
+    }
 }
 
 template <int P, int SET>
@@ -340,8 +374,8 @@ __global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t
             if (m > n || !m_in_set<P>(m, SET)) continue;
             const int k = tri(n, m);
             if ((k & 31) == lane) {
-                const float s = ((n + m) & 1) ? -iaL : iaL;
-                out[k] = make_float2(s * Ar[k], s * Ai[k]);
+                const float sg = ((n + m) & 1) ? -iaL : iaL;
+                out[k] = make_float2(sg * Ar[k], sg * Ai[k]);
             }
         }
     }
