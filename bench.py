@@ -33,9 +33,11 @@ sys.path.insert(0, ROOT)
 METRIC = "BEM solves/s to 1e-6 residual, mixed+learned vs plain FP64 GMRES; FMM Mpts/s"
 N_DEFAULT = 1 << 20
 WORKLOAD = "fmm_matvec_uniform_unit_cube_N1048576_p8_leaf64_theta0.5_fp32"
-# algorithmic FP32 flops of one M2L pair at p = 8: 45 target x 81 source
-# complex multiply-adds of 8 real flops each
-M2L_FLOPS_PER_PAIR = 8 * 45 * 81
+# algorithmic FP32 flops of one M2L pair at p = 8 in the azimuth-factored
+# form the kernel evaluates: 45 x 81 real-by-complex multiply-adds (4 flops),
+# two azimuthal rotations of 45 coefficients (complex multiply, 8 flops
+# each) and 153 real harmonics by a 3-term recurrence (6 flops each)
+M2L_FLOPS_PER_PAIR = 4 * 45 * 81 + 2 * 8 * 45 + 6 * 153
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
 # as the reference FLOP model's 20 flops (autotune.py:622-667)
 P2P_FLOPS_PER_INTERACTION = 20
