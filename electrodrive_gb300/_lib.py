@@ -84,6 +84,7 @@ def _declare(L):
         "edfmm_plan_p2p": (i32, [_vp, _vp, _vp]),
         "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
+        "edfmm_dense_matvec": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -148,6 +149,27 @@ def measure_fp32_peak(iters: int = 20000) -> float:
     out = C.c_double()
     check(L.edfmm_measure_fp32_peak(int(iters), stream_handle(), C.byref(out)), "edfmm_measure_fp32_peak")
     return float(out.value)
+
+
+def dense_matvec(centroids, sigma, areas, self_integrals=None, *, k_e: float = 1.0, out=None):
+    """Dense single-layer operator on CUDA tensors (edfmm_dense_matvec)."""
+    L = load_library()
+    n = int(sigma.shape[0])
+    dev, dt = sigma.device, sigma.dtype
+    for name, t in (("centroids", centroids), ("areas", areas), ("self_integrals", self_integrals)):
+        if t is None:
+            continue
+        if t.device != dev or t.dtype != dt or not t.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous {dt} tensor on {dev}")
+    if centroids.shape != (n, 3) or areas.shape != (n,) or (self_integrals is not None and self_integrals.shape != (n,)):
+        raise ValueError("centroids must be (N, 3) and areas / self_integrals (N,) matching sigma")
+    sigma = sigma.contiguous()
+    if out is None:
+        out = torch.empty_like(sigma)
+    with torch.cuda.device(dev):
+        check(L.edfmm_dense_matvec(ptr(centroids), ptr(sigma), ptr(areas), ptr(self_integrals), n, dtype_code(dt),
+                                   float(k_e), ptr(out), stream_handle(dev)), "edfmm_dense_matvec")
+    return out
 
 
 class Plan:

@@ -1,0 +1,82 @@
+"""Single-layer BEM operator entry point (electrodrive/core/bem_kernel.py:558-707).
+
+``bem_matvec_gpu`` keeps the reference's signature and backend names:
+``"external"`` calls ``matvec_impl`` (e.g. ``LaplaceFmm3D.matvec``) with the
+reference's keyword arguments; ``"auto"``, ``"torch_tiled"`` and ``"keops"``
+all run libedfmm's dense CUDA operator (``edfmm_dense_matvec``).  Results are
+returned on sigma's device.
+"""
+from __future__ import annotations
+
+import os
+from typing import Any, Callable, Optional
+
+import torch
+from torch import Tensor
+
+from .. import _lib
+from ..utils.config import K_E
+
+
+class LaplaceSingleLayerKernel:
+    """G(r) = K_E / r (the only kernel the reference's fast paths implement)."""
+
+    name = "laplace_single_layer"
+
+    def potential(self, diff: Tensor, r: Tensor) -> Tensor:
+        return K_E / r
+
+
+DEFAULT_SINGLE_LAYER_KERNEL = LaplaceSingleLayerKernel()
+
+
+def _ensure_tile_size(tile_size: Optional[int]) -> int:
+    if tile_size is not None and tile_size > 0:
+        return int(tile_size)
+    env_val = os.getenv("EDE_BEM_TILE_SIZE")
+    if env_val is not None:
+        try:
+            v = int(env_val)
+            if v > 0:
+                return v
+        except ValueError:
+            pass
+    return 1024
+
+
+def _dense(sigma: Tensor, src_centroids: Tensor, areas: Tensor, self_integrals: Optional[Tensor]) -> Tensor:
+    dev = sigma.device if sigma.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    dt = sigma.dtype
+    c = src_centroids.to(dev, dt).contiguous()
+    a = areas.to(dev, dt).contiguous()
+    s = sigma.to(dev).contiguous()
+    si = None if self_integrals is None else self_integrals.to(dev, dt).contiguous()
+    out = _lib.dense_matvec(c, s, a, si, k_e=float(K_E))
+    return out if sigma.is_cuda else out.to(sigma.device)
+
+
+def bem_matvec_gpu(sigma: Tensor, src_centroids: Tensor, areas: Tensor, *, tile_size: int = 1024,
+                   self_integrals: Optional[Tensor] = None, logger: Optional[Any] = None, use_keops: bool = False,
+                   kernel: Optional[Any] = None, backend: str = "auto", matvec_impl: Optional[Callable[..., Tensor]] = None,
+                   **kwargs) -> Tensor:
+    """Matrix-free V = sum_j K_ij sigma_j A_j with K_ii = self_integrals_i (or 0)."""
+    if "self_correction" in kwargs and self_integrals is None:
+        self_integrals = kwargs.get("self_correction")
+    if backend not in {"auto", "torch_tiled", "keops", "external"}:
+        raise ValueError(f"Unknown BEM backend: {backend!r}")
+    ker = kernel or DEFAULT_SINGLE_LAYER_KERNEL
+    tile_size = _ensure_tile_size(tile_size)
+    if backend == "external":
+        if matvec_impl is None:
+            raise ValueError("backend='external' requires matvec_impl.")
+        return matvec_impl(sigma=sigma, src_centroids=src_centroids, areas=areas, tile_size=tile_size,
+                           self_integrals=self_integrals, logger=logger, kernel=ker, **kwargs)
+    if not isinstance(ker, LaplaceSingleLayerKernel):
+        raise ValueError("electrodrive_gb300 implements the Laplace single-layer kernel only")
+    n = int(sigma.shape[0])
+    if n == 0:
+        return torch.zeros_like(sigma)
+    return _dense(sigma, src_centroids, areas, self_integrals)
+
+
+__all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu"]

@@ -1,0 +1,182 @@
+// Dense single-layer operator (the reference's torch-tiled A(x),
+// electrodrive/core/bem_kernel.py:157-230 and :341-381):
+//   V_i = k_e sum_{j != i} sigma_j A_j / sqrt(max(|c_i - c_j|^2, 1e-24))
+//         + self_integrals_i sigma_i A_i        (self term only if given)
+//   non-finite V_i -> 0.
+//
+// The source index is split into chunks so that small N (5,120 panels) still
+// fills every SM: block (row tile, chunk) accumulates its chunk's sources for
+// 256 targets from (x, y, z, sigma A) tiles staged in shared memory and
+// writes one partial sum per target; a second kernel adds the partials of a
+// row in chunk order (deterministic) and applies k_e, the self term and the
+// non-finite clamp.  With a single chunk the first kernel finishes the rows
+// itself.
+#include <algorithm>
+#include <mutex>
+
+#include "edfmm_internal.cuh"
+
+namespace edfmm {
+
+namespace {
+
+constexpr int kRows = 256;  // targets per block (one per thread)
+constexpr int kTile = 256;  // sources staged per shared-memory tile
+
+__device__ __forceinline__ float inv_r(float r2) { return rsqrtf(fmaxf(r2, 1e-24f)); }
+__device__ __forceinline__ double inv_r(double r2) { return rsqrt(fmax(r2, 1e-24)); }
+
+template <typename T>
+__device__ __forceinline__ T finish(T acc, int64_t i, T k_e, const T *self_int, const T *sigma, const T *areas) {
+    T v = acc * k_e;
+    if (self_int) v += self_int[i] * sigma[i] * areas[i];
+    return isfinite(v) ? v : (T)0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRows) k_dense_partial(const T *__restrict__ c, const T *__restrict__ sigma,
+                                                         const T *__restrict__ areas, int64_t n, int64_t chunk,
+                                                         T *__restrict__ partial, int finish_rows, T k_e,
+                                                         const T *__restrict__ self_int, T *__restrict__ out) {
+    using T4 = typename Vec4<T>::type;
+    __shared__ T4 src[kTile];
+    const int64_t i = (int64_t)blockIdx.x * kRows + threadIdx.x;
+    const int64_t j0 = (int64_t)blockIdx.y * chunk;
+    const int64_t j1 = min(n, j0 + chunk);
+    T xi = 0, yi = 0, zi = 0;
+    if (i < n) {
+        xi = c[3 * i];
+        yi = c[3 * i + 1];
+        zi = c[3 * i + 2];
+    }
+    T acc = 0;
+    for (int64_t jb = j0; jb < j1; jb += kTile) {
+        const int64_t j = jb + threadIdx.x;
+        T4 s;
+        if (j < j1) {
+            s.x = c[3 * j];
+            s.y = c[3 * j + 1];
+            s.z = c[3 * j + 2];
+            s.w = sigma[j] * areas[j];
+        } else {
+            s.x = s.y = s.z = s.w = 0;
+        }
+        __syncthreads();
+        src[threadIdx.x] = s;
+        __syncthreads();
+        const int cnt = (int)((j1 - jb) < (int64_t)kTile ? (j1 - jb) : (int64_t)kTile);
+        const bool diag_here = i >= jb && i < jb + cnt;
+        // two-level sum (tile, then chunk) bounds FP32 rounding growth
+        T tacc = 0;
+#pragma unroll 8
+        for (int k = 0; k < cnt; ++k) {
+            const T4 q = src[k];
+            const T dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+            T w = q.w * inv_r(dx * dx + dy * dy + dz * dz);
+            if (diag_here && jb + k == i) w = 0;
+            tacc += w;
+        }
+        acc += tacc;
+    }
+    if (i >= n) return;
+    if (finish_rows)
+        out[i] = finish(acc, i, k_e, self_int, sigma, areas);
+    else
+        partial[(int64_t)blockIdx.y * n + i] = acc;
+}
+
+template <typename T>
+__global__ void k_dense_reduce(const T *__restrict__ partial, int chunks, int64_t n, T k_e,
+                               const T *__restrict__ self_int, const T *__restrict__ sigma,
+                               const T *__restrict__ areas, T *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T acc = 0;
+    for (int c = 0; c < chunks; ++c) acc += partial[(int64_t)c * n + i];
+    out[i] = finish(acc, i, k_e, self_int, sigma, areas);
+}
+
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    if (dev < 64 && cached[dev]) return cached[dev];
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (dev < 64) cached[dev] = sms;
+    return sms;
+}
+
+}  // namespace
+
+// Source chunking: enough blocks for ~8 per SM, at most 64 chunks, chunks a
+// multiple of the shared-memory tile.
+void dense_plan(int64_t n, int &chunks, int64_t &chunk) {
+    const int64_t rows = (n + kRows - 1) / kRows;
+    const int64_t want = 8LL * sm_count();
+    int64_t c = rows >= want ? 1 : (want + rows - 1) / rows;
+    c = std::min<int64_t>(std::max<int64_t>(c, 1), 64);
+    chunk = ((n + c - 1) / c + kTile - 1) / kTile * kTile;
+    if (chunk <= 0) chunk = kTile;
+    chunks = (int)((n + chunk - 1) / chunk);
+    if (chunks < 1) chunks = 1;
+}
+
+size_t dense_scratch_bytes(int64_t n, int dtype) {
+    int chunks;
+    int64_t chunk;
+    dense_plan(n, chunks, chunk);
+    if (chunks <= 1) return 0;
+    return (size_t)chunks * (size_t)n * (dtype == EDFMM_F64 ? 8 : 4);
+}
+
+template <typename T>
+int dense_run(const T *c, const T *sigma, const T *areas, const T *self_int, int64_t n, T k_e, T *out, T *partial,
+              cudaStream_t s) {
+    int chunks;
+    int64_t chunk;
+    dense_plan(n, chunks, chunk);
+    dim3 grid((unsigned)((n + kRows - 1) / kRows), (unsigned)chunks);
+    k_dense_partial<T><<<grid, kRows, 0, s>>>(c, sigma, areas, n, chunk, partial, chunks == 1, k_e, self_int, out);
+    EDFMM_LAUNCH_CHECK("k_dense_partial");
+    if (chunks > 1) {
+        k_dense_reduce<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(partial, chunks, n, k_e, self_int, sigma, areas,
+                                                                     out);
+        EDFMM_LAUNCH_CHECK("k_dense_reduce");
+    }
+    return EDFMM_OK;
+}
+
+int dense_matvec(const void *c, const void *sigma, const void *areas, const void *self_int, int64_t n, int dtype,
+                 double k_e, void *out, void *scratch, cudaStream_t s) {
+    if (dtype == EDFMM_F64)
+        return dense_run<double>(static_cast<const double *>(c), static_cast<const double *>(sigma),
+                                 static_cast<const double *>(areas), static_cast<const double *>(self_int), n, k_e,
+                                 static_cast<double *>(out), static_cast<double *>(scratch), s);
+    return dense_run<float>(static_cast<const float *>(c), static_cast<const float *>(sigma),
+                            static_cast<const float *>(areas), static_cast<const float *>(self_int), n, (float)k_e,
+                            static_cast<float *>(out), static_cast<float *>(scratch), s);
+}
+
+}  // namespace edfmm
+
+using namespace edfmm;
+
+extern "C" EDFMM_API int edfmm_dense_matvec(const void *centroids, const void *sigma, const void *areas,
+                                            const void *self_integrals, int64_t n, int dtype, double k_e, void *out,
+                                            void *stream) {
+    if (n < 0) return fail(EDFMM_ERR_ARG, "n must be >= 0");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (n == 0) return EDFMM_OK;
+    if (!centroids || !sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "centroids, sigma, areas, out must be non-NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = dense_scratch_bytes(n, dtype);
+    void *scratch = nullptr;
+    if (bytes) EDFMM_CUDA_TRY(cudaMallocAsync(&scratch, bytes, s));
+    int rc = dense_matvec(centroids, sigma, areas, self_integrals, n, dtype, k_e, out, scratch, s);
+    if (scratch) {
+        cudaError_t e = cudaFreeAsync(scratch, s);
+        if (!rc && e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("cudaFreeAsync: ") + cudaGetErrorString(e));
+    }
+    return rc;
+}

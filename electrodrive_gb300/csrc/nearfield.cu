@@ -92,6 +92,8 @@ template <typename T, int TPL, bool SELF>
 __device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *sp, int cnt, int sbase,
                                                  const typename Vec4<T>::type (&x)[2], const int (&ti)[2], T eps2,
                                                  T (&acc)[2]) {
+    // per-chunk partial sums, then one add: two-level summation
+    T part[2] = {(T)0, (T)0};
 #pragma unroll 8
     for (int j = 0; j < cnt; ++j) {
         const typename Vec4<T>::type q = sp[j];
@@ -100,9 +102,11 @@ __device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *s
             const T dx = x[u].x - q.x, dy = x[u].y - q.y, dz = x[u].z - q.z;
             T inv = inv_dist(dx * dx + dy * dy + dz * dz, eps2);
             if (SELF && sbase + j == ti[u]) inv = (T)0;
-            acc[u] += q.w * inv;
+            part[u] += q.w * inv;
         }
     }
+#pragma unroll
+    for (int u = 0; u < TPL; ++u) acc[u] += part[u];
 }
 
 template <typename T, int TPL>

@@ -160,6 +160,19 @@ EDFMM_API int edfmm_plan_get_expansions(const edfmm_plan *plan, void *multipoles
                               void *stream);
 
 /*
+ * Dense single-layer operator, the reference's torch-tiled A(x)
+ * (electrodrive/core/bem_kernel.py:157-230, wrapper :341-381):
+ *   out_i = k_e sum_{j != i} sigma_j areas_j / sqrt(max(|c_i - c_j|^2, 1e-24))
+ *           + self_integrals_i sigma_i areas_i   (self term only if non-NULL);
+ *   non-finite entries -> 0.  centroids (n, 3) row-major, vectors (n,).
+ * Partial sums live in stream-ordered scratch (cudaMallocAsync/cudaFreeAsync
+ * on `stream`).
+ */
+EDFMM_API int edfmm_dense_matvec(const void *centroids_dev, const void *sigma_dev, const void *areas_dev,
+                                 const void *self_integrals_dev, int64_t n, int dtype, double k_e, void *out_dev,
+                                 void *stream);
+
+/*
  * Number of the library's own kernel launches issued since load (all
  * threads).  Used by benchmarks to report launches inside a timed region.
  */
