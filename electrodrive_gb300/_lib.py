@@ -85,6 +85,7 @@ def _declare(L):
         "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
         "edfmm_dense_matvec": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
+        "edfmm_dense_matvec_noalloc": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -162,6 +162,76 @@ int dense_matvec(const void *c, const void *sigma, const void *areas, const void
 
 using namespace edfmm;
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some callers cannot allocate device memory while they apply the operator:
+// an application whose framework allocator has already reserved the GPU's
+// free memory (so a cudaMalloc/cudaMallocAsync from this library would fail
+// or fragment that pool), or a host language binding that exposes no CUDA
+// allocator and cannot release device memory it did not create.  For them,
+// the partial sums live in one fixed, file-scope device array instead of
+// stream-ordered scratch.  The array (8 MiB) is part of the library's
+// device image: every GPU that loads the library holds it until the process
+// exits.  Host code must not pass the array's name to a kernel (on the host
+// it is only a stand-in symbol); its device address is looked up once per
+// device with cudaGetSymbolAddress, with that device current.
+// ---------------------------------------------------------------------------
+#define EDFMM_DENSE_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define EDFMM_DENSE_NOALLOC_MAX_N 262144
+
+static __device__ __align__(256) unsigned char g_dense_noalloc_scratch[EDFMM_DENSE_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void *g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_dense_noalloc_scratch on the current device (looked up
+// on the first call per device).
+int noalloc_scratch(void **addr) {
+    int dev = 0;
+    EDFMM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(EDFMM_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_dense_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(EDFMM_ERR_CUDA,
+                        std::string("cudaGetSymbolAddress(g_dense_noalloc_scratch) failed: ") + cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    *addr = g_noalloc_addr[dev];
+    return EDFMM_OK;
+}
+}  // namespace
+
+extern "C" EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids, const void *sigma, const void *areas,
+                                                    const void *self_integrals, int64_t n, int dtype, double k_e,
+                                                    void *out, void *stream) {
+    if (n < 0) return fail(EDFMM_ERR_ARG, "n must be >= 0");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (n > EDFMM_DENSE_NOALLOC_MAX_N)
+        return fail(EDFMM_ERR_ARG, "edfmm_dense_matvec_noalloc: n = " + std::to_string(n) + " exceeds its limit of " +
+                                       std::to_string(EDFMM_DENSE_NOALLOC_MAX_N) +
+                                       " panels (fixed 8 MiB device scratch); use edfmm_dense_matvec");
+    if (n == 0) return EDFMM_OK;
+    if (!centroids || !sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "centroids, sigma, areas, out must be non-NULL");
+    const size_t bytes = dense_scratch_bytes(n, dtype);
+    if (bytes > EDFMM_DENSE_NOALLOC_SCRATCH_BYTES)
+        return fail(EDFMM_ERR_ARG, "edfmm_dense_matvec_noalloc: this device needs " + std::to_string(bytes) +
+                                       " bytes of partial sums, above the fixed 8 MiB scratch; use edfmm_dense_matvec");
+    void *scratch = nullptr;
+    if (bytes) {
+        if (int rc = noalloc_scratch(&scratch)) return rc;
+    }
+    // every partial-sum slot the reduction reads is written by this call, so
+    // nothing left by an earlier call needs clearing
+    return dense_matvec(centroids, sigma, areas, self_integrals, n, dtype, k_e, out, scratch,
+                        static_cast<cudaStream_t>(stream));
+}
+
 extern "C" EDFMM_API int edfmm_dense_matvec(const void *centroids, const void *sigma, const void *areas,
                                             const void *self_integrals, int64_t n, int dtype, double k_e, void *out,
                                             void *stream) {

@@ -173,6 +173,28 @@ EDFMM_API int edfmm_dense_matvec(const void *centroids_dev, const void *sigma_de
                                  void *stream);
 
 /*
+ * The same dense operator for callers that cannot allocate device memory:
+ * for example an application whose framework allocator already holds the
+ * GPU's free memory, or a host-language binding that has no CUDA allocator
+ * and cannot free device memory it did not create.  No counterpart in the
+ * reference (it has no device code for this operator).
+ *
+ * Allocates nothing: the partial sums live in a fixed 8 MiB file-scope
+ * device array that every GPU loading the library keeps until exit.
+ * Limit: n <= 262144 panels; larger n returns EDFMM_ERR_ARG with a message
+ * (use edfmm_dense_matvec).  The caller still provides all inputs and `out`.
+ * The first call on each device looks up the array's device address with
+ * cudaGetSymbolAddress; make that first call before any stream capture.
+ * All calls share the array, so calls whose work overlaps on the GPU (on
+ * different streams, or on different host threads without ordering) race;
+ * order them on one stream.  Each call rewrites every scratch slot it reads,
+ * so no clearing is needed between calls.
+ */
+EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids_dev, const void *sigma_dev, const void *areas_dev,
+                                         const void *self_integrals_dev, int64_t n, int dtype, double k_e,
+                                         void *out_dev, void *stream);
+
+/*
  * Number of the library's own kernel launches issued since load (all
  * threads).  Used by benchmarks to report launches inside a timed region.
  */
