@@ -38,6 +38,10 @@ WORKLOAD = "fmm_matvec_uniform_unit_cube_N1048576_p8_leaf64_theta0.5_fp32"
 # two azimuthal rotations of 45 coefficients (complex multiply, 8 flops
 # each) and 153 real harmonics by a 3-term recurrence (6 flops each)
 M2L_FLOPS_PER_PAIR = 4 * 45 * 81 + 2 * 8 * 45 + 6 * 153
+# DRAM bytes one M2L pass moves per pair (ncu --set full of k_m2l_fast<8, SET>
+# at N = 262,144: 44.6 MB for 9,091,877 pairs; traffic grows with the pair
+# count, so it is scaled to the benchmark's pair count)
+M2L_DRAM_BYTES_PER_PAIR_PER_PASS = 44.6e6 / 9_091_877
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
 # as the reference FLOP model's 20 flops (autotune.py:622-667)
 P2P_FLOPS_PER_INTERACTION = 20
@@ -320,7 +324,9 @@ def main():
             "clocks": clk.summary(),
             "roofline": {"kernel": "k_m2l_fast (M2L stage: two passes over split output sets)", "bound": "fp32",
                          "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "frac": achieved / fp32_peak if fp32_peak else None,
+                         "traffic": 2 * M2L_DRAM_BYTES_PER_PAIR_PER_PASS * info.n_m2l_pairs,
+                         "traffic_note": "DRAM bytes of the M2L stage, scaled from an ncu capture at N=262,144",
                          "peak_source": "FP32 FMA probe measured in this run (edfmm_measure_fp32_peak)",
                          "flops_per_pair": M2L_FLOPS_PER_PAIR},
             "stages_ms": stage_ms,

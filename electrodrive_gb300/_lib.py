@@ -86,6 +86,12 @@ def _declare(L):
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
         "edfmm_dense_matvec": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_matvec_noalloc": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
+        "edfmm_dense_workspace_bytes": (C.c_size_t, [i64, i32]),
+        "edfmm_dense_matvec_ws": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp, C.c_size_t, _vp]),
+        "edfmm_gmres_work_bytes": (C.c_size_t, [i64, i32]),
+        "edfmm_gmres_start": (i32, [i64, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "edfmm_gmres_arnoldi": (i32, [i64, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "edfmm_gmres_update": (i32, [i64, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,0 +1,304 @@
+"""Restarted left-preconditioned GMRES on the GPU
+(electrodrive/core/bem_solver.py:36-920).
+
+``gmres_restart`` keeps the reference's signature, defaults, stopping rule and
+``info`` dictionary:
+
+* tol_abs = max(tol * |b - A x0|, tol * 1e-12, 1e-12) (|b - A x0| replaced by 1
+  when below 1e-16);
+* every restart cycle runs ``restart`` Arnoldi steps (the reference does not
+  leave a cycle early on the inner estimate), then x += V y and the TRUE
+  residual |b - A x| decides convergence;
+* codes 0 converged, 1 maxiter, 2 terminate/stagnation, 3 non-finite initial
+  residual, 5 non-finite inner residual, 6 non-finite post-update residual,
+  7 non-finite initial preconditioned residual; for N <= 512 a failed
+  preconditioned run is retried once without the preconditioner;
+* the Krylov dtype is b's dtype (FP64 for FP32 systems with N <= 64).
+
+The Krylov arithmetic runs in libedfmm (``edfmm_gmres_*``): CGS2
+orthogonalisation with FP64 inner products, Hessenberg / Givens / triangular
+solve in FP64 on the device.  The host reads the device status once per
+cycle.  When the operator advertises ``capturable = True`` (the operators of
+``electrodrive_gb300.core.operators``) each full cycle is captured once as a
+CUDA graph and replayed.
+"""
+from __future__ import annotations
+
+import math
+import time
+from typing import Any, Callable, Dict, Optional, Tuple, Union
+
+import torch
+from torch import Tensor
+
+from .. import _lib
+
+
+class DiagonalPreconditioner:
+    """x -> pinv * x (the form setup_preconditioner builds; pinv is read by the kernels)."""
+
+    def __init__(self, pinv: Tensor):
+        self.pinv = pinv
+
+    def __call__(self, x: Tensor) -> Tensor:
+        return self.pinv.to(x.device, x.dtype) * x
+
+
+def setup_preconditioner(method: Optional[str], A_diag: Optional[Tensor] = None, areas: Optional[Tensor] = None,
+                         logger: Optional[Any] = None) -> Optional[DiagonalPreconditioner]:
+    """Same rules as bem_solver.py:36-117 (non-finite / |d| < 1e-18 entries act as identity)."""
+    if method is None or method == "none":
+        return None
+    if method in ("diag", "jacobi"):
+        if A_diag is None:
+            if areas is None:
+                return None
+            method = "mass"
+        else:
+            d = A_diag.clone()
+            bad = (~torch.isfinite(d)) | (d.abs() < 1e-18)
+            d[bad] = 1.0
+            return DiagonalPreconditioner(1.0 / d)
+    if method == "mass":
+        if areas is None:
+            return None
+        d = areas.clone()
+        bad = (~torch.isfinite(d)) | (d.abs() < 1e-18)
+        if not torch.any(~bad):
+            return None
+        d[bad] = 1.0
+        return DiagonalPreconditioner(1.0 / d)
+    return None
+
+
+def _info(iters, resid, success, code, resid_true0, tol_abs, used_precond, **extra):
+    d = dict(iters=int(iters), resid=float(resid), success=bool(success), code=int(code),
+             resid_true0=float(resid_true0), tol_abs=float(tol_abs), used_preconditioner=bool(used_precond))
+    d.update(extra)
+    return d
+
+
+class _Krylov:
+    """Device buffers of one GMRES run."""
+
+    def __init__(self, n: int, restart: int, dtype: torch.dtype, device: torch.device):
+        L = _lib.load_library()
+        self.n, self.restart, self.dtype, self.device = n, restart, dtype, device
+        self.code = _lib.dtype_code(dtype)
+        self.V = torch.zeros(restart + 1, n, dtype=dtype, device=device)
+        self.H = torch.zeros(restart + 1, restart, dtype=torch.float64, device=device)
+        self.g = torch.zeros(restart + 1, dtype=torch.float64, device=device)
+        self.cs = torch.zeros(restart, dtype=torch.float64, device=device)
+        self.sn = torch.zeros(restart, dtype=torch.float64, device=device)
+        self.scal = torch.zeros(5 + restart, dtype=torch.float64, device=device)
+        self.w = torch.zeros(n, dtype=dtype, device=device)
+        nbytes = int(L.edfmm_gmres_work_bytes(n, restart))
+        self.work = torch.zeros((nbytes + 7) // 8, dtype=torch.float64, device=device)
+        self.L = L
+
+    def start(self, b: Tensor, ax: Tensor, pinv: Optional[Tensor]):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_gmres_start(self.n, self.code, self.restart, P(b), P(ax), P(pinv), P(self.V[0]),
+                                            P(self.g), P(self.scal), P(self.work), _lib.stream_handle(self.device)),
+                   "edfmm_gmres_start")
+
+    def arnoldi(self, j: int, av: Tensor, pinv: Optional[Tensor]):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_gmres_arnoldi(self.n, self.code, self.restart, j, P(self.V), P(av), P(pinv), P(self.H),
+                                              P(self.g), P(self.cs), P(self.sn), P(self.scal), P(self.w),
+                                              P(self.work), _lib.stream_handle(self.device)), "edfmm_gmres_arnoldi")
+
+    def update(self, m: int, x: Tensor):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_gmres_update(self.n, self.code, self.restart, m, P(self.V), P(self.H), P(self.g), P(x),
+                                             P(self.work), _lib.stream_handle(self.device)), "edfmm_gmres_update")
+
+
+@torch.no_grad()
+def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable[[Tensor], Tensor]] = None,
+                  restart: int = 80, tol: float = 1e-8, maxiter: int = 500, logger: Optional[Any] = None,
+                  x0: Optional[Tensor] = None, telemetry: Optional[Any] = None, pass_index: int = 0,
+                  live_control_poll_fn: Optional[Callable[[], Dict[str, Any]]] = None, log_every: int = 1, *,
+                  callback: Optional[Callable[[int, float, Dict[str, Any]], None]] = None,
+                  callback_context: Optional[Dict[str, Any]] = None,
+                  precond: Optional[Union[str, Callable[[Tensor], Tensor]]] = None, areas: Optional[Tensor] = None,
+                  A_diag: Optional[Tensor] = None, validate_operators: bool = False, use_graph: Union[bool, str] = "auto",
+                  _retry_without_precond: bool = False) -> Tuple[Tensor, Dict[str, Any]]:
+    if restart <= 0:
+        raise ValueError("restart must be positive")
+    if maxiter <= 0:
+        raise ValueError("maxiter must be positive")
+    if restart > 256:
+        raise ValueError("restart must be <= 256")
+    _lib.load_library()
+    orig_dtype, orig_device = b.dtype, b.device
+    dev = orig_device if orig_device.type == "cuda" else torch.device("cuda", torch.cuda.current_device())
+    N = int(b.numel())
+    work_dtype = torch.float64 if (N <= 64 and orig_dtype in (torch.float16, torch.bfloat16, torch.float32)) \
+        else orig_dtype
+    if work_dtype not in (torch.float32, torch.float64):
+        work_dtype = torch.float32
+
+    def A_apply(v: Tensor) -> Tensor:
+        if work_dtype == orig_dtype and orig_device.type == "cuda":
+            return A(v)
+        out = A(v.to(dtype=orig_dtype, device=orig_device))
+        return out.to(dtype=work_dtype, device=dev)
+
+    # preconditioner: diagonal forms run inside the kernels, others in Python
+    if M is None and precond is not None:
+        M_local = setup_preconditioner(precond, A_diag=A_diag, areas=areas, logger=logger) if isinstance(precond, str) \
+            else (precond if callable(precond) else None)
+    else:
+        M_local = M
+    if M_local is not None:
+        probe = torch.ones(N, dtype=work_dtype, device=dev)
+        try:
+            Mp = M_local(probe.to(orig_dtype).to(orig_device)).to(dev, work_dtype)
+            if Mp.shape != b.shape or not torch.isfinite(Mp).all():
+                M_local = None
+        except Exception:
+            M_local = None
+    pinv = None
+    M_python = None
+    if isinstance(M_local, DiagonalPreconditioner):
+        pinv = M_local.pinv.to(dev, work_dtype).contiguous()
+    elif M_local is not None:
+        M_python = M_local
+    used_pc = M_local is not None
+
+    if validate_operators:
+        probe = torch.randn(N, dtype=work_dtype, device=dev)
+        probe = probe / probe.norm()
+        try:
+            Ap = A_apply(probe)
+        except Exception:
+            return b.to(dtype=orig_dtype), _info(0, float("nan"), False, 4, float("nan"), float("nan"), False)
+        if Ap.shape != b.shape or not torch.isfinite(Ap).all():
+            return b.to(dtype=orig_dtype), _info(0, float("nan"), False, 4, float("nan"), float("nan"), False)
+
+    def retry():
+        return gmres_restart(A=A, b=b, M=None, restart=restart, tol=tol, maxiter=maxiter, logger=logger, x0=x0,
+                             telemetry=telemetry, pass_index=pass_index, live_control_poll_fn=live_control_poll_fn,
+                             log_every=log_every, callback=callback, callback_context=callback_context, precond=None,
+                             areas=None, validate_operators=False, use_graph=use_graph, _retry_without_precond=True)
+
+    can_retry = used_pc and not _retry_without_precond and N <= 512
+    K = _Krylov(N, restart, work_dtype, dev)
+    x = torch.zeros(N, dtype=work_dtype, device=dev) if x0 is None else x0.to(dev, work_dtype).clone()
+    b_work = b.to(dev, work_dtype).contiguous()
+    av = torch.empty(N, dtype=work_dtype, device=dev)
+    graph = None
+    want_graph = (use_graph is True) or (use_graph == "auto" and bool(getattr(A, "capturable", False))
+                                          and M_python is None and work_dtype == orig_dtype
+                                          and orig_device.type == "cuda")
+
+    def start_cycle():
+        ax = A_apply(x)
+        if M_python is None:
+            K.start(b_work, ax, pinv)
+        else:  # generic preconditioner: precondition on the host side of the call
+            rt = b_work - ax
+            K.start(M_python(rt).to(dev, work_dtype).contiguous(), torch.zeros_like(rt), None)
+            K.scal[0] = torch.linalg.norm(rt.double())
+
+    def inner_steps(steps: int):
+        for j in range(steps):
+            y = A_apply(K.V[j])
+            if M_python is not None:
+                y = M_python(y).to(dev, work_dtype)
+            av.copy_(y)
+            K.arnoldi(j, av, pinv if M_python is None else None)
+
+    total_iters = 0
+    tol_abs = float("nan")
+    r_true_norm = float("nan")
+    r_norm = float("nan")
+    max_cycles = max(1, (maxiter + restart - 1) // restart)
+    for cycle in range(max_cycles + 1):
+        start_cycle()
+        scal = K.scal[:2].cpu()
+        r_true_norm, beta = float(scal[0]), float(scal[1])
+        if cycle == 0:
+            if not math.isfinite(r_true_norm):
+                return x.to(orig_dtype).to(orig_device), _info(0, r_true_norm, False, 3, r_true_norm, float("nan"),
+                                                               used_pc)
+            if not math.isfinite(beta):
+                if can_retry or (used_pc and not _retry_without_precond):
+                    return retry()
+                return x.to(orig_dtype).to(orig_device), _info(0, r_true_norm, False, 7, r_true_norm, float("nan"),
+                                                               used_pc)
+            init_true = r_true_norm if r_true_norm > 1e-16 else 1.0
+            tol_abs = max(tol * init_true, tol * 1e-12, 1e-12)
+        else:
+            if not math.isfinite(r_true_norm):
+                if can_retry:
+                    return retry()
+                return x.to(orig_dtype).to(orig_device), _info(total_iters, r_true_norm, False, 6, r_true_norm, tol_abs,
+                                                               used_pc)
+            r_norm = beta
+            if r_true_norm <= tol_abs:
+                return x.to(orig_dtype).to(orig_device), _info(total_iters, r_true_norm, True, 0, r_true_norm, tol_abs,
+                                                               used_pc, converged_on="true")
+            if total_iters >= maxiter:
+                break
+        if live_control_poll_fn is not None:
+            try:
+                state = live_control_poll_fn() or {}
+            except Exception:
+                state = {}
+            if state.get("terminate"):
+                return x.to(orig_dtype).to(orig_device), _info(total_iters, float("nan"), False, 2, r_true_norm,
+                                                               tol_abs, used_pc)
+        steps = min(restart, maxiter - total_iters)
+        if want_graph and steps == restart:
+            if graph is None:
+                # warm the operator's lazy state outside the capture
+                torch.cuda.synchronize(dev)
+                s = torch.cuda.Stream(device=dev)
+                s.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.stream(s):
+                    inner_steps(1)
+                torch.cuda.current_stream(dev).wait_stream(s)
+                torch.cuda.synchronize(dev)
+                start_cycle()  # the warm-up step overwrote w/H; recompute the start state
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph):
+                    inner_steps(restart)
+            graph.replay()
+        else:
+            inner_steps(steps)
+        total_iters += steps
+        scal = K.scal.cpu()
+        breakdown = int(scal[2]) if scal[2] >= 0 else -1
+        nonfinite = bool(scal[3] != 0)
+        ests = scal[4:4 + steps].tolist()
+        if callback is not None:
+            ctx = dict(callback_context or {})
+            ctx.setdefault("pass_index", int(pass_index))
+            for k, e in enumerate(ests if breakdown < 0 else ests[:breakdown]):
+                try:
+                    callback(total_iters - steps + k + 1, float(e), dict(ctx, arnoldi_dim=k + 1))
+                except Exception:
+                    pass
+        m_use = breakdown if breakdown >= 0 else steps
+        if breakdown >= 0 and can_retry:
+            return retry()
+        if nonfinite:
+            bad = next((k for k, e in enumerate(ests) if not math.isfinite(e)), steps)
+            if bad < m_use:
+                if can_retry:
+                    return retry()
+                return x.to(orig_dtype).to(orig_device), _info(total_iters, float("nan"), False, 5, r_true_norm,
+                                                               tol_abs, used_pc)
+        if m_use == 0:
+            if can_retry:
+                return retry()
+            return x.to(orig_dtype).to(orig_device), _info(total_iters, r_norm, False, 2, r_true_norm, tol_abs, used_pc)
+        K.update(m_use, x)
+    if can_retry:
+        return retry()
+    return x.to(orig_dtype).to(orig_device), _info(total_iters, r_norm, False, 1, r_true_norm, tol_abs, used_pc)
+
+
+__all__ = ["DiagonalPreconditioner", "setup_preconditioner", "gmres_restart"]

@@ -232,6 +232,24 @@ extern "C" EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids, const
                         static_cast<cudaStream_t>(stream));
 }
 
+extern "C" EDFMM_API size_t edfmm_dense_workspace_bytes(int64_t n, int dtype) {
+    return n > 0 ? dense_scratch_bytes(n, dtype) : 0;
+}
+
+extern "C" EDFMM_API int edfmm_dense_matvec_ws(const void *centroids, const void *sigma, const void *areas,
+                                               const void *self_integrals, int64_t n, int dtype, double k_e, void *out,
+                                               void *workspace, size_t workspace_bytes, void *stream) {
+    if (n < 0) return fail(EDFMM_ERR_ARG, "n must be >= 0");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (n == 0) return EDFMM_OK;
+    if (!centroids || !sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "centroids, sigma, areas, out must be non-NULL");
+    const size_t bytes = dense_scratch_bytes(n, dtype);
+    if (bytes && (!workspace || workspace_bytes < bytes))
+        return fail(EDFMM_ERR_ARG, "workspace smaller than edfmm_dense_workspace_bytes(n, dtype)");
+    return dense_matvec(centroids, sigma, areas, self_integrals, n, dtype, k_e, out, workspace,
+                        static_cast<cudaStream_t>(stream));
+}
+
 extern "C" EDFMM_API int edfmm_dense_matvec(const void *centroids, const void *sigma, const void *areas,
                                             const void *self_integrals, int64_t n, int dtype, double k_e, void *out,
                                             void *stream) {

@@ -195,6 +195,40 @@ EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids_dev, const void *
                                          void *out_dev, void *stream);
 
 /*
+ * Dense operator with a caller-provided workspace of
+ * edfmm_dense_workspace_bytes(n, dtype) bytes (may be 0): allocates nothing,
+ * so it can be captured in a CUDA graph.  Same math as edfmm_dense_matvec.
+ */
+EDFMM_API size_t edfmm_dense_workspace_bytes(int64_t n, int dtype);
+EDFMM_API int edfmm_dense_matvec_ws(const void *centroids_dev, const void *sigma_dev, const void *areas_dev,
+                                    const void *self_integrals_dev, int64_t n, int dtype, double k_e, void *out_dev,
+                                    void *workspace_dev, size_t workspace_bytes, void *stream);
+
+/*
+ * Device Krylov arithmetic of restarted left-preconditioned GMRES
+ * (gmres_restart, electrodrive/core/bem_solver.py:125-920).  Vectors in
+ * `dtype`; inner products, H (restart+1, restart) row-major, g, cs, sn and
+ * scal are FP64.  pinv (n,) is the diagonal left preconditioner or NULL.
+ * scal (5 + restart doubles): [0] |b - Ax| at cycle start, [1] beta = |M(b - Ax)|,
+ * [2] first breakdown step or -1, [3] non-finite flag, [4 + j] |g_{j+1}| after
+ * step j.  work: edfmm_gmres_work_bytes(n, restart) bytes, zeroed once.
+ *   start:   V0 = M(b - ax) / beta, g = beta e1                (bem_solver.py:399-450)
+ *   arnoldi: w = M av, CGS2 against V0..Vj, H[:, j], Givens,
+ *            g, V_{j+1} = w / H[j+1, j]                          (bem_solver.py:536-616)
+ *   update:  y = R^{-1} g[0:m], x += V[0:m]^T y                  (bem_solver.py:762-772)
+ * All stream-ordered, no host synchronisation, no allocation.
+ */
+EDFMM_API size_t edfmm_gmres_work_bytes(int64_t n, int restart);
+EDFMM_API int edfmm_gmres_start(int64_t n, int dtype, int restart, const void *b_dev, const void *ax_dev,
+                                const void *pinv_dev, void *v0_dev, void *g_dev, void *scal_dev, void *work_dev,
+                                void *stream);
+EDFMM_API int edfmm_gmres_arnoldi(int64_t n, int dtype, int restart, int j, void *V_dev, const void *av_dev,
+                                  const void *pinv_dev, void *H_dev, void *g_dev, void *cs_dev, void *sn_dev,
+                                  void *scal_dev, void *w_dev, void *work_dev, void *stream);
+EDFMM_API int edfmm_gmres_update(int64_t n, int dtype, int restart, int m, const void *V_dev, const void *H_dev,
+                                 const void *g_dev, void *x_dev, void *work_dev, void *stream);
+
+/*
  * Number of the library's own kernel launches issued since load (all
  * threads).  Used by benchmarks to report launches inside a timed region.
  */

@@ -124,8 +124,54 @@ def save_fmm_case(name, n, seed, dtype, leaf, theta, p):
     print(f"fmm_{name}: N={n} ref-FMM vs dense rel-L2 {rel:.3e} ({t1 - t0:.1f}s per matvec incl. setup)")
 
 
+def save_gmres_cases():
+    """electrodrive/core/bem_solver.py:125 gmres_restart on seeded dense systems."""
+    from electrodrive.core.bem_solver import gmres_restart, setup_preconditioner
+
+    cases = {}
+    g = torch.Generator().manual_seed(40)
+    # SPD 8x8 (as in the reference's tests/test_gmres.py), restart 8
+    Q = torch.randn(8, 8, generator=g, dtype=torch.float64)
+    cases["spd8"] = (Q @ Q.T + 8 * torch.eye(8, dtype=torch.float64), 8, 1e-8, 200, None)
+    # nonsymmetric, diagonally weighted, 120x120, restart 10, Jacobi
+    B = torch.randn(120, 120, generator=g, dtype=torch.float64) / 12 + torch.diag(1 + torch.rand(120, generator=g,
+                                                                                                  dtype=torch.float64) * 5)
+    cases["nonsym120_jacobi"] = (B, 10, 1e-10, 400, "jacobi")
+    # single-layer-like matrix on 300 random points, restart 20, Jacobi:
+    # A_ij = 1 / (300 |p_i - p_j|) (i != j), A_ii = 2 + u_i; the test rebuilds
+    # it from the stored points and diagonal
+    p = torch.rand(300, 3, generator=g, dtype=torch.float64)
+    diag = 2.0 + torch.rand(300, generator=g, dtype=torch.float64)
+    d = torch.sqrt(((p[:, None, :] - p[None, :, :]) ** 2).sum(-1))
+    K = 1.0 / (300.0 * (d + torch.eye(300, dtype=torch.float64)))
+    K.fill_diagonal_(0.0)
+    K += torch.diag(diag)
+    cases["bemlike300_jacobi"] = (K, 20, 1e-10, 600, "jacobi")
+    # maxiter reached
+    cases["nonsym120_maxiter"] = (B, 4, 1e-14, 7, None)
+    out = {}
+    for name, (Amat, restart, tol, maxiter, pc) in cases.items():
+        n = Amat.shape[0]
+        b = torch.randn(n, generator=g, dtype=torch.float64)
+        M = setup_preconditioner(pc, A_diag=torch.diag(Amat)) if pc else None
+        x, info = gmres_restart(A=lambda v, Am=Amat: Am @ v, b=b, M=M, restart=restart, tol=tol, maxiter=maxiter)
+        if name.startswith("bemlike"):
+            out[f"{name}__points"] = p.numpy()
+            out[f"{name}__diag"] = diag.numpy()
+        else:
+            out[f"{name}__A"] = Amat.numpy()
+        out[f"{name}__b"] = b.numpy()
+        out[f"{name}__x"] = x.numpy()
+        out[f"{name}__meta"] = np.array([restart, tol, maxiter, 1.0 if pc else 0.0, info["iters"], info["code"],
+                                         float(info["resid"])])
+        print(f"gmres {name}: iters={info['iters']} code={info['code']} resid={info['resid']:.3e}")
+    np.savez_compressed(os.path.join(HERE, "gmres_cases.npz"), **out)
+
+
 def main():
-    which = sys.argv[1:] or ["trees", "fmm"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres"]
+    if "gmres" in which:
+        save_gmres_cases()
     if "trees" in which:
         save_tree_case("uniform4096_f32", "uniform", 4096, 0, torch.float32, 64, 0.5)
         save_tree_case("clusters3000_f32", "clusters", 3000, 1, torch.float32, 32, 0.5)
