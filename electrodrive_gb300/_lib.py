@@ -88,6 +88,16 @@ def _declare(L):
         "edfmm_dense_matvec_noalloc": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_workspace_bytes": (C.c_size_t, [i64, i32]),
         "edfmm_dense_matvec_ws": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp, C.c_size_t, _vp]),
+        "edfmm_dense_potential_targets": (i32, [_vp, i64, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
+        "edfmm_self_integrals": (i32, [_vp, _vp, i64, i32, i32, dbl, _vp, _vp]),
+        "edfmm_near_create": (i32, [_vp, _vp, _vp, i64, dbl, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
+        "edfmm_near_destroy": (i32, [_vp]),
+        "edfmm_near_num_pairs": (i64, [_vp]),
+        "edfmm_near_export": (i32, [_vp, _vp, _vp, _vp]),
+        "edfmm_near_apply": (i32, [_vp, _vp, _vp, _vp, _vp]),
+        "edfmm_near_rows": (i32, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+        "edfmm_near_quadrature_matvec": (i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, i64, dbl, i32, i32, _vp, _vp]),
+        "edfmm_point_charge_potential": (i32, [_vp, i64, _vp, i32, dbl, i32, _vp, _vp]),
         "edfmm_gmres_work_bytes": (C.c_size_t, [i64, i32]),
         "edfmm_gmres_start": (i32, [i64, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "edfmm_gmres_arnoldi": (i32, [i64, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

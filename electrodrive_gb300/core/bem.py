@@ -1,0 +1,237 @@
+"""BEM solve on the GPU (electrodrive/core/bem.py:1550-2695, one pass).
+
+``bem_solve(spec, cfg)`` runs the reference's solve section for a single
+mesh resolution (``cfg.initial_h``): mesh -> self integrals (adaptive
+near-singular quadrature, depth 3 for spheres / two planes, else 4) ->
+optional near-pair corrections (``cfg.use_near_quadrature_matvec``) ->
+single-layer operator (dense below ``fmm_threshold`` panels, FMM above) ->
+``b = bc - V_free``, ``x0 = b / I_self`` -> Jacobi-preconditioned restarted
+GMRES -> surface charge density.  The reference's h-refinement loop, energy
+bookkeeping, control-file polling and damped-Jacobi fallback are not part of
+this operator path.
+
+``solve_mixed`` is the FP32-inner / FP64-outer iterative refinement solver:
+the FP64 operator computes the true residual, an FP32 GMRES solves the
+correction equation, and the loop stops on the FP64 relative true residual.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Any, Dict, List, Optional, Tuple
+
+import numpy as np
+import torch
+from torch import Tensor
+
+from .. import _lib
+from ..utils.config import K_E, BEMConfig
+from .bem_mesh import TriMesh, generate_mesh
+from .bem_near import NearCorrection, point_charge_potential, potential_at_targets, self_integrals
+from .bem_solver import gmres_restart
+from .operators import DenseOperator, FmmOperator
+
+
+def _cget(c: Any, key: str, default=None):
+    return c.get(key, default) if isinstance(c, dict) else getattr(c, key, default)
+
+
+def quad_depths(spec: Any) -> Tuple[int, int]:
+    """(self-integral depth, near-matvec depth) as chosen in bem.py:1764-1776."""
+    types = [_cget(c, "type") for c in (_cget(spec, "conductors", []) or [])]
+    if any(t == "sphere" for t in types) or types.count("plane") >= 2:
+        return 3, 3
+    return 4, 3
+
+
+def bc_vector(spec: Any, mesh: TriMesh) -> np.ndarray:
+    """Per-panel Dirichlet value of its conductor (bem.py:373-403)."""
+    id_to_v: Dict[int, float] = {}
+    for i, c in enumerate(_cget(spec, "conductors", []) or []):
+        try:
+            v = float(_cget(c, "potential", 0.0))
+        except Exception:
+            v = 0.0
+        id_to_v[int(_cget(c, "id", i))] = v
+    return np.asarray([id_to_v.get(int(cid), 0.0) for cid in mesh.conductor_ids], dtype=np.float64)
+
+
+def point_charges(spec: Any) -> List[Tuple[float, Tuple[float, float, float]]]:
+    out = []
+    for ch in _cget(spec, "charges", []) or []:
+        if _cget(ch, "type") != "point":
+            continue
+        try:
+            out.append((float(_cget(ch, "q")), tuple(float(x) for x in _cget(ch, "pos"))))
+        except Exception:
+            continue
+    return out
+
+
+class BEMOperator:
+    """A(sigma) = single-layer operator (+ near correction); capturable."""
+
+    capturable = True
+
+    def __init__(self, base, near: Optional[NearCorrection] = None):
+        self.base = base
+        self.near = near
+        self.n = base.n
+        self.device, self.dtype = base.device, base.dtype
+
+    def __call__(self, sigma: Tensor, out: Optional[Tensor] = None) -> Tensor:
+        v = self.base(sigma, out)
+        if self.near is not None and self.near.n_pairs > 0:
+            self.near.apply(sigma, v, v)
+        return v
+
+
+def build_operator(centroids, areas, self_corr: Tensor, *, dtype: torch.dtype, kind: str = "auto",
+                   fmm_threshold: int = 20000, near: Optional[NearCorrection] = None, leaf_size: int = 64,
+                   theta: float = 0.5, expansion_order: int = 8, device=None) -> BEMOperator:
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    n = int(np.asarray(areas).shape[0]) if not isinstance(areas, Tensor) else int(areas.shape[0])
+    use_fmm = kind == "fmm" or (kind == "auto" and n >= fmm_threshold)
+    c = torch.as_tensor(np.asarray(centroids) if not isinstance(centroids, Tensor) else centroids)
+    a = torch.as_tensor(np.asarray(areas) if not isinstance(areas, Tensor) else areas)
+    if use_fmm:
+        plan = _lib.Plan(c.to(dev, dtype).contiguous(), leaf_size=leaf_size, mac_theta=theta,
+                         expansion_order=expansion_order)
+        base = FmmOperator(plan, a.to(dev, dtype), self_corr.to(dev, dtype))
+    else:
+        base = DenseOperator(c, a, self_corr, dtype=dtype, device=dev)
+    return BEMOperator(base, near)
+
+
+@dataclass
+class BEMSolution:
+    """Panel solution with the reference's evaluation entry points (bem.py:1367-1542)."""
+
+    centroids: Tensor
+    areas: Tensor
+    sigma: Tensor
+    charges: List[Tuple[float, Tuple[float, float, float]]] = field(default_factory=list)
+
+    def eval(self, points: Tensor) -> Tensor:
+        """Total potential V_free + V_induced at points (N, 3) (dense induced part)."""
+        pts = torch.as_tensor(points).to(self.sigma.device, self.sigma.dtype).reshape(-1, 3).contiguous()
+        v = potential_at_targets(pts, self.centroids, self.sigma, self.areas)
+        if self.charges:
+            v = v + point_charge_potential(pts, self.charges)
+        return v
+
+
+def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,
+              *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
+              use_graph: bool = True, self_integral: str = "auto") -> Dict[str, Any]:
+    """One solve pass.  ``self_integral``: "auto" follows the reference
+    (quadrature self terms only when a near-quadrature option is on, else the
+    equal-area disk value 2 pi K_E sqrt(A / pi), bem.py:1747-1816), or force
+    "quadrature" / "disk"."""
+    if differentiable:
+        raise NotImplementedError("the differentiable (xitorch) path is not part of electrodrive_gb300")
+    cfg = cfg or BEMConfig()
+    _lib.load_library()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dtype = torch.float64 if getattr(cfg, "fp64", False) else torch.float32
+    h = float(getattr(cfg, "initial_h", 0.2))
+    t0 = time.perf_counter()
+    mesh = mesh if mesh is not None else generate_mesh(spec, h)
+    N = mesh.n_panels
+    if N == 0:
+        return {"error": "empty mesh"}
+    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
+    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
+    PV = mesh.vertices[mesh.triangles]
+    depth_self, depth_near = quad_depths(spec)
+    order = int(getattr(cfg, "near_quadrature_order", 2))
+    use_quad = self_integral == "quadrature" or (self_integral == "auto" and (
+        bool(getattr(cfg, "use_near_quadrature_matvec", False)) or bool(getattr(cfg, "use_near_quadrature", False))))
+    if use_quad:
+        I_self = self_integrals(PV, mesh.centroids, order=order, depth=depth_self, device=dev)
+    else:
+        a = np.clip(mesh.areas, 0.0, None)
+        I_self = torch.as_tensor(np.where(mesh.areas > 0, 2.0 * np.pi * K_E * np.sqrt(a / np.pi), 0.0),
+                                 dtype=torch.float64, device=dev)
+    A_dev = A64.to(dev)
+    tiny = torch.finfo(dtype).tiny
+    self_corr = (I_self / A_dev.clamp_min(tiny)).to(dtype)
+    near = None
+    if getattr(cfg, "use_near_quadrature_matvec", False) and N > 1:
+        near = NearCorrection(mesh.centroids, mesh.areas, PV,
+                              distance_factor=float(getattr(cfg, "near_quadrature_distance_factor", 1.5)),
+                              order=order, depth=depth_near, dtype=dtype, device=dev)
+    op = build_operator(C64, A64, self_corr, dtype=dtype, kind=operator, fmm_threshold=fmm_threshold, near=near,
+                        device=dev)
+    charges = point_charges(spec)
+    C_dev = C64.to(dev, dtype)
+    V_free = point_charge_potential(C_dev, charges) if charges else torch.zeros(N, dtype=dtype, device=dev)
+    bc = torch.as_tensor(bc_vector(spec, mesh), dtype=dtype, device=dev)
+    b = bc - V_free
+    diag = I_self.to(dtype).clamp_min(1e-18)
+    x0 = b / diag
+    t_setup = time.perf_counter() - t0
+    sigma, info = gmres_restart(op, b, restart=int(getattr(cfg, "gmres_restart", 256)),
+                                tol=float(getattr(cfg, "gmres_tol", 5e-8)),
+                                maxiter=int(getattr(cfg, "gmres_maxiter", 2000)),
+                                precond="jacobi" if getattr(cfg, "use_precond", True) else None, areas=A_dev.to(dtype),
+                                A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
+    V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
+    bc_resid = float(torch.max(torch.abs(V_tot - bc)))
+    torch.cuda.synchronize(dev)
+    t_total = time.perf_counter() - t0
+    sol = BEMSolution(centroids=C_dev, areas=A_dev.to(dtype), sigma=sigma, charges=charges)
+    mesh_stats = dict(n_panels=N, total_area=float(mesh.areas.sum()), bc_residual_linf=bc_resid, h_final=h,
+                      operator="fmm" if isinstance(op.base, FmmOperator) else "dense",
+                      near_pairs=0 if near is None else near.n_pairs)
+    info = dict(info)
+    info.update(setup_seconds=t_setup, total_seconds=t_total)
+    return dict(solution=sol, surface_charge_density=sigma, mesh_stats=mesh_stats, gmres_stats=info,
+                refinement_history=[dict(pass_index=0, h=h, n_panels=N, bc_resid_linf=bc_resid,
+                                         gmres_iters=info["iters"])], boundary_samples=None, sample_points=None)
+
+
+def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: Optional[Tensor] = None,
+                rtol: float = 1e-6, inner_restart: int = 40, inner_tol: float = 1e-4, inner_maxiter: int = 400,
+                max_outer: int = 30, use_graph: bool = True) -> Tuple[Tensor, Dict[str, Any]]:
+    """FP32 GMRES corrections inside FP64 iterative refinement.
+
+    Stops when ||b - A64 x|| / ||b|| <= rtol (FP64 true residual).  The FP32
+    inner solve is left-preconditioned by Jacobi with ``A_diag``.
+    """
+    dev = b.device
+    b64 = b.to(torch.float64)
+    x = torch.zeros_like(b64) if x0 is None else x0.to(torch.float64).clone()
+    bn = float(torch.linalg.norm(b64))
+    bn = bn if bn > 0 else 1.0
+    d32 = None if A_diag is None else A_diag.to(dev, torch.float32)
+    hist = []
+    inner_total = 0
+    matvec64 = 0
+    r = b64 - op64(x)
+    matvec64 += 1
+    for it in range(max_outer + 1):
+        rel = float(torch.linalg.norm(r)) / bn
+        hist.append(rel)
+        if not math.isfinite(rel):
+            return x, dict(success=False, code=6, outer=it, inner_iters=inner_total, rel_resid=rel, history=hist,
+                           matvec64=matvec64)
+        if rel <= rtol:
+            return x, dict(success=True, code=0, outer=it, inner_iters=inner_total, rel_resid=rel, history=hist,
+                           matvec64=matvec64)
+        if it == max_outer:
+            break
+        r32 = r.to(torch.float32)
+        d, info = gmres_restart(op32, r32, restart=inner_restart, tol=inner_tol, maxiter=inner_maxiter,
+                                precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph)
+        inner_total += info["iters"]
+        x = x + d.to(torch.float64)
+        r = b64 - op64(x)
+        matvec64 += 1
+    return x, dict(success=False, code=1, outer=max_outer, inner_iters=inner_total, rel_resid=hist[-1], history=hist,
+                   matvec64=matvec64)
+
+
+__all__ = ["BEMOperator", "BEMSolution", "bem_solve", "build_operator", "bc_vector", "point_charges", "quad_depths",
+           "solve_mixed"]

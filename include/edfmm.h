@@ -195,6 +195,16 @@ EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids_dev, const void *
                                          void *out_dev, void *stream);
 
 /*
+ * Induced potential at separate targets (bem_potential_targets,
+ * electrodrive/core/bem_kernel.py:233-270):
+ *   out_t = k_e sum_j sigma_j areas_j / sqrt(max(|x_t - c_j|^2, 1e-24)).
+ * targets (m, 3); stream-ordered scratch.
+ */
+EDFMM_API int edfmm_dense_potential_targets(const void *targets_dev, int64_t m, const void *centroids_dev,
+                                            const void *sigma_dev, const void *areas_dev, int64_t n, int dtype,
+                                            double k_e, void *out_dev, void *stream);
+
+/*
  * Dense operator with a caller-provided workspace of
  * edfmm_dense_workspace_bytes(n, dtype) bytes (may be 0): allocates nothing,
  * so it can be captured in a CUDA graph.  Same math as edfmm_dense_matvec.
@@ -227,6 +237,58 @@ EDFMM_API int edfmm_gmres_arnoldi(int64_t n, int dtype, int restart, int j, void
                                   void *scal_dev, void *w_dev, void *work_dev, void *stream);
 EDFMM_API int edfmm_gmres_update(int64_t n, int dtype, int restart, int m, const void *V_dev, const void *H_dev,
                                  const void *g_dev, void *x_dev, void *work_dev, void *stream);
+
+/*
+ * Singular and near-singular panel quadrature (FP64 geometry).
+ * panel_vertices (n, 3, 3), centroids (n, 3), areas (n,): FP64 device arrays.
+ *
+ * edfmm_self_integrals: I_i = sum_k k_e w_k / max(|C_i - y_k|, 1e-12) with the
+ *   adaptive rule near_singular_quadrature(C_i, panel_i, order, max_depth=depth)
+ *   (electrodrive/core/bem_quadrature.py:217-308, used at core/bem.py:1781-1805).
+ */
+EDFMM_API int edfmm_self_integrals(const void *panel_vertices_dev, const void *centroids_dev, int64_t n,
+                                   int quad_order, int depth, double k_e, void *out_dev, void *stream);
+
+/*
+ * Near-pair correction set (core/bem.py:475-734): pairs 0 < |C_i - C_j| <=
+ * f (R_i + R_j), R = sqrt(A / pi) (_build_near_pairs_for_panels), weights
+ * delta_ij = I_near(C_i, panel_j refined uniformly `depth` times) -
+ * k_e A_j / |C_i - C_j| (_precompute_near_correction_weights), stored as CSR
+ * rows by target with sources ascending.  edfmm_near_apply computes
+ * v_out = v_in + sum_j sigma_j delta_ij (_apply_near_quadrature_matvec_torch)
+ * in `dtype` (v_in may be NULL, v_out may alias v_in).
+ */
+typedef struct edfmm_near edfmm_near;
+EDFMM_API int edfmm_near_create(const void *centroids_dev, const void *areas_dev, const void *panel_vertices_dev,
+                                int64_t n, double distance_factor, int quad_order, int depth, double k_e, int dtype,
+                                void *stream, edfmm_near **near_out);
+EDFMM_API int edfmm_near_destroy(edfmm_near *near_set);
+EDFMM_API int64_t edfmm_near_num_pairs(const edfmm_near *near_set);
+/* (P, 2) int64 (i, j) pairs in row order and FP64 weights; either may be NULL */
+EDFMM_API int edfmm_near_export(const edfmm_near *near_set, int64_t *pairs_dev, double *weights_dev, void *stream);
+EDFMM_API int edfmm_near_apply(const edfmm_near *near_set, const void *sigma_dev, const void *v_in_dev,
+                               void *v_out_dev, void *stream);
+EDFMM_API int edfmm_near_rows(const edfmm_near *near_set, const int32_t **row_off_dev, const int32_t **cols_dev);
+
+/*
+ * The reference CUDA near-field module's operation (pybind
+ * near_quadrature_matvec, core/bem_near_cuda.cpp:239-271; kernel
+ * core/bem_near_cuda_kernel.cu:110-232): v_out = v_far + correction with the
+ * unrefined rule of quad_order (1 or 2) recomputed per call; pairs as CSR
+ * (row_off (n+1), cols) by target.  Arrays in `dtype`.
+ */
+EDFMM_API int edfmm_near_quadrature_matvec(const void *v_far_dev, const void *sigma_dev, const void *centroids_dev,
+                                           const void *areas_dev, const void *panel_vertices_dev,
+                                           const int32_t *row_off_dev, const int32_t *cols_dev, int64_t n,
+                                           double k_e, int quad_order, int dtype, void *v_out_dev, void *stream);
+
+/*
+ * Free-space potential of point charges at points (core/bem.py:291-320):
+ * out_i = sum_k k_e q_k / max(|x_i - r_k|, 1e-12); charges (n_charges, 4) FP64
+ * rows (q, x, y, z) on the device; points / out in `dtype`.
+ */
+EDFMM_API int edfmm_point_charge_potential(const void *points_dev, int64_t n, const double *charges_dev,
+                                           int n_charges, double k_e, int dtype, void *out_dev, void *stream);
 
 /*
  * Number of the library's own kernel launches issued since load (all

@@ -743,3 +743,145 @@ ORC_API int orc_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------ */
+/* Panel quadrature (core/bem_quadrature.py:79-308, core/bem.py:475-734) */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    double x, y, z;
+} v3d;
+
+static inline v3d v3_mid(v3d a, v3d b) { return (v3d){0.5 * (a.x + b.x), 0.5 * (a.y + b.y), 0.5 * (a.z + b.z)}; }
+static inline double v3_dist(v3d a, v3d b) {
+    double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return sqrt((dx * dx + dy * dy) + dz * dz);
+}
+static inline v3d v3_cent(v3d a, v3d b, v3d c) {
+    return (v3d){(a.x + b.x + c.x) / 3.0, (a.y + b.y + c.y) / 3.0, (a.z + b.z + c.z) / 3.0};
+}
+static double tri_area_d(v3d a, v3d b, v3d c) {
+    double e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z, e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
+    double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+    return 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+}
+/* standard_triangle_quadrature (order 1 or 2) applied to 1/r */
+static double rule_sum_d(v3d a, v3d b, v3d c, v3d t, int order, double ke) {
+    double area = tri_area_d(a, b, c);
+    if (!(area > 0.0)) return 0.0;
+    if (order <= 1) return ke / fmax(v3_dist(t, v3_cent(a, b, c)), 1e-12) * area;
+    double p = 2.0 / 3.0, q = 1.0 / 6.0, s = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        double l0 = k == 0 ? p : q, l1 = k == 1 ? p : q, l2 = k == 2 ? p : q;
+        v3d y = {l0 * a.x + l1 * b.x + l2 * c.x, l0 * a.y + l1 * b.y + l2 * c.y, l0 * a.z + l1 * b.z + l2 * c.z};
+        s += ke / fmax(v3_dist(t, y), 1e-12) * (area / 3.0);
+    }
+    return s;
+}
+
+/* near_singular_quadrature at target t, summed against K_E / r */
+static double adaptive_sum_d(v3d v0, v3d v1, v3d v2, v3d t, int order, int depth, double ke) {
+    v3d tri[64][3];
+    int n = 1;
+    tri[0][0] = v0;
+    tri[0][1] = v1;
+    tri[0][2] = v2;
+    for (int d = 0; d < depth && n + 3 <= 64; ++d) {
+        int best = 0;
+        double bd = INFINITY;
+        for (int i = 0; i < n; ++i) {
+            double dd = v3_dist(v3_cent(tri[i][0], tri[i][1], tri[i][2]), t);
+            if (dd < bd) {
+                bd = dd;
+                best = i;
+            }
+        }
+        v3d a = tri[best][0], b = tri[best][1], c = tri[best][2];
+        memmove(tri[best], tri[best + 1], sizeof(v3d) * 3 * (n - best - 1));
+        n--;
+        v3d m01 = v3_mid(a, b), m12 = v3_mid(b, c), m20 = v3_mid(c, a);
+        v3d k[4][3] = {{a, m01, m20}, {m01, b, m12}, {m20, m12, c}, {m01, m12, m20}};
+        for (int i = 0; i < 4; ++i) {
+            memcpy(tri[n], k[i], sizeof(v3d) * 3);
+            n++;
+        }
+    }
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += rule_sum_d(tri[i][0], tri[i][1], tri[i][2], t, order, ke);
+    return s;
+}
+
+ORC_API void orc_self_integrals(const double *verts, const double *cent, int64_t n, int order, int depth, double ke,
+                                double *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const double *v = verts + 9 * i;
+        out[i] = adaptive_sum_d((v3d){v[0], v[1], v[2]}, (v3d){v[3], v[4], v[5]}, (v3d){v[6], v[7], v[8]},
+                                (v3d){cent[3 * i], cent[3 * i + 1], cent[3 * i + 2]}, order, depth, ke);
+    }
+}
+
+/* _build_near_pairs_for_panels: row-major (i ascending, j ascending) */
+ORC_API int64_t orc_near_pairs(const double *cent, const double *areas, int64_t n, double factor, int64_t *pairs,
+                               int64_t cap) {
+    int64_t np = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double ri = sqrt((areas[i] > 0 ? areas[i] : 0.0) / M_PI);
+        v3d ci = {cent[3 * i], cent[3 * i + 1], cent[3 * i + 2]};
+        for (int64_t j = 0; j < n; ++j) {
+            double rj = sqrt((areas[j] > 0 ? areas[j] : 0.0) / M_PI);
+            double d = v3_dist(ci, (v3d){cent[3 * j], cent[3 * j + 1], cent[3 * j + 2]});
+            double th = factor * (ri + rj);
+            if (isfinite(d) && isfinite(th) && d > 0.0 && d <= th) {
+                if (pairs && np < cap) {
+                    pairs[2 * np] = i;
+                    pairs[2 * np + 1] = j;
+                }
+                np++;
+            }
+        }
+    }
+    return np;
+}
+
+/* _precompute_near_correction_weights with uniform refinement `depth` */
+ORC_API void orc_near_weights(const double *cent, const double *areas, const double *verts, const int64_t *pairs,
+                              int64_t np, int order, int depth, double ke, double *w) {
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < np; ++p) {
+        int64_t i = pairs[2 * p], j = pairs[2 * p + 1];
+        double aj = areas[j];
+        if (!(aj > 0.0)) {
+            w[p] = 0.0;
+            continue;
+        }
+        v3d ci = {cent[3 * i], cent[3 * i + 1], cent[3 * i + 2]};
+        const double *v = verts + 9 * j;
+        int leaves = 1 << (2 * depth);
+        double s = 0.0;
+        for (int leaf = 0; leaf < leaves; ++leaf) {
+            v3d a = {v[0], v[1], v[2]}, b = {v[3], v[4], v[5]}, c = {v[6], v[7], v[8]};
+            for (int d = depth - 1; d >= 0; --d) {
+                int digit = (leaf >> (2 * d)) & 3;
+                v3d m01 = v3_mid(a, b), m12 = v3_mid(b, c), m20 = v3_mid(c, a);
+                if (digit == 0) {
+                    b = m01;
+                    c = m20;
+                } else if (digit == 1) {
+                    a = m01;
+                    c = m12;
+                } else if (digit == 2) {
+                    a = m20;
+                    b = m12;
+                } else {
+                    a = m01;
+                    b = m12;
+                    c = m20;
+                }
+            }
+            s += rule_sum_d(a, b, c, ci, order, ke);
+        }
+        double far = ke * aj / fmax(v3_dist(ci, (v3d){cent[3 * j], cent[3 * j + 1], cent[3 * j + 2]}), 1e-12);
+        w[p] = s - far;
+    }
+}

@@ -229,3 +229,49 @@ def fmm_matvec(tree: OracleTree, lists: OracleLists, points, sigma, areas, self_
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+def _declare_bem():
+    L = lib()
+    if getattr(L, "_bem_declared", False):
+        return L
+    vp, i64, i32, dbl = C.c_void_p, C.c_int64, C.c_int, C.c_double
+    L.orc_self_integrals.argtypes = [vp, vp, i64, i32, i32, dbl, vp]
+    L.orc_near_pairs.restype = i64
+    L.orc_near_pairs.argtypes = [vp, vp, i64, dbl, vp, i64]
+    L.orc_near_weights.argtypes = [vp, vp, vp, vp, i64, i32, i32, dbl, vp]
+    L._bem_declared = True
+    return L
+
+
+def self_integrals(panel_vertices, centroids, order=2, depth=3, ke=K_E) -> np.ndarray:
+    """near_singular_quadrature self terms (bem_quadrature.py:217-308, bem.py:1781-1805)."""
+    L = _declare_bem()
+    pv = np.ascontiguousarray(panel_vertices, dtype=np.float64)
+    c = np.ascontiguousarray(centroids, dtype=np.float64)
+    out = np.empty(c.shape[0])
+    L.orc_self_integrals(_p(pv), _p(c), c.shape[0], int(order), int(depth), float(ke), _p(out))
+    return out
+
+
+def near_pairs(centroids, areas, factor=1.5) -> np.ndarray:
+    """_build_near_pairs_for_panels (bem.py:475-555), O(N^2)."""
+    L = _declare_bem()
+    c = np.ascontiguousarray(centroids, dtype=np.float64)
+    a = np.ascontiguousarray(areas, dtype=np.float64)
+    n = L.orc_near_pairs(_p(c), _p(a), c.shape[0], float(factor), None, 0)
+    out = np.empty((n, 2), np.int64)
+    L.orc_near_pairs(_p(c), _p(a), c.shape[0], float(factor), _p(out), n)
+    return out
+
+
+def near_weights(centroids, areas, panel_vertices, pairs, order=2, depth=3, ke=K_E) -> np.ndarray:
+    """_precompute_near_correction_weights (bem.py:558-667)."""
+    L = _declare_bem()
+    c = np.ascontiguousarray(centroids, dtype=np.float64)
+    a = np.ascontiguousarray(areas, dtype=np.float64)
+    pv = np.ascontiguousarray(panel_vertices, dtype=np.float64)
+    pr = np.ascontiguousarray(pairs, dtype=np.int64)
+    w = np.empty(pr.shape[0])
+    L.orc_near_weights(_p(c), _p(a), _p(pv), _p(pr), pr.shape[0], int(order), int(depth), float(ke), _p(w))
+    return w

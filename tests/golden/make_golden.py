@@ -168,8 +168,133 @@ def save_gmres_cases():
     np.savez_compressed(os.path.join(HERE, "gmres_cases.npz"), **out)
 
 
+def _ref_self_integrals(C, PV, depth, order=2):
+    """The per-panel loop of electrodrive/core/bem.py:1781-1805."""
+    from electrodrive.core.bem_quadrature import near_singular_quadrature
+    from electrodrive.utils.config import K_E
+
+    vals = np.empty(C.shape[0])
+    for i in range(C.shape[0]):
+        pts, w = near_singular_quadrature(target=C[i], panel_vertices=PV[i], method="telles", order=order,
+                                          max_depth=depth)
+        r = np.maximum(np.linalg.norm(pts - C[i][None, :], axis=1), 1e-12)
+        vals[i] = float(np.sum((K_E / r) * w))
+    return vals
+
+
+def _spec(conductors, charges):
+    from electrodrive.orchestration.parser import CanonicalSpec
+
+    return CanonicalSpec.from_json(dict(domain="free", conductors=conductors, charges=charges, dielectrics=[]))
+
+
+def save_near_cases():
+    """Self integrals, near pairs, correction weights and their application
+    (electrodrive/core/bem.py:475-734, core/bem_quadrature.py:217-308)."""
+    from electrodrive.core.bem import (_apply_near_quadrature_matvec_torch, _build_near_pairs_for_panels,
+                                       _precompute_near_correction_weights)
+    from electrodrive.core.bem_mesh import generate_mesh
+
+    cases = {
+        "sphere": (dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=0.0), 0.5, 3),
+        "torus": (dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0), 0.45, 4),
+        "plane": (dict(type="plane", z=0.0, potential=0.0), 1.2, 4),
+    }
+    out = {}
+    g = torch.Generator().manual_seed(77)
+    for name, (cond, h, depth) in cases.items():
+        mesh = generate_mesh(_spec([cond], [dict(type="point", q=1.0, pos=[0.2, 0.1, 1.7])]), h)
+        C, A = mesh.centroids, mesh.areas
+        PV = np.asarray(mesh.vertices)[np.asarray(mesh.triangles)]
+        si = _ref_self_integrals(C, PV, depth)
+        pairs = _build_near_pairs_for_panels(C, A, distance_factor=1.5, n_panels=C.shape[0])
+        w = _precompute_near_correction_weights(C, A, PV, pairs, 2, max_depth=max(1, depth - 1))
+        sig = torch.randn(C.shape[0], generator=g, dtype=torch.float64)
+        v = _apply_near_quadrature_matvec_torch(torch.zeros_like(sig), sig, near_pairs=torch.as_tensor(pairs),
+                                                weights=torch.as_tensor(w))
+        for k, val in dict(centroids=C, areas=A, panel_vertices=PV, self_integrals=si, near_pairs=pairs,
+                           near_weights=w, sigma=sig.numpy(), v_corr=v.numpy(),
+                           meta=np.array([h, depth, max(1, depth - 1)])).items():
+            out[f"{name}__{k}"] = val
+        print(f"near {name}: N={C.shape[0]} pairs={pairs.shape[0]}")
+    np.savez_compressed(os.path.join(HERE, "near_cases.npz"), **out)
+
+
+def save_solve_cases():
+    """electrodrive/core/bem.py:1550 bem_solve, one pass, FP64, CPU."""
+    import tempfile
+
+    from electrodrive.core.bem import bem_solve
+    from electrodrive.utils.config import BEMConfig
+    from electrodrive.utils.logging import JsonlLogger
+
+    cases = {
+        "sphere_h05": ([dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=0.0)],
+                       [dict(type="point", q=1.0, pos=[0.0, 0.0, 2.0])], 0.5, False),
+        "torus_h045_near": ([dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0)],
+                            [dict(type="point", q=1.0, pos=[1.6, 0.3, 0.2])], 0.45, True),
+    }
+    out = {}
+    for name, (conds, charges, h, near) in cases.items():
+        cfg = BEMConfig()
+        cfg.fp64 = True
+        cfg.use_gpu = False
+        cfg.max_refine_passes = 1
+        cfg.min_refine_passes = 1
+        cfg.initial_h = h
+        cfg.use_near_quadrature_matvec = near
+        t0 = time.time()
+        res = bem_solve(_spec(conds, charges), cfg, JsonlLogger(tempfile.mkdtemp()))
+        dt = time.time() - t0
+        st = res["gmres_stats"]
+        out[f"{name}__sigma"] = np.asarray(res["surface_charge_density"], dtype=np.float64)
+        out[f"{name}__meta"] = np.array([h, float(near), st["iters"], st["code"], st["resid"], st["tol_abs"],
+                                         res["mesh_stats"]["n_panels"], res["mesh_stats"]["bc_residual_linf"], dt])
+        print(f"solve {name}: N={res['mesh_stats']['n_panels']} iters={st['iters']} code={st['code']} {dt:.1f}s")
+    np.savez_compressed(os.path.join(HERE, "solve_cases.npz"), **out)
+
+
+def save_icosphere_solve():
+    """The sphere workload (5,120 icosphere panels, unit charge at (0,0,2),
+    grounded, FP64, dense operator, GMRES(50) tol 1e-8) run through the
+    reference's own building blocks on the icosphere arrays."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from electrodrive.core.bem_kernel import bem_matvec_gpu
+    from electrodrive.core.bem_solver import gmres_restart
+    from electrodrive.utils.config import K_E
+    from electrodrive_gb300.core.bem_mesh import icosphere
+
+    mesh = icosphere(4)
+    C = torch.as_tensor(mesh.centroids)
+    A = torch.as_tensor(mesh.areas)
+    PV = mesh.vertices[mesh.triangles]
+    t0 = time.time()
+    si = torch.as_tensor(_ref_self_integrals(mesh.centroids, PV, 3))
+    self_corr = si / A
+    q, rq = 1.0, torch.tensor([0.0, 0.0, 2.0], dtype=torch.float64)
+    V_free = K_E * q / torch.linalg.norm(C - rq[None, :], dim=1).clamp_min(1e-12)
+    b = torch.zeros_like(A) - V_free
+    x0 = b / si.clamp_min(1e-18)
+    t1 = time.time()
+    mv = lambda s: bem_matvec_gpu(sigma=s, src_centroids=C, areas=A, tile_size=1024, self_integrals=self_corr,
+                                  backend="torch_tiled")
+    sigma, info = gmres_restart(mv, b, restart=50, tol=1e-8, maxiter=2000, precond="jacobi", areas=A, A_diag=si,
+                                x0=x0)
+    t2 = time.time()
+    np.savez_compressed(os.path.join(HERE, "icosphere5120_solve.npz"), self_integrals=si.numpy(),
+                        sigma=sigma.numpy(), meta=np.array([info["iters"], info["code"], info["resid"],
+                                                            info["tol_abs"], t1 - t0, t2 - t1]))
+    print(f"icosphere solve: iters={info['iters']} code={info['code']} setup {t1 - t0:.1f}s solve {t2 - t1:.1f}s")
+
+
 def main():
-    which = sys.argv[1:] or ["trees", "fmm", "gmres"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico"]
+    if "near" in which:
+        save_near_cases()
+    if "solve" in which:
+        save_solve_cases()
+    if "ico" in which:
+        save_icosphere_solve()
     if "gmres" in which:
         save_gmres_cases()
     if "trees" in which:
