@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["fmm_matvec", "sphere_solve", "torus_solve"], default="fmm_matvec",
+                    help="fmm_matvec: the headline operator benchmark; sphere_solve: 5,120-panel icosphere dense "
+                         "FP64 solve; torus_solve: 200,000-panel torus, FMM + near correction, mixed-precision solve")
     return ap.parse_args()
 
 
@@ -175,11 +178,298 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+SPHERE_WORKLOAD = "sphere_solve_icosphere5120_q1_at_0_0_2_grounded_dense_fp64_gmres50_tol1e-8"
+TORUS_WORKLOAD = ("torus_solve_R1_r0.35_grid500x200_200000panels_V1_q1_at_1.6_0.3_0.2_fmm_p8_leaf64_theta0.5_"
+                  "near1.5_depth3_self_depth4_mixed_fp32_gmres40_in_fp64_refinement_rtol1e-6")
+
+
+def _solve_case(name):
+    """Mesh, conductor spec and solver settings of the two solve workloads."""
+    from electrodrive_gb300.core.bem_mesh import icosphere, torus_mesh
+
+    if name == "sphere_solve":
+        spec = dict(conductors=[dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=0.0)],
+                    charges=[dict(type="point", q=1.0, pos=[0.0, 0.0, 2.0])])
+        return icosphere(4), spec, dict(depth_self=3, near=False, kind="dense")
+    spec = dict(conductors=[dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0)],
+                charges=[dict(type="point", q=1.0, pos=[1.6, 0.3, 0.2])])
+    return torus_mesh(1.0, 0.35, 500, 200), spec, dict(depth_self=4, near=True, kind="fmm")
+
+
+def _solve_system(mesh, spec, opts, dev, dtypes):
+    """Device-resident operator(s), right-hand side, Jacobi diagonal and x0
+    exactly as bem_solve assembles them."""
+    import numpy as np
+    import torch
+
+    from electrodrive_gb300.core.bem import bc_vector, build_operator, point_charges
+    from electrodrive_gb300.core.bem_near import NearCorrection, point_charge_potential, self_integrals
+
+    PV = mesh.vertices[mesh.triangles]
+    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
+    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
+    I_self = self_integrals(PV, mesh.centroids, order=2, depth=opts["depth_self"], device=dev)
+    A_dev = A64.to(dev)
+    self_corr = I_self / A_dev.clamp_min(torch.finfo(torch.float64).tiny)
+    ops = {}
+    for dt in dtypes:
+        near = (NearCorrection(mesh.centroids, mesh.areas, PV, distance_factor=1.5, order=2, depth=3, dtype=dt,
+                               device=dev) if opts["near"] else None)
+        ops[dt] = build_operator(C64, A64, self_corr.to(dt), dtype=dt, kind=opts["kind"], near=near, device=dev)
+    V_free = point_charge_potential(C64.to(dev), point_charges(spec))
+    b = torch.as_tensor(bc_vector(spec, mesh), dtype=torch.float64, device=dev) - V_free
+    diag = I_self.clamp_min(1e-18)
+    return dict(ops=ops, b=b, diag=diag, x0=b / diag, A=A_dev, C=C64, n=mesh.n_panels,
+                near_pairs=0 if not opts["near"] else ops[dtypes[0]].near.n_pairs)
+
+
+def _time_cuda(fn, dev, stream, flush, warmup, steps):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize(dev)
+    ms = []
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def _solve_cpu_baseline(name, mesh, spec, opts, plain_matvecs=None):
+    """The oracle's FP64 restatement on all host cores: the whole dense solve
+    (sphere) or one FP64 FMM + near-correction application (torus)."""
+    import numpy as np
+
+    from electrodrive_gb300.core.bem import bc_vector, point_charges
+    from oracle import gmres_ref
+    from oracle import oracle as O
+
+    O.lib()
+    C, A = mesh.centroids, mesh.areas
+    PV = mesh.vertices[mesh.triangles]
+    t0 = time.perf_counter()
+    si = O.self_integrals(PV, C, 2, opts["depth_self"])
+    q = [(qq, np.asarray(pos)) for qq, pos in point_charges(spec)]
+    vf = sum(qq * O.K_E / np.maximum(np.linalg.norm(C - pos, axis=1), 1e-12) for qq, pos in q)
+    b = bc_vector(spec, mesh) - vf
+    diag = np.maximum(si, 1e-18)
+    if name == "sphere_solve":
+        x, info = gmres_ref.gmres_restart(lambda v: O.dense_matvec(C, v, A, si / A), b, 1.0 / diag, restart=50,
+                                          tol=1e-8, maxiter=2000, x0=b / diag)
+        dt = time.perf_counter() - t0
+        return {"value": 1.0 / dt, "unit": "solves/s", "cores": O.num_threads(), "kind": "port",
+                "sample": f"one whole FP64 solve (self integrals, dense operator, MGS GMRES(50)) of the same "
+                          f"{mesh.n_panels}-panel system: {info['iters']} iterations, {dt:.2f} s"}
+    t = O.build_tree(C, 64, 32)
+    lists = O.build_lists(t, 0.5)
+    pairs = O.near_pairs(C, A, 1.5)
+    w = O.near_weights(C, A, PV, pairs, 2, 3)
+    sig = b / diag
+    t1 = time.perf_counter()
+    v = O.fmm_matvec(t, lists, C, sig, A, si / A, p=8)
+    np.add.at(v, pairs[:, 0], w * sig[pairs[:, 1]])
+    dt = time.perf_counter() - t1
+    nmv = plain_matvecs or 1
+    return {"value": 1.0 / (dt * nmv), "unit": "solves/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"one FP64 FMM (p=8) + near-correction application of the {mesh.n_panels}-panel operator "
+                      f"({dt:.2f} s, tree/lists/pairs/weights prebuilt) times the {nmv} operator applications "
+                      f"the plain FP64 GPU solve needed"}
+
+
+def run_solve_workload(args, rank, world, local):
+    """sphere_solve / torus_solve: one BEM solve per step (solves/s)."""
+    import numpy as np
+
+    name = args.workload
+    workload = SPHERE_WORKLOAD if name == "sphere_solve" else TORUS_WORKLOAD
+    mesh, spec, opts = _solve_case(name)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = [_solve_cpu_baseline(name, mesh, spec, opts)["value"] for _ in range(max(1, args.steps))]
+        cpu = _solve_cpu_baseline(name, mesh, spec, opts)
+        val = float(np.mean(vals))
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": 0, "ms_per_step": 1e3 / val,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": {"workload": workload, "n_panels": mesh.n_panels},
+                          "cpu_baseline": dict(cpu, value=val),
+                          "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+
+    import torch
+
+    from electrodrive_gb300 import _lib
+    from electrodrive_gb300.core.bem import bem_solve, solve_mixed
+    from electrodrive_gb300.core.bem_solver import gmres_restart
+    from electrodrive_gb300.utils.config import BEMConfig
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    t_setup = time.perf_counter()
+    dtypes = [torch.float64] if name == "sphere_solve" else [torch.float64, torch.float32]
+    sysd = _solve_system(mesh, spec, opts, dev, dtypes)
+    torch.cuda.synchronize(dev)
+    t_setup = time.perf_counter() - t_setup
+    op64 = sysd["ops"][torch.float64]
+    b, diag, x0, n = sysd["b"], sysd["diag"], sysd["x0"], sysd["n"]
+    bn = float(torch.linalg.norm(b))
+    result = {}
+
+    if name == "sphere_solve":
+        def step():
+            result["x"], result["info"] = gmres_restart(op64, b, restart=50, tol=1e-8, maxiter=2000, precond="jacobi",
+                                                        areas=sysd["A"], A_diag=diag, x0=x0, use_graph=True)
+    else:
+        op32 = sysd["ops"][torch.float32]
+
+        def step():
+            result["x"], result["info"] = solve_mixed(op64, op32, b, A_diag=diag, x0=x0, rtol=1e-6,
+                                                      inner_restart=40)
+
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        step()
+    torch.cuda.synchronize(dev)
+    l0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        times = _time_cuda(step, dev, stream, flush, 0, args.steps)
+    launches = _lib.launch_count() - l0
+    ms = sum(times) / len(times)
+    value = world * 1e3 / ms
+    x, info = result["x"], result["info"]
+    true_rel = float(torch.linalg.norm(b - op64(x.to(torch.float64))) / bn)
+
+    # operator application timing and roofline of the dominant kernel
+    sig = x0.clone()
+    mv = {}
+    for dt, op in sysd["ops"].items():
+        s_dt = sig.to(dt)
+        mv[str(dt).replace("torch.", "")] = statistics.median(_time_cuda(lambda: op(s_dt), dev, stream, flush, 3, 10))
+    extra = {}
+    if name == "sphere_solve":
+        peak = _lib.measure_fp64_peak()
+        flops = 20.0 * n * n
+        achieved = flops / (mv["float64"] * 1e-3) / 1e12
+        roof = {"kernel": "k_dense_partial<double> (dense FP64 operator)", "bound": "fp64", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "FP64 FMA probe measured in this run (edfmm_measure_fp64_peak)",
+                "flops_per_matvec": flops}
+        # Kelvin image and exterior potential
+        from electrodrive_gb300.core.bem import BEMSolution
+
+        xs = x.double().cpu().numpy()
+        c = mesh.centroids
+        d = np.linalg.norm(c - np.array([0.0, 0.0, 2.0]), axis=1)
+        sig_k = -(4.0 - 1.0) / (4 * np.pi * d ** 3)
+        g = torch.Generator().manual_seed(2)
+        u = torch.randn(1000, 3, generator=g, dtype=torch.float64)
+        u = u / u.norm(dim=1, keepdim=True)
+        r = 1.2 + 1.8 * torch.rand(1000, 1, generator=g, dtype=torch.float64)
+        pts = (u * r).numpy()
+        sol = BEMSolution(centroids=sysd["C"].to(dev), areas=sysd["A"], sigma=x.double(), charges=[(1.0, (0, 0, 2.0))])
+        v = sol.eval(torch.as_tensor(pts, device=dev)).cpu().numpy()
+        from electrodrive_gb300.utils.config import K_E
+
+        vk = K_E * (1.0 / np.linalg.norm(pts - [0, 0, 2.0], axis=1) - 0.5 / np.linalg.norm(pts - [0, 0, 0.5], axis=1))
+        extra = {"sigma_rel_l2_vs_kelvin": float(np.linalg.norm(xs - sig_k) / np.linalg.norm(sig_k)),
+                 "exterior_potential_rel_l2_vs_kelvin_1000pts": float(np.linalg.norm(v - vk) / np.linalg.norm(vk))}
+        cfg = BEMConfig(fp64=True, gmres_restart=50, gmres_tol=1e-8, gmres_maxiter=2000)
+        e2e_call = lambda: bem_solve(spec, cfg, mesh=mesh, operator="dense", self_integral="quadrature")
+        h2d = n * 8 * (3 + 1 + 9 + 3 + 1)
+    else:
+        # plain FP64 GMRES (the reference's method and restart) to the same true residual
+        op32 = sysd["ops"][torch.float32]
+        r0 = float(torch.linalg.norm(b - op64(x0)))
+        plain = {}
+
+        def plain_solve():
+            plain["x"], plain["info"] = gmres_restart(op64, b, restart=256, tol=1e-6 * bn / r0, maxiter=4000,
+                                                      precond="jacobi", areas=sysd["A"], A_diag=diag, x0=x0,
+                                                      use_graph=True)
+        t_plain = _time_cuda(plain_solve, dev, stream, flush, 0, 1)[0]
+        pinfo = plain["info"]
+        plain_rel = float(torch.linalg.norm(b - op64(plain["x"])) / bn)
+        p64 = op64.base.plan
+        p32 = op32.base.plan
+        fp32_peak = _lib.measure_fp32_peak()
+        p32.set_charges(sig.float() * sysd["A"].float())
+        m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 2, 5))
+        achieved = p32.info.n_m2l_pairs * M2L_FLOPS_PER_PAIR / (m2l_ms * 1e-3) / 1e12
+        roof = {"kernel": "k_m2l_fast (M2L of the FP32 inner operator)", "bound": "fp32", "achieved": achieved,
+                "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
+                "traffic": 2 * M2L_DRAM_BYTES_PER_PAIR_PER_PASS * p32.info.n_m2l_pairs,
+                "traffic_note": "scaled from an ncu capture of the same kernel at N=262,144 (uniform cube)",
+                "peak_source": "FP32 FMA probe measured in this run (edfmm_measure_fp32_peak)"}
+        extra = {"plain_fp64_gmres": {"solves_per_s": 1e3 / t_plain, "ms": t_plain, "iters": pinfo["iters"],
+                                      "code": pinfo["code"], "true_rel_resid": plain_rel, "restart": 256},
+                 "mixed_speedup_vs_plain_fp64": t_plain / ms,
+                 "sigma_rel_l2_mixed_vs_plain_fp64": float(torch.linalg.norm(x - plain["x"]) /
+                                                           torch.linalg.norm(plain["x"])),
+                 "outer_iters": info["outer"], "inner_iters": info["inner_iters"], "fp64_matvecs": info["matvec64"],
+                 "n_nodes_fp32": p32.info.n_nodes, "n_m2l_pairs_fp32": p32.info.n_m2l_pairs,
+                 "n_p2p_pairs_fp32": p32.info.n_p2p_pairs, "p2p_interactions_fp32": p32.info.p2p_interactions,
+                 "n_m2l_pairs_fp64": p64.info.n_m2l_pairs, "m2l_fp32_ms": m2l_ms}
+        plain_matvecs = pinfo["iters"] + pinfo["iters"] // 256 + 2
+        cfg = BEMConfig(use_near_quadrature_matvec=True)
+        e2e_call = lambda: bem_solve(spec, cfg, mesh=mesh, operator="fmm", self_integral="quadrature", mixed=True,
+                                     mixed_rtol=1e-6, inner_restart=40)
+        h2d = n * 8 * (3 + 1 + 9 + 3 + 1) * 2
+
+    # end to end through the public API: host mesh -> solve -> host sigma
+    e2e_ms = []
+    for i in range(1 + args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = e2e_call()
+        sig_host = res["surface_charge_density"].cpu()
+        if i:
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_val = world * 1e3 / (sum(e2e_ms) / len(e2e_ms))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = _solve_cpu_baseline(name, mesh, spec, opts,
+                                      None if name == "sphere_solve" else plain_matvecs)
+        except Exception as e:
+            cpu = {"value": None, "error": str(e)[:200]}
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+               "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64" if name == "sphere_solve" else "f32+f64", "data": "synthetic",
+               "config": {"workload": workload, "n_panels": n, "near_pairs": sysd["near_pairs"],
+                          "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
+                          "setup_s": t_setup},
+               "solve": {"iters": info.get("iters", info.get("inner_iters")), "code": info["code"],
+                         "true_rel_resid": true_rel, **extra},
+               "matvec_ms": mv,
+               "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * n,
+                       "ms_per_step": sum(e2e_ms) / len(e2e_ms),
+                       "includes": "set-up from the host mesh (self integrals, near pairs and weights, trees and "
+                                   "lists), the solve and the sigma read-back"},
+               "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload != "fmm_matvec":
+        run_solve_workload(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

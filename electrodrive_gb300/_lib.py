@@ -84,6 +84,7 @@ def _declare(L):
         "edfmm_plan_p2p": (i32, [_vp, _vp, _vp]),
         "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
+        "edfmm_measure_fp64_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
         "edfmm_dense_matvec": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_matvec_noalloc": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_workspace_bytes": (C.c_size_t, [i64, i32]),
@@ -156,8 +157,19 @@ def dtype_code(dt: torch.dtype) -> int:
     raise ValueError(f"unsupported dtype {dt}; expected float32 or float64")
 
 
+_replayed_launches = 0
+
+
+def note_graph_replay(kernels_per_replay: int) -> None:
+    """Account the library kernels a CUDA-graph replay re-launches (the C
+    counter sees them once, when they are captured)."""
+    global _replayed_launches
+    _replayed_launches += int(kernels_per_replay)
+
+
 def launch_count() -> int:
-    return int(load_library(require_cuda=False).edfmm_launch_count())
+    """Library kernel launches so far, graph replays included."""
+    return int(load_library(require_cuda=False).edfmm_launch_count()) + _replayed_launches
 
 
 def measure_fp32_peak(iters: int = 20000) -> float:
@@ -165,6 +177,14 @@ def measure_fp32_peak(iters: int = 20000) -> float:
     L = load_library()
     out = C.c_double()
     check(L.edfmm_measure_fp32_peak(int(iters), stream_handle(), C.byref(out)), "edfmm_measure_fp32_peak")
+    return float(out.value)
+
+
+def measure_fp64_peak(iters: int = 4000) -> float:
+    """FP64 FMA throughput of the current device, TFLOP/s."""
+    L = load_library()
+    out = C.c_double()
+    check(L.edfmm_measure_fp64_peak(int(iters), stream_handle(), C.byref(out)), "edfmm_measure_fp64_peak")
     return float(out.value)
 
 

@@ -124,17 +124,20 @@ class BEMSolution:
 
 def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,
               *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
-              use_graph: bool = True, self_integral: str = "auto") -> Dict[str, Any]:
+              use_graph: bool = True, self_integral: str = "auto", mixed: bool = False, mixed_rtol: float = 1e-6,
+              inner_restart: int = 40) -> Dict[str, Any]:
     """One solve pass.  ``self_integral``: "auto" follows the reference
     (quadrature self terms only when a near-quadrature option is on, else the
     equal-area disk value 2 pi K_E sqrt(A / pi), bem.py:1747-1816), or force
-    "quadrature" / "disk"."""
+    "quadrature" / "disk".  ``mixed=True`` builds the operator (and the near
+    correction) in FP64 and FP32 and solves with :func:`solve_mixed` to an FP64
+    relative true residual of ``mixed_rtol`` (``cfg.fp64`` is then ignored)."""
     if differentiable:
         raise NotImplementedError("the differentiable (xitorch) path is not part of electrodrive_gb300")
     cfg = cfg or BEMConfig()
     _lib.load_library()
     dev = torch.device("cuda", torch.cuda.current_device())
-    dtype = torch.float64 if getattr(cfg, "fp64", False) else torch.float32
+    dtype = torch.float64 if (getattr(cfg, "fp64", False) or mixed) else torch.float32
     h = float(getattr(cfg, "initial_h", 0.2))
     t0 = time.perf_counter()
     mesh = mesh if mesh is not None else generate_mesh(spec, h)
@@ -157,13 +160,22 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     A_dev = A64.to(dev)
     tiny = torch.finfo(dtype).tiny
     self_corr = (I_self / A_dev.clamp_min(tiny)).to(dtype)
-    near = None
-    if getattr(cfg, "use_near_quadrature_matvec", False) and N > 1:
-        near = NearCorrection(mesh.centroids, mesh.areas, PV,
+    want_near = bool(getattr(cfg, "use_near_quadrature_matvec", False)) and N > 1
+
+    def make_near(dt):
+        if not want_near:
+            return None
+        return NearCorrection(mesh.centroids, mesh.areas, PV,
                               distance_factor=float(getattr(cfg, "near_quadrature_distance_factor", 1.5)),
-                              order=order, depth=depth_near, dtype=dtype, device=dev)
+                              order=order, depth=depth_near, dtype=dt, device=dev)
+
+    near = make_near(dtype)
     op = build_operator(C64, A64, self_corr, dtype=dtype, kind=operator, fmm_threshold=fmm_threshold, near=near,
                         device=dev)
+    op32 = None
+    if mixed:
+        op32 = build_operator(C64, A64, self_corr.to(torch.float32), dtype=torch.float32, kind=operator,
+                              fmm_threshold=fmm_threshold, near=make_near(torch.float32), device=dev)
     charges = point_charges(spec)
     C_dev = C64.to(dev, dtype)
     V_free = point_charge_potential(C_dev, charges) if charges else torch.zeros(N, dtype=dtype, device=dev)
@@ -172,11 +184,19 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     diag = I_self.to(dtype).clamp_min(1e-18)
     x0 = b / diag
     t_setup = time.perf_counter() - t0
-    sigma, info = gmres_restart(op, b, restart=int(getattr(cfg, "gmres_restart", 256)),
-                                tol=float(getattr(cfg, "gmres_tol", 5e-8)),
-                                maxiter=int(getattr(cfg, "gmres_maxiter", 2000)),
-                                precond="jacobi" if getattr(cfg, "use_precond", True) else None, areas=A_dev.to(dtype),
-                                A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
+    if mixed:
+        sigma, minfo = solve_mixed(op, op32, b, A_diag=diag if getattr(cfg, "use_precond", True) else None, x0=x0,
+                                   rtol=mixed_rtol, inner_restart=inner_restart, use_graph=use_graph)
+        bn = float(torch.linalg.norm(b))
+        info = dict(iters=minfo["inner_iters"], resid=minfo["rel_resid"] * bn, success=minfo["success"],
+                    code=minfo["code"], tol_abs=mixed_rtol * bn, used_preconditioner=bool(getattr(cfg, "use_precond", True)),
+                    outer=minfo["outer"], matvec64=minfo["matvec64"], history=minfo["history"], precision="mixed")
+    else:
+        sigma, info = gmres_restart(op, b, restart=int(getattr(cfg, "gmres_restart", 256)),
+                                    tol=float(getattr(cfg, "gmres_tol", 5e-8)),
+                                    maxiter=int(getattr(cfg, "gmres_maxiter", 2000)),
+                                    precond="jacobi" if getattr(cfg, "use_precond", True) else None,
+                                    areas=A_dev.to(dtype), A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
     V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
     bc_resid = float(torch.max(torch.abs(V_tot - bc)))
     torch.cuda.synchronize(dev)
@@ -194,11 +214,14 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
 
 def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: Optional[Tensor] = None,
                 rtol: float = 1e-6, inner_restart: int = 40, inner_tol: float = 1e-4, inner_maxiter: int = 400,
-                max_outer: int = 30, use_graph: bool = True) -> Tuple[Tensor, Dict[str, Any]]:
+                max_outer: int = 30, use_graph: bool = True, inner_early_exit: Optional[int] = 8
+                ) -> Tuple[Tensor, Dict[str, Any]]:
     """FP32 GMRES corrections inside FP64 iterative refinement.
 
     Stops when ||b - A64 x|| / ||b|| <= rtol (FP64 true residual).  The FP32
-    inner solve is left-preconditioned by Jacobi with ``A_diag``.
+    inner solve is left-preconditioned by Jacobi with ``A_diag``; its cycles
+    may end early on the inner estimate (checked every ``inner_early_exit``
+    steps; None runs full cycles).
     """
     dev = b.device
     b64 = b.to(torch.float64)
@@ -224,7 +247,8 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
             break
         r32 = r.to(torch.float32)
         d, info = gmres_restart(op32, r32, restart=inner_restart, tol=inner_tol, maxiter=inner_maxiter,
-                                precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph)
+                                precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph,
+                                early_exit=inner_early_exit)
         inner_total += info["iters"]
         x = x + d.to(torch.float64)
         r = b64 - op64(x)

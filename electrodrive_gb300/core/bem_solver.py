@@ -123,7 +123,15 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                   callback_context: Optional[Dict[str, Any]] = None,
                   precond: Optional[Union[str, Callable[[Tensor], Tensor]]] = None, areas: Optional[Tensor] = None,
                   A_diag: Optional[Tensor] = None, validate_operators: bool = False, use_graph: Union[bool, str] = "auto",
+                  early_exit: Optional[int] = None,
                   _retry_without_precond: bool = False) -> Tuple[Tensor, Dict[str, Any]]:
+    """Restarted GMRES with the reference's semantics (see the module docstring).
+
+    ``early_exit=c`` (not in the reference) lets a cycle end before ``restart``
+    steps: every ``c`` steps the device's inner residual estimate is read, and
+    the cycle ends once it is below ``tol`` times the first cycle's
+    preconditioned residual norm; the true-residual test then decides as usual.
+    """
     if restart <= 0:
         raise ValueError("restart must be positive")
     if maxiter <= 0:
@@ -181,14 +189,14 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
         return gmres_restart(A=A, b=b, M=None, restart=restart, tol=tol, maxiter=maxiter, logger=logger, x0=x0,
                              telemetry=telemetry, pass_index=pass_index, live_control_poll_fn=live_control_poll_fn,
                              log_every=log_every, callback=callback, callback_context=callback_context, precond=None,
-                             areas=None, validate_operators=False, use_graph=use_graph, _retry_without_precond=True)
+                             areas=None, validate_operators=False, use_graph=use_graph, early_exit=early_exit,
+                             _retry_without_precond=True)
 
     can_retry = used_pc and not _retry_without_precond and N <= 512
     K = _Krylov(N, restart, work_dtype, dev)
     x = torch.zeros(N, dtype=work_dtype, device=dev) if x0 is None else x0.to(dev, work_dtype).clone()
     b_work = b.to(dev, work_dtype).contiguous()
     av = torch.empty(N, dtype=work_dtype, device=dev)
-    graph = None
     want_graph = (use_graph is True) or (use_graph == "auto" and bool(getattr(A, "capturable", False))
                                           and M_python is None and work_dtype == orig_dtype
                                           and orig_device.type == "cuda")
@@ -202,15 +210,51 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
             K.start(M_python(rt).to(dev, work_dtype).contiguous(), torch.zeros_like(rt), None)
             K.scal[0] = torch.linalg.norm(rt.double())
 
-    def inner_steps(steps: int):
-        for j in range(steps):
+    def inner_steps(steps: int, j0: int = 0):
+        for j in range(j0, j0 + steps):
             y = A_apply(K.V[j])
             if M_python is not None:
                 y = M_python(y).to(dev, work_dtype)
             av.copy_(y)
             K.arnoldi(j, av, pinv if M_python is None else None)
 
+    graphs: Dict[Tuple[int, int], Any] = {}
+    warmed = [False]
+
+    def run_steps(j0: int, count: int):
+        """Arnoldi steps j0 .. j0+count-1, as a captured graph when allowed."""
+        if not want_graph:
+            inner_steps(count, j0)
+            return
+        key = (j0, count)
+        if key not in graphs:
+            if not warmed[0]:
+                # warm the operator's lazy state outside the capture
+                torch.cuda.synchronize(dev)
+                s = torch.cuda.Stream(device=dev)
+                s.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.stream(s):
+                    inner_steps(1, j0)
+                torch.cuda.current_stream(dev).wait_stream(s)
+                torch.cuda.synchronize(dev)
+                warmed[0] = True
+                if j0 == 0:
+                    start_cycle()  # the warm-up step overwrote w/H; recompute the start state
+                else:
+                    raise RuntimeError("graph warm-up must happen at the start of a cycle")
+            g = torch.cuda.CUDAGraph()
+            l0 = _lib.launch_count()
+            with torch.cuda.graph(g):
+                inner_steps(count, j0)
+            n_k = _lib.launch_count() - l0
+            _lib.note_graph_replay(-n_k)  # captured, not executed
+            graphs[key] = (g, n_k)
+        g, n_k = graphs[key]
+        g.replay()
+        _lib.note_graph_replay(n_k)
+
     total_iters = 0
+    beta_first = float("nan")
     tol_abs = float("nan")
     r_true_norm = float("nan")
     r_norm = float("nan")
@@ -230,6 +274,7 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                                                                used_pc)
             init_true = r_true_norm if r_true_norm > 1e-16 else 1.0
             tol_abs = max(tol * init_true, tol * 1e-12, 1e-12)
+            beta_first = beta
         else:
             if not math.isfinite(r_true_norm):
                 if can_retry:
@@ -251,21 +296,20 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                 return x.to(orig_dtype).to(orig_device), _info(total_iters, float("nan"), False, 2, r_true_norm,
                                                                tol_abs, used_pc)
         steps = min(restart, maxiter - total_iters)
-        if want_graph and steps == restart:
-            if graph is None:
-                # warm the operator's lazy state outside the capture
-                torch.cuda.synchronize(dev)
-                s = torch.cuda.Stream(device=dev)
-                s.wait_stream(torch.cuda.current_stream(dev))
-                with torch.cuda.stream(s):
-                    inner_steps(1)
-                torch.cuda.current_stream(dev).wait_stream(s)
-                torch.cuda.synchronize(dev)
-                start_cycle()  # the warm-up step overwrote w/H; recompute the start state
-                graph = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(graph):
-                    inner_steps(restart)
-            graph.replay()
+        if early_exit:
+            chunk = max(1, int(early_exit))
+            j0 = 0
+            while j0 < steps:
+                cnt = min(chunk, steps - j0)
+                run_steps(j0, cnt)
+                j0 += cnt
+                tail = K.scal[2:5 + restart].cpu()
+                est = float(tail[2 + j0 - 1])
+                if tail[0] >= 0 or tail[1] != 0 or not math.isfinite(est) or est <= tol * beta_first:
+                    break
+            steps = j0
+        elif want_graph and steps == restart:
+            run_steps(0, steps)
         else:
             inner_steps(steps)
         total_iters += steps

@@ -1,8 +1,9 @@
 // Far-field stages of the FMM: P2M, M2M, M2L, L2L.
 //
 // Coefficients are stored per node as (p+1)(p+2)/2 complex numbers (m >= 0),
-// scaled by the node's expansion radius a (the tight-box radius, floored at
-// 2^-40 of the root radius):  Mhat_n^m = M_n^m / a^n,  Lhat_n^m = L_n^m a^n.
+// scaled by the node's expansion radius a (the tight-box radius, but at least
+// 1/8 of the parent's a and 2^-40 of the root radius):
+//   Mhat_n^m = M_n^m / a^n,  Lhat_n^m = L_n^m a^n.
 // This keeps every coefficient O(1) in FP32 at any tree depth.
 //
 // M2L (the dominant stage) is organised so that one lane owns one
@@ -13,7 +14,7 @@
 // one target's row of the interaction list; the 32 partial sums are reduced
 // with shuffles, so the result is deterministic.  With this scaling
 //   Lhat_n^m = (-1)^(n+m) / a_L  sum_pairs sum_{k,l} Mhat_k^l (a_M/a_L)^k I_{n+k}^{l-m}(v),
-// which is exact algebra; pairs whose source radius exceeds 256x the target's
+// which is exact algebra; pairs whose source scale exceeds 256x the target's
 // (only in strongly adaptive trees) would overflow (a_M/a_L)^k in FP32 and are
 // instead translated by a shared-memory kernel using
 //   Lhat_n^m = (-1)^(n+m) / a_L  (a_L/a_M)^(n+1) sum_{k,l} Mhat_k^l I_{n+k}^{l-m}((c_L - c_M)/a_M).
@@ -187,78 +188,77 @@ template <int P> constexpr int m2l_passes() { return P >= 7 ? 2 : 1; }
 // so, with the source rotated, Mt_k^l = Mhat_k^l (a_M/a_L)^k e^{i l phi},
 //   S_n^m = sum_{k,l} Mt_k^l R_{n+k}^{l-m}   (real coefficients)
 //   A_n^m += e^{-i m phi} S_n^m,   Lhat_n^m = (-1)^(n+m) A_n^m / a_L.
-// Each term is a real x complex multiply-add (2 FMAs, against 4 for the
-// unfactored complex contraction), and the harmonics columns are real.
-// One column mu is generated at a time (template recursion: constant
-// register indices) and applied to every (l, m) block that uses it.
-template <int P, int SET, int MU>
-__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float s,
-                                           float z, float ir2, float &diag, float (&Sr)[ncoef(P)],
-                                           float (&Si)[ncoef(P)]) {
-    if constexpr (MU > 0) diag *= -(float)(2 * MU - 1) * s * ir2;  // R_mu^mu
-    float c[2 * P + 1];                                            // R_j^mu at [j], j >= mu
-#pragma unroll
-    for (int j = 0; j <= 2 * P; ++j) {
-        if (j == MU) {
-            c[j] = diag;
-        } else if (j == MU + 1) {
-            c[j] = ((float)(2 * j - 1) * z * ir2) * c[j - 1];
-        } else if (j > MU + 1) {
-            const float b = (float)((j - 1 + MU) * (j - 1 - MU));
-            c[j] = ((float)(2 * j - 1) * z * c[j - 1] - b * c[j - 2]) * ir2;
-        }
+// Each term is a real x complex multiply-add, issued as one packed FP32 pair
+// FMA (FFMA2: the re and im halves in one instruction), against 4 FMAs for
+// the unfactored complex contraction.  The harmonic R_j^mu is broadcast to
+// both halves; the sign patterns a term can carry ((-1)^mu, and the
+// conjugate of a negative-order source coefficient) become the pairs (c,c),
+// (-c,-c), (c,-c), (-c,c), formed once per degree.  Columns mu and degrees j
+// are visited by template recursion (constant register indices) and only
+// one degree's pairs are live at a time.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+// (sr, si) += (xr, xi) * c as one packed FMA on coefficients held in separate
+// re / im register arrays.
+__device__ __forceinline__ void fma2_into(float &sr, float &si, float xr, float xi, float2 c) {
+    const float2 r = __ffma2_rn(f2(xr, xi), c, f2(sr, si));
+    sr = r.x;
+    si = r.y;
+}
+
+// one degree j of column mu: R_j^mu by the recurrence, then every term with
+// n + k = j (template recursion over j keeps all register indices constant)
+template <int P, int SET, int MU, int J>
+__device__ __forceinline__ void m2l_degree(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float z,
+                                            float ir2, float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
+                                            float (&Si)[ncoef(P)]) {
+    float c;
+    if constexpr (J == MU) {
+        c = diag;
+    } else if constexpr (J == MU + 1) {
+        c = ((float)(2 * J - 1) * z * ir2) * cm1;
+    } else {
+        constexpr float b = (float)((J - 1 + MU) * (J - 1 - MU));
+        c = ((float)(2 * J - 1) * z * cm1 - b * cm2) * ir2;
     }
+    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
 #pragma unroll
-    for (int m = 0; m <= P; ++m) {
-        if (!m_in_set<P>(m, SET)) continue;
+    for (int n = 0; n <= P; ++n) {
+        const int k = J - n;
+        if (k < 0 || k > P) continue;
 #pragma unroll
-        for (int n = 0; n <= P; ++n) {
-#pragma unroll
-            for (int k = 0; k <= P; ++k) {
-                const int j = n + k;
-                // l - m = +mu, l >= 0:  Mt_k^l R^mu
-                {
-                    const int l = m + MU;
-                    if (l <= P && n >= m && k >= l) {
-                        Sr[tri(n, m)] += mr[tri(k, l)] * c[j];
-                        Si[tri(n, m)] += mi[tri(k, l)] * c[j];
-                    }
-                }
-                // l - m = -mu: R^{-mu} = (-1)^mu R^mu
-                if (MU > 0) {
-                    const int l = m - MU;
-                    const int al = l < 0 ? -l : l;
-                    if (al <= P && n >= m && k >= al) {
-                        if (l >= 0) {
-                            // (-1)^mu Mt_k^l R
-                            if (MU & 1) {
-                                Sr[tri(n, m)] -= mr[tri(k, al)] * c[j];
-                                Si[tri(n, m)] -= mi[tri(k, al)] * c[j];
-                            } else {
-                                Sr[tri(n, m)] += mr[tri(k, al)] * c[j];
-                                Si[tri(n, m)] += mi[tri(k, al)] * c[j];
-                            }
-                        } else {
-                            // Mt_k^l = (-1)^|l| conj(Mt_k^|l|): (-1)^m conj(Mt) R
-                            if (m & 1) {
-                                Sr[tri(n, m)] -= mr[tri(k, al)] * c[j];
-                                Si[tri(n, m)] += mi[tri(k, al)] * c[j];
-                            } else {
-                                Sr[tri(n, m)] += mr[tri(k, al)] * c[j];
-                                Si[tri(n, m)] -= mi[tri(k, al)] * c[j];
-                            }
-                        }
-                    }
+        for (int m = 0; m <= P; ++m) {
+            if (m > n || !m_in_set<P>(m, SET)) continue;
+            {  // l - m = +mu
+                const int l = m + MU;
+                if (l <= P && k >= l) fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, l)], mi[tri(k, l)], cpp);
+            }
+            if (MU > 0) {
+                const int l = m - MU;
+                if (l >= 0) {  // (-1)^mu Mt_k^l R
+                    if (k >= l)
+                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, l)], mi[tri(k, l)], (MU & 1) ? cnn : cpp);
+                } else {  // (-1)^m conj(Mt_k^|l|) R
+                    const int al = -l;
+                    if (al <= P && k >= al)
+                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, al)], mi[tri(k, al)], (m & 1) ? cnp : cpn);
                 }
             }
         }
     }
+    if constexpr (J < 2 * P) m2l_degree<P, SET, MU, J + 1>(mr, mi, z, ir2, diag, c, cm1, Sr, Si);
+}
+
+template <int P, int SET, int MU>
+__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float s, float z,
+                                            float ir2, float &diag, float (&Sr)[ncoef(P)], float (&Si)[ncoef(P)]) {
+    if constexpr (MU > 0) diag *= -(float)(2 * MU - 1) * s * ir2;  // R_mu^mu
+    m2l_degree<P, SET, MU, MU>(mr, mi, z, ir2, diag, 0.0f, 0.0f, Sr, Si);
     if constexpr (MU < 2 * P) m2l_column<P, SET, MU + 1>(mr, mi, s, z, ir2, diag, Sr, Si);
 }
 
 template <int P, int SET>
 __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, float c, float vx, float vy, float vz,
-                                               float (&Ar)[ncoef(P)], float (&Ai)[ncoef(P)]) {
+                                                float (&Ar)[ncoef(P)], float (&Ai)[ncoef(P)]) {
     constexpr int NC = ncoef(P);
     const float s2 = vx * vx + vy * vy;
     const float r2 = s2 + vz * vz;
@@ -270,7 +270,6 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
         ec = vx * is;
         es = vy * is;
     }
-    // rotated, rescaled source coefficients
     float mr[NC], mi[NC];
 #pragma unroll
     for (int q = 0; q < (NC + 1) / 2; ++q) {
@@ -296,9 +295,11 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
             for (int k = 0; k <= P; ++k) {
                 if (k >= l) {
                     const float fr = wr * ck, fi = wi * ck;
-                    const float xr = mr[tri(k, l)], xi = mi[tri(k, l)];
-                    mr[tri(k, l)] = xr * fr - xi * fi;
-                    mi[tri(k, l)] = xr * fi + xi * fr;
+                    const float2 x = f2(mr[tri(k, l)], mi[tri(k, l)]);
+                    // (xr fr - xi fi, xi fr + xr fi)
+                    const float2 y = __ffma2_rn(f2(x.y, x.x), f2(-fi, fi), __fmul2_rn(x, f2(fr, fr)));
+                    mr[tri(k, l)] = y.x;
+                    mi[tri(k, l)] = y.y;
                 }
                 ck *= c;
             }
@@ -309,7 +310,7 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
     for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
     float diag = sqrtf(ir2);  // R_0^0 = 1 / |v|
     m2l_column<P, SET, 0>(mr, mi, s, vz, ir2, diag, Sr, Si);
-    // rotate back: A_n^m += e^{-i m phi} S_n^m
+    // rotate back: A_n^m += e^{-i m phi} S_n^m = (xr wr + xi wi, xi wr - xr wi)
     float wr = 1.0f, wi = 0.0f;
 #pragma unroll
     for (int m = 0; m <= P; ++m) {
@@ -322,18 +323,19 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
 #pragma unroll
         for (int n = 0; n <= P; ++n) {
             if (n < m) continue;
-            const float xr = Sr[tri(n, m)], xi = Si[tri(n, m)];
-            Ar[tri(n, m)] += xr * wr + xi * wi;
-            Ai[tri(n, m)] += xi * wr - xr * wi;
+            const float2 x = f2(Sr[tri(n, m)], Si[tri(n, m)]);
+            const float2 a = __ffma2_rn(f2(x.y, x.x), f2(wi, -wi), __ffma2_rn(x, f2(wr, wr), f2(Ar[tri(n, m)], Ai[tri(n, m)])));
+            Ar[tri(n, m)] = a.x;
+            Ai[tri(n, m)] = a.y;
         }
     }
 }
 
 template <int P, int SET>
 __global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
-                                                  const int32_t *__restrict__ src, const float4 *__restrict__ center,
-                                                  const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
-                                                  float2 *__restrict__ Lexp, int nc_pad) {
+                                                   const int32_t *__restrict__ src, const float4 *__restrict__ center,
+                                                   const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
+                                                   float2 *__restrict__ Lexp, int nc_pad) {
     constexpr int NC = ncoef(P);
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t
         const float c = __ldg(&half[s].w) * iaL;
         if (c > kExtremeRatio) continue;  // translated by k_m2l_generic
         m2l_accumulate<P, SET>(reinterpret_cast<const float4 *>(Mexp + (int64_t)s * nc_pad), c, (ct.x - cs.x) * iaL,
-                               (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL, Ar, Ai);
+                                (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL, Ar, Ai);
     }
 #pragma unroll
     for (int n = 0; n <= P; ++n) {
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t
             const int k = tri(n, m);
             if ((k & 31) == lane) {
                 const float sg = ((n + m) & 1) ? -iaL : iaL;
-                out[k] = make_float2(sg * Ar[k], sg * Ai[k]);
+                out[k] = f2(sg * Ar[k], sg * Ai[k]);
             }
         }
     }

@@ -402,6 +402,23 @@ __global__ void k_permute_nodes(int64_t M, const int32_t *dfs, const int2 *rng, 
     level_nodes[b] = d;
 }
 
+// Expansion scale of one level's nodes: at least 1/8 of the parent's scale.
+// A node whose points coincide (radius 0, e.g. a single-point leaf) would
+// otherwise get the global floor, and every M2L pair into it would have a
+// source/target scale ratio far above the fast kernel's range.  Any positive
+// scale is exact algebra; this one keeps the ratios O(10).
+template <typename T>
+__global__ void k_scale_from_parent(const int32_t *__restrict__ nodes, int count, const int32_t *__restrict__ parent,
+                                    typename Vec4<T>::type *half) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int d = nodes[i];
+    const int p = parent[d];
+    if (p < 0) return;
+    const T lo = half[p].w * (T)0.125;
+    if (half[d].w < lo) half[d].w = lo;
+}
+
 __global__ void k_leaf_flags(const uint8_t *leaf, int64_t M, int32_t *flag) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < M) flag[i] = leaf[i];
@@ -584,6 +601,13 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
         dptr<int32_t>(tree.parent), dptr<int32_t>(tree.children), dptr<T4>(tree.center), dptr<T4>(tree.half),
         dptr<uint8_t>(tree.is_leaf), dptr<int32_t>(tree.level_nodes));
     EDFMM_LAUNCH_CHECK("k_permute_nodes");
+    for (size_t l = 1; l + 1 < tree.level_offsets.size(); ++l) {
+        const int a = tree.level_offsets[l], b = tree.level_offsets[l + 1];
+        if (b <= a) continue;
+        k_scale_from_parent<T><<<nblk(b - a, 256), 256, 0, s>>>(dptr<int32_t>(tree.level_nodes) + a, b - a,
+                                                                 dptr<int32_t>(tree.parent), dptr<T4>(tree.half));
+        EDFMM_LAUNCH_CHECK("k_scale_from_parent");
+    }
     // leaves
     DevBuf flag, loff;
     if ((rc = flag.reserve(sizeof(int32_t) * M)) || (rc = loff.reserve(sizeof(int32_t) * M))) return rc;

@@ -303,6 +303,12 @@ EDFMM_API int64_t edfmm_launch_count(void);
  */
 EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_out);
 
+/*
+ * Measured FP64 FMA throughput (TFLOP/s): the roofline denominator of the
+ * FP64 dense operator.  No counterpart in the reference.
+ */
+EDFMM_API int edfmm_measure_fp64_peak(int iters, void *stream, double *tflops_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -822,26 +822,99 @@ ORC_API void orc_self_integrals(const double *verts, const double *cent, int64_t
 }
 
 /* _build_near_pairs_for_panels: row-major (i ascending, j ascending) */
+static const double *g_sort_x;
+static int cmp_by_x(const void *a, const void *b) {
+    int64_t i = *(const int64_t *)a, j = *(const int64_t *)b;
+    double xi = g_sort_x[3 * i], xj = g_sort_x[3 * j];
+    if (xi < xj) return -1;
+    if (xi > xj) return 1;
+    return (i > j) - (i < j);
+}
+
+/* The pair test of _build_near_pairs_for_panels (0 < |C_i - C_j| <= f (R_i + R_j),
+ * R = sqrt(max(A, 0) / pi)), evaluated for every candidate inside an x-window
+ * of half-width 2 f (R_i + R_max) over the points sorted by x; points outside
+ * the window fail the test (|C_i - C_j| >= |dx|), so the set and its (i, j)
+ * order are those of the all-pairs loop. */
 ORC_API int64_t orc_near_pairs(const double *cent, const double *areas, int64_t n, double factor, int64_t *pairs,
                                int64_t cap) {
-    int64_t np = 0;
+    if (n <= 0) return 0;
+    double *r = (double *)malloc(sizeof(double) * n);
+    int64_t *ord = (int64_t *)malloc(sizeof(int64_t) * n);
+    int64_t *cnt = (int64_t *)calloc(n + 1, sizeof(int64_t));
+    int64_t m = 0;
+    double rmax = 0.0;
     for (int64_t i = 0; i < n; ++i) {
-        double ri = sqrt((areas[i] > 0 ? areas[i] : 0.0) / M_PI);
-        v3d ci = {cent[3 * i], cent[3 * i + 1], cent[3 * i + 2]};
-        for (int64_t j = 0; j < n; ++j) {
-            double rj = sqrt((areas[j] > 0 ? areas[j] : 0.0) / M_PI);
-            double d = v3_dist(ci, (v3d){cent[3 * j], cent[3 * j + 1], cent[3 * j + 2]});
-            double th = factor * (ri + rj);
-            if (isfinite(d) && isfinite(th) && d > 0.0 && d <= th) {
-                if (pairs && np < cap) {
-                    pairs[2 * np] = i;
-                    pairs[2 * np + 1] = j;
+        r[i] = sqrt((areas[i] > 0 ? areas[i] : 0.0) / M_PI);
+        if (isfinite(r[i]) && r[i] > rmax) rmax = r[i];
+        if (isfinite(cent[3 * i]) && isfinite(cent[3 * i + 1]) && isfinite(cent[3 * i + 2])) ord[m++] = i;
+    }
+    g_sort_x = cent;
+    qsort(ord, m, sizeof(int64_t), cmp_by_x);
+    double *xs = (double *)malloc(sizeof(double) * (m > 0 ? m : 1));
+    for (int64_t k = 0; k < m; ++k) xs[k] = cent[3 * ord[k]];
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            if (!pairs) break;
+            int64_t acc = 0;
+            for (int64_t i = 0; i < n; ++i) {
+                int64_t c = cnt[i];
+                cnt[i] = acc;
+                acc += c;
+            }
+            cnt[n] = acc;
+        }
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < n; ++i) {
+            v3d ci = {cent[3 * i], cent[3 * i + 1], cent[3 * i + 2]};
+            if (!(isfinite(ci.x) && isfinite(ci.y) && isfinite(ci.z))) continue;
+            double w = 2.0 * factor * (r[i] + rmax);
+            if (!isfinite(w)) w = INFINITY;
+            int64_t lo = 0, hi = m;
+            while (lo < hi) {
+                int64_t mid = lo + (hi - lo) / 2;
+                if (xs[mid] < ci.x - w) lo = mid + 1;
+                else hi = mid;
+            }
+            int64_t row = pass == 1 ? cnt[i] : 0, k0 = row, c = 0;
+            for (int64_t k = lo; k < m && xs[k] <= ci.x + w; ++k) {
+                int64_t j = ord[k];
+                double d = v3_dist(ci, (v3d){cent[3 * j], cent[3 * j + 1], cent[3 * j + 2]});
+                double th = factor * (r[i] + r[j]);
+                if (isfinite(d) && isfinite(th) && d > 0.0 && d <= th) {
+                    if (pass == 1 && row < cap) {
+                        pairs[2 * row] = i;
+                        pairs[2 * row + 1] = j;
+                    }
+                    row++;
+                    c++;
                 }
-                np++;
+            }
+            if (pass == 0) {
+                cnt[i] = c;
+            } else {
+                /* order the row by j (insertion sort: rows are short) */
+                int64_t e = row < cap ? row : cap;
+                for (int64_t a = k0 + 1; a < e; ++a) {
+                    int64_t v = pairs[2 * a + 1], b = a - 1;
+                    while (b >= k0 && pairs[2 * b + 1] > v) {
+                        pairs[2 * (b + 1) + 1] = pairs[2 * b + 1];
+                        --b;
+                    }
+                    pairs[2 * (b + 1) + 1] = v;
+                }
             }
         }
     }
-    return np;
+    int64_t total = 0;
+    if (pairs) total = cnt[n];
+    else
+        for (int64_t i = 0; i < n; ++i) total += cnt[i];
+    free(r);
+    free(ord);
+    free(cnt);
+    free(xs);
+    return total;
 }
 
 /* _precompute_near_correction_weights with uniform refinement `depth` */

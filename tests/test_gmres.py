@@ -92,3 +92,30 @@ def test_device_gmres_failure_codes(cuda_lib):
     assert info["code"] in (0, 2)
     with pytest.raises(ValueError):
         gmres_restart(lambda v: v, b, restart=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [False, True])
+def test_device_gmres_early_exit(cuda_lib, graph):
+    """early_exit (not in the reference): cycles end on the inner estimate, the
+    true residual still decides, and the answer is the converged one."""
+    from electrodrive_gb300.core.bem_solver import gmres_restart, setup_preconditioner
+
+    A, b, x_ref, restart, tol, maxiter, pc, iters, code = _case("bemlike300_jacobi")
+    At = torch.as_tensor(A, device="cuda")
+    out = torch.empty(A.shape[0], dtype=torch.float64, device="cuda")
+
+    class Op:
+        capturable = True
+
+        def __call__(self, v):
+            torch.mv(At, v, out=out)
+            return out
+
+    M = setup_preconditioner("jacobi", A_diag=torch.diag(At))
+    x, info = gmres_restart(Op(), torch.as_tensor(b, device="cuda"), M=M, restart=restart, tol=tol,
+                            maxiter=maxiter, use_graph=graph, early_exit=4)
+    assert info["code"] == 0 and info["iters"] < iters
+    x = x.cpu().numpy()
+    assert np.linalg.norm(A @ x - b) <= info["tol_abs"] * (1 + 1e-9)
+    assert np.linalg.norm(x - x_ref) <= 1e-6 * np.linalg.norm(x_ref)
