@@ -169,6 +169,7 @@ struct FmmBuffers {
     int nc_pad = 46;  // per-node stride in complex numbers (even: 16-byte rows for float)
     DevBuf multipoles;  // complex T, n_nodes x nc_pad
     DevBuf locals;      // complex T, n_nodes x nc_pad
+    DevBuf translated;  // complex T, n_nodes x nc_pad: each node's multipole moved to its parent's centre
     ExtremeRows extreme, extreme_swapped;
 };
 

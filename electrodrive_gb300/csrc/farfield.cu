@@ -18,7 +18,8 @@
 // (only in strongly adaptive trees) would overflow (a_M/a_L)^k in FP32 and are
 // instead translated by a shared-memory kernel using
 //   Lhat_n^m = (-1)^(n+m) / a_L  (a_L/a_M)^(n+1) sum_{k,l} Mhat_k^l I_{n+k}^{l-m}((c_L - c_M)/a_M).
-// FP64 plans use that kernel for every pair.
+// FP64 plans (p <= 8) translate every pair with an FP64 form of the fast
+// kernel; orders above 8 use the shared-memory kernel.
 #include <algorithm>
 
 #include "edfmm_internal.cuh"
@@ -384,6 +385,444 @@ __global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t
 }
 
 // ---------------------------------------------------------------------------
+// M2M / L2L fast paths (FP32, compile-time order): one thread per node of a
+// level, everything in registers, packed FMAs.  Both translations factor the
+// azimuth out like the M2L.  With d = (c_C - c_P) / a_P = (s cos phi,
+// s sin phi, z) and the real regular harmonics rho_k^l := R_k^l(s, 0, z)
+// (R_k^l(d) = e^{i l phi} rho_k^l, rho_k^{-l} = (-1)^l rho_k^l):
+//   M2M  Mhat_P,n^m = sum_C e^{-i m phi} sum_{k,l} rho_k^l Mt_{n-k}^{m-l},
+//        Mt_j^u = e^{i u phi} (a_C/a_P)^j Mhat_C,j^u
+//   L2L  Lhat_C,j^u += (a_C/a_P)^j e^{-i u phi} sum_{k,l} rho_k^l Lt_{j+k}^{u+l},
+//        Lt_n^m = e^{i m phi} Lhat_P,n^m
+// with negative orders through X^{-m} = (-1)^m conj(X^m).  The M2M runs from
+// the deepest level up: a node first sums its children's translated
+// multipoles (fixed order: deterministic), stores its own multipole, then
+// writes its translation to the parent's centre for the next level up.
+// ---------------------------------------------------------------------------
+template <int P, int MU, int K>
+__device__ __forceinline__ void m2m_degree(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float z, float r2,
+                                           float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
+                                           float (&Si)[ncoef(P)]) {
+    float c;
+    if constexpr (K == MU) {
+        c = diag;
+    } else if constexpr (K == MU + 1) {
+        c = ((float)(2 * K - 1) / (float)((K + MU) * (K - MU))) * z * cm1;
+    } else {
+        c = ((float)(2 * K - 1) * z * cm1 - r2 * cm2) * (1.0f / (float)((K + MU) * (K - MU)));
+    }
+    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+        if (n < K) continue;
+        const int j = n - K;
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > n) continue;
+            {  // l = +mu, u = m - mu
+                const int u = m - MU, au = u < 0 ? -u : u;
+                if (au <= j) {
+                    if (u >= 0)
+                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(j, u)], mi[tri(j, u)], cpp);
+                    else  // (-1)^|u| conj(Mt_j^|u|)
+                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(j, au)], mi[tri(j, au)], (au & 1) ? cnp : cpn);
+                }
+            }
+            if (MU > 0) {  // l = -mu: (-1)^mu rho, u = m + mu
+                const int u = m + MU;
+                if (u <= j) fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(j, u)], mi[tri(j, u)], (MU & 1) ? cnn : cpp);
+            }
+        }
+    }
+    if constexpr (K < P) m2m_degree<P, MU, K + 1>(mr, mi, z, r2, diag, c, cm1, Sr, Si);
+}
+
+template <int P, int MU, int K>
+__device__ __forceinline__ void l2l_degree(const float (&lr)[ncoef(P)], const float (&li)[ncoef(P)], float z, float r2,
+                                           float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
+                                           float (&Si)[ncoef(P)]) {
+    float c;
+    if constexpr (K == MU) {
+        c = diag;
+    } else if constexpr (K == MU + 1) {
+        c = ((float)(2 * K - 1) / (float)((K + MU) * (K - MU))) * z * cm1;
+    } else {
+        c = ((float)(2 * K - 1) * z * cm1 - r2 * cm2) * (1.0f / (float)((K + MU) * (K - MU)));
+    }
+    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
+#pragma unroll
+    for (int j = 0; j <= P; ++j) {
+        if (j + K > P) continue;
+        const int n = j + K;
+#pragma unroll
+        for (int u = 0; u <= P; ++u) {
+            if (u > j) continue;
+            {  // l = +mu, m' = u + mu
+                const int mp = u + MU;
+                if (mp <= n) fma2_into(Sr[tri(j, u)], Si[tri(j, u)], lr[tri(n, mp)], li[tri(n, mp)], cpp);
+            }
+            if (MU > 0) {  // l = -mu: (-1)^mu rho, m' = u - mu
+                const int mp = u - MU;
+                if (mp >= 0) {
+                    fma2_into(Sr[tri(j, u)], Si[tri(j, u)], lr[tri(n, mp)], li[tri(n, mp)], (MU & 1) ? cnn : cpp);
+                } else {  // (-1)^(mu + |m'|) conj(Lt_n^|m'|)
+                    const int am = -mp;
+                    if (am <= n)
+                        fma2_into(Sr[tri(j, u)], Si[tri(j, u)], lr[tri(n, am)], li[tri(n, am)],
+                                  ((MU + am) & 1) ? cnp : cpn);
+                }
+            }
+        }
+    }
+    if constexpr (K < P) l2l_degree<P, MU, K + 1>(lr, li, z, r2, diag, c, cm1, Sr, Si);
+}
+
+// columns mu = 0..P of rho; diag carries rho_mu^mu = -s / (2 mu) rho_{mu-1}^{mu-1}
+template <int P, bool L2L, int MU>
+__device__ __forceinline__ void shift_column(const float (&xr)[ncoef(P)], const float (&xi)[ncoef(P)], float s, float z,
+                                             float r2, float &diag, float (&Sr)[ncoef(P)], float (&Si)[ncoef(P)]) {
+    if constexpr (MU > 0) diag *= -s * (1.0f / (float)(2 * MU));
+    if constexpr (L2L)
+        l2l_degree<P, MU, MU>(xr, xi, z, r2, diag, 0.0f, 0.0f, Sr, Si);
+    else
+        m2m_degree<P, MU, MU>(xr, xi, z, r2, diag, 0.0f, 0.0f, Sr, Si);
+    if constexpr (MU < P) shift_column<P, L2L, MU + 1>(xr, xi, s, z, r2, diag, Sr, Si);
+}
+
+// Load a coefficient row (16-byte aligned float2 x nc_pad) into re / im arrays.
+template <int P>
+__device__ __forceinline__ void load_row(const float2 *row, float (&xr)[ncoef(P)], float (&xi)[ncoef(P)]) {
+    constexpr int NC = ncoef(P);
+    const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+    for (int q = 0; q < (NC + 1) / 2; ++q) {
+        const float4 v = r4[q];
+        xr[2 * q] = v.x;
+        xi[2 * q] = v.y;
+        if (2 * q + 1 < NC) {
+            xr[2 * q + 1] = v.z;
+            xi[2 * q + 1] = v.w;
+        }
+    }
+}
+
+// x_n^m <- e^{i m phi} f^n x_n^m  (f = 1 for the L2L)
+template <int P>
+__device__ __forceinline__ void rotate_scale(float (&xr)[ncoef(P)], float (&xi)[ncoef(P)], float ec, float es, float f) {
+    float wr = 1.0f, wi = 0.0f;
+#pragma unroll
+    for (int m = 0; m <= P; ++m) {
+        if (m > 0) {
+            const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+            wr = nr;
+            wi = ni;
+        }
+        float fk = 1.0f;
+#pragma unroll
+        for (int n = 0; n <= P; ++n) {
+            if (n >= m) {
+                const float fr = wr * fk, fi = wi * fk;
+                const float2 x = f2(xr[tri(n, m)], xi[tri(n, m)]);
+                const float2 y = __ffma2_rn(f2(x.y, x.x), f2(-fi, fi), __fmul2_rn(x, f2(fr, fr)));
+                xr[tri(n, m)] = y.x;
+                xi[tri(n, m)] = y.y;
+            }
+            fk *= f;
+        }
+    }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m_fast(const int32_t *__restrict__ nodes, int count,
+                                                  const uint8_t *__restrict__ is_leaf,
+                                                  const int32_t *__restrict__ children, const int32_t *__restrict__ parent,
+                                                  const float4 *__restrict__ center, const float4 *__restrict__ half,
+                                                  float2 *__restrict__ Mexp, float2 *__restrict__ moved, int nc_pad) {
+    constexpr int NC = ncoef(P);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int node = nodes[i];
+    float xr[NC], xi[NC];
+    if (is_leaf[node]) {
+        load_row<P>(Mexp + (int64_t)node * nc_pad, xr, xi);
+    } else {
+#pragma unroll
+        for (int q = 0; q < NC; ++q) xr[q] = xi[q] = 0.0f;
+        for (int o = 0; o < 8; ++o) {
+            const int ch = children[8 * node + o];
+            if (ch < 0) continue;
+            float yr[NC], yi[NC];
+            load_row<P>(moved + (int64_t)ch * nc_pad, yr, yi);
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                xr[q] += yr[q];
+                xi[q] += yi[q];
+            }
+        }
+        float4 *o4 = reinterpret_cast<float4 *>(Mexp + (int64_t)node * nc_pad);
+#pragma unroll
+        for (int q = 0; q < (NC + 1) / 2; ++q)
+            o4[q] = make_float4(xr[2 * q], xi[2 * q], 2 * q + 1 < NC ? xr[2 * q + 1] : 0.0f,
+                                2 * q + 1 < NC ? xi[2 * q + 1] : 0.0f);
+    }
+    const int par = parent[node];
+    if (par < 0) return;
+    const float4 cc = center[node], cp = center[par];
+    const float iaP = 1.0f / half[par].w;
+    const float ratio = half[node].w * iaP;
+    const float dx = (cc.x - cp.x) * iaP, dy = (cc.y - cp.y) * iaP, z = (cc.z - cp.z) * iaP;
+    const float s2 = dx * dx + dy * dy;
+    const float s = sqrtf(s2);
+    float ec = 1.0f, es = 0.0f;
+    if (s2 > 0.0f) {
+        const float is = 1.0f / s;
+        ec = dx * is;
+        es = dy * is;
+    }
+    rotate_scale<P>(xr, xi, ec, es, ratio);
+    float Sr[NC], Si[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
+    float diag = 1.0f;
+    shift_column<P, false, 0>(xr, xi, s, z, s2 + z * z, diag, Sr, Si);
+    rotate_scale<P>(Sr, Si, ec, -es, 1.0f);  // e^{-i m phi}
+    float4 *o4 = reinterpret_cast<float4 *>(moved + (int64_t)node * nc_pad);
+#pragma unroll
+    for (int q = 0; q < (NC + 1) / 2; ++q)
+        o4[q] = make_float4(Sr[2 * q], Si[2 * q], 2 * q + 1 < NC ? Sr[2 * q + 1] : 0.0f,
+                            2 * q + 1 < NC ? Si[2 * q + 1] : 0.0f);
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2l_fast(const int32_t *__restrict__ nodes, int count,
+                                                  const int32_t *__restrict__ parent, const float4 *__restrict__ center,
+                                                  const float4 *__restrict__ half, float2 *__restrict__ Lexp,
+                                                  int nc_pad) {
+    constexpr int NC = ncoef(P);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int node = nodes[i];
+    const int par = parent[node];
+    if (par < 0) return;
+    const float4 cc = center[node], cp = center[par];
+    const float iaP = 1.0f / half[par].w;
+    const float ratio = half[node].w * iaP;
+    const float dx = (cc.x - cp.x) * iaP, dy = (cc.y - cp.y) * iaP, z = (cc.z - cp.z) * iaP;
+    const float s2 = dx * dx + dy * dy;
+    const float s = sqrtf(s2);
+    float ec = 1.0f, es = 0.0f;
+    if (s2 > 0.0f) {
+        const float is = 1.0f / s;
+        ec = dx * is;
+        es = dy * is;
+    }
+    float xr[NC], xi[NC];
+    load_row<P>(Lexp + (int64_t)par * nc_pad, xr, xi);
+    rotate_scale<P>(xr, xi, ec, es, 1.0f);
+    float Sr[NC], Si[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
+    float diag = 1.0f;
+    shift_column<P, true, 0>(xr, xi, s, z, s2 + z * z, diag, Sr, Si);
+    rotate_scale<P>(Sr, Si, ec, -es, ratio);  // (a_C/a_P)^j e^{-i u phi}
+    float cr[NC], ci[NC];
+    load_row<P>(Lexp + (int64_t)node * nc_pad, cr, ci);
+    float4 *o4 = reinterpret_cast<float4 *>(Lexp + (int64_t)node * nc_pad);
+#pragma unroll
+    for (int q = 0; q < (NC + 1) / 2; ++q)
+        o4[q] = make_float4(cr[2 * q] + Sr[2 * q], ci[2 * q] + Si[2 * q],
+                            2 * q + 1 < NC ? cr[2 * q + 1] + Sr[2 * q + 1] : 0.0f,
+                            2 * q + 1 < NC ? ci[2 * q + 1] + Si[2 * q + 1] : 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// M2L fast path, FP64.  The same azimuth-factored algebra as the FP32 kernel.
+// On this part the FP64 FMA pipe is ~70x slower than the FP32 one, so FP64
+// FMAs are the whole cost and shared-memory traffic is free by comparison:
+// each lane keeps its pair's rotated source coefficients and its target
+// accumulators in its own shared-memory slots ([coef][lane], conflict-free),
+// and only the per-pair accumulators of the pass's output set in registers.
+// ---------------------------------------------------------------------------
+// A shared-memory load the compiler may not hoist or merge: the contraction
+// re-reads each rotated coefficient where it is used instead of keeping all
+// 45 of them live in registers.
+__device__ __forceinline__ double2 lds_f64x2(const double2 *p) {
+    double2 v;
+    asm volatile("ld.volatile.shared.v2.f64 {%0, %1}, [%2];"
+                 : "=d"(v.x), "=d"(v.y)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+template <int P, int SET, int MU, int J>
+__device__ __forceinline__ void m2l64_degree(const double2 *__restrict__ sM, double z, double ir2, double diag,
+                                             double cm1, double cm2, double (&Sr)[ncoef(P)], double (&Si)[ncoef(P)]) {
+    double c;
+    if constexpr (J == MU) {
+        c = diag;
+    } else if constexpr (J == MU + 1) {
+        c = ((double)(2 * J - 1) * z * ir2) * cm1;
+    } else {
+        constexpr double b = (double)((J - 1 + MU) * (J - 1 - MU));
+        c = ((double)(2 * J - 1) * z * cm1 - b * cm2) * ir2;
+    }
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+        const int k = J - n;
+        if (k < 0 || k > P) continue;
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > n || !m_in_set<P>(m, SET)) continue;
+            {  // l - m = +mu
+                const int l = m + MU;
+                if (l <= P && k >= l) {
+                    const double2 x = lds_f64x2(sM + tri(k, l) * 128);
+                    Sr[tri(n, m)] = fma(x.x, c, Sr[tri(n, m)]);
+                    Si[tri(n, m)] = fma(x.y, c, Si[tri(n, m)]);
+                }
+            }
+            if (MU > 0) {
+                const int l = m - MU;
+                if (l >= 0) {  // (-1)^mu Mt_k^l R
+                    if (k >= l) {
+                        const double2 x = lds_f64x2(sM + tri(k, l) * 128);
+                        const double cs = (MU & 1) ? -c : c;
+                        Sr[tri(n, m)] = fma(x.x, cs, Sr[tri(n, m)]);
+                        Si[tri(n, m)] = fma(x.y, cs, Si[tri(n, m)]);
+                    }
+                } else {  // (-1)^m conj(Mt_k^|l|) R
+                    const int al = -l;
+                    if (al <= P && k >= al) {
+                        const double2 x = lds_f64x2(sM + tri(k, al) * 128);
+                        const double cs = (m & 1) ? -c : c;
+                        Sr[tri(n, m)] = fma(x.x, cs, Sr[tri(n, m)]);
+                        Si[tri(n, m)] = fma(-x.y, cs, Si[tri(n, m)]);
+                    }
+                }
+            }
+        }
+    }
+    if constexpr (J < 2 * P) m2l64_degree<P, SET, MU, J + 1>(sM, z, ir2, diag, c, cm1, Sr, Si);
+}
+
+template <int P, int SET, int MU>
+__device__ __forceinline__ void m2l64_column(const double2 *__restrict__ sM, double s, double z, double ir2,
+                                             double &diag, double (&Sr)[ncoef(P)], double (&Si)[ncoef(P)]) {
+    if constexpr (MU > 0) diag *= -(double)(2 * MU - 1) * s * ir2;  // R_mu^mu
+    m2l64_degree<P, SET, MU, MU>(sM, z, ir2, diag, 0.0, 0.0, Sr, Si);
+    if constexpr (MU < 2 * P) m2l64_column<P, SET, MU + 1>(sM, s, z, ir2, diag, Sr, Si);
+}
+
+template <int P>
+constexpr size_t m2l64_smem_bytes() {
+    return (size_t)2 * ncoef(P) * 128 * sizeof(double2);
+}
+
+template <int P, int SET>
+__global__ void __launch_bounds__(128) k_m2l_fast64(int64_t n_nodes, const int32_t *__restrict__ off,
+                                                    const int32_t *__restrict__ src,
+                                                    const double4 *__restrict__ center,
+                                                    const double4 *__restrict__ half,
+                                                    const double2 *__restrict__ Mexp, double2 *__restrict__ Lexp,
+                                                    int nc_pad) {
+    constexpr int NC = ncoef(P);
+    extern __shared__ double2 smem64[];
+    double2 *sM = smem64 + threadIdx.x;            // rotated source coefficients, slot stride 128
+    double2 *sA = smem64 + NC * 128 + threadIdx.x;  // target accumulators
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= n_nodes) return;
+    const double4 ct = center[t];
+    const double aL = half[t].w;
+    const double iaL = 1.0 / aL;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) sA[q * 128] = make_double2(0.0, 0.0);
+    const int e = off[t + 1];
+    for (int k = off[t] + lane; k < e; k += 32) {
+        const int s = __ldg(src + k);
+        const double4 cs = center[s];
+        const double c = half[s].w * iaL;
+        const double vx = (ct.x - cs.x) * iaL, vy = (ct.y - cs.y) * iaL, vz = (ct.z - cs.z) * iaL;
+        const double s2 = vx * vx + vy * vy;
+        const double r2 = s2 + vz * vz;
+        const double ir2 = 1.0 / r2;
+        const double sr = sqrt(s2);
+        double ec = 1.0, es = 0.0;  // e^{i phi}
+        if (s2 > 0.0) {
+            const double is = 1.0 / sr;
+            ec = vx * is;
+            es = vy * is;
+        }
+        const double2 *Mrow = Mexp + (int64_t)s * nc_pad;
+        {
+            double wr = 1.0, wi = 0.0;  // e^{i l phi}
+#pragma unroll
+            for (int l = 0; l <= P; ++l) {
+                if (l > 0) {
+                    const double nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+                    wr = nr;
+                    wi = ni;
+                }
+                double ck = 1.0;
+#pragma unroll
+                for (int kk = 0; kk <= P; ++kk) {
+                    if (kk >= l) {
+                        const double fr = wr * ck, fi = wi * ck;
+                        const double2 x = Mrow[tri(kk, l)];
+                        sM[tri(kk, l) * 128] = make_double2(x.x * fr - x.y * fi, x.x * fi + x.y * fr);
+                    }
+                    ck *= c;
+                }
+            }
+        }
+        double Sr[NC], Si[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0;
+        double diag = sqrt(ir2);  // R_0^0 = 1 / |v|
+        m2l64_column<P, SET, 0>(sM, sr, vz, ir2, diag, Sr, Si);
+        // rotate back: A_n^m += e^{-i m phi} S_n^m
+        double wr = 1.0, wi = 0.0;
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > 0) {
+                const double nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+                wr = nr;
+                wi = ni;
+            }
+            if (!m_in_set<P>(m, SET)) continue;
+#pragma unroll
+            for (int n = 0; n <= P; ++n) {
+                if (n < m) continue;
+                const double xr = Sr[tri(n, m)], xi = Si[tri(n, m)];
+                double2 a = sA[tri(n, m) * 128];
+                a.x += xr * wr + xi * wi;
+                a.y += xi * wr - xr * wi;
+                sA[tri(n, m) * 128] = a;
+            }
+        }
+    }
+    double2 *out = Lexp + t * nc_pad;
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+            if (m > n || !m_in_set<P>(m, SET)) continue;
+            const int q = tri(n, m);
+            double2 a = sA[q * 128];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+                a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+            }
+            if ((q & 31) == lane) {
+                const double sg = ((n + m) & 1) ? -iaL : iaL;
+                out[q] = make_double2(sg * a.x, sg * a.y);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // M2L generic path: any precision / order; warp per target row, lanes over
 // harmonics columns and output coefficients, operands in shared memory.
 // ---------------------------------------------------------------------------
@@ -593,8 +1032,45 @@ template <typename T> int p2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
     return EDFMM_OK;
 }
 
+template <int P> void launch_m2m_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    for (int lev = tree.max_level; lev >= 0; --lev) {
+        const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
+        if (hi <= lo) continue;
+        k_m2m_fast<P><<<nblk(hi - lo, 128), 128, 0, s>>>(
+            dptr<int32_t>(tree.level_nodes) + lo, hi - lo, dptr<uint8_t>(tree.is_leaf), dptr<int32_t>(tree.children),
+            dptr<int32_t>(tree.parent), dptr<float4>(tree.center), dptr<float4>(tree.half), dptr<float2>(buf.multipoles),
+            dptr<float2>(buf.translated), buf.nc_pad);
+        if (lev > 0) count_launch();
+    }
+}
+
+template <int P> void launch_l2l_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    for (int lev = 1; lev <= tree.max_level; ++lev) {
+        const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
+        if (hi <= lo) continue;
+        k_l2l_fast<P><<<nblk(hi - lo, 128), 128, 0, s>>>(dptr<int32_t>(tree.level_nodes) + lo, hi - lo,
+                                                          dptr<int32_t>(tree.parent), dptr<float4>(tree.center),
+                                                          dptr<float4>(tree.half), dptr<float2>(buf.locals), buf.nc_pad);
+        if (lev < tree.max_level) count_launch();
+    }
+}
+
 template <typename T> int m2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
+    if (sizeof(T) == 4 && buf.p <= 8 && tree.n_nodes > 0) {
+        switch (buf.p) {
+            case 1: launch_m2m_fast<1>(tree, buf, s); break;
+            case 2: launch_m2m_fast<2>(tree, buf, s); break;
+            case 3: launch_m2m_fast<3>(tree, buf, s); break;
+            case 4: launch_m2m_fast<4>(tree, buf, s); break;
+            case 5: launch_m2m_fast<5>(tree, buf, s); break;
+            case 6: launch_m2m_fast<6>(tree, buf, s); break;
+            case 7: launch_m2m_fast<7>(tree, buf, s); break;
+            default: launch_m2m_fast<8>(tree, buf, s); break;
+        }
+        EDFMM_LAUNCH_CHECK("k_m2m_fast");
+        return EDFMM_OK;
+    }
     for (int lev = tree.max_level - 1; lev >= 0; --lev) {
         const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
         if (hi <= lo) continue;
@@ -608,6 +1084,21 @@ template <typename T> int m2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
 
 template <typename T> int l2l_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
+    if (sizeof(T) == 4 && buf.p <= 8) {
+        if (tree.max_level < 1) return EDFMM_OK;
+        switch (buf.p) {
+            case 1: launch_l2l_fast<1>(tree, buf, s); break;
+            case 2: launch_l2l_fast<2>(tree, buf, s); break;
+            case 3: launch_l2l_fast<3>(tree, buf, s); break;
+            case 4: launch_l2l_fast<4>(tree, buf, s); break;
+            case 5: launch_l2l_fast<5>(tree, buf, s); break;
+            case 6: launch_l2l_fast<6>(tree, buf, s); break;
+            case 7: launch_l2l_fast<7>(tree, buf, s); break;
+            default: launch_l2l_fast<8>(tree, buf, s); break;
+        }
+        EDFMM_LAUNCH_CHECK("k_l2l_fast");
+        return EDFMM_OK;
+    }
     for (int lev = 1; lev <= tree.max_level; ++lev) {
         const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
         if (hi <= lo) continue;
@@ -669,6 +1160,34 @@ void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t
     }
 }
 
+template <int P>
+int launch_m2l_fast64(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const double4 *cen,
+                      const double4 *hal, const double2 *Mx, double2 *Lx, int nc_pad, cudaStream_t s) {
+    constexpr size_t smem = m2l64_smem_bytes<P>();
+    static const cudaError_t attr = [] {
+        cudaError_t e = cudaSuccess;
+        if constexpr (m2l_passes<P>() == 1) {
+            e = cudaFuncSetAttribute(k_m2l_fast64<P, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        } else {
+            e = cudaFuncSetAttribute(k_m2l_fast64<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_m2l_fast64<P, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        return e;
+    }();
+    if (attr != cudaSuccess)
+        return fail(EDFMM_ERR_CUDA, std::string("k_m2l_fast64 shared memory attribute: ") + cudaGetErrorString(attr));
+    if constexpr (m2l_passes<P>() == 1) {
+        k_m2l_fast64<P, 0><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+    } else {
+        k_m2l_fast64<P, 1><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        count_launch();
+        k_m2l_fast64<P, 2><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+    }
+    EDFMM_LAUNCH_CHECK("k_m2l_fast64");
+    return EDFMM_OK;
+}
+
 template <typename T>
 int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
@@ -676,6 +1195,23 @@ int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool s
     if (M == 0) return EDFMM_OK;
     const int32_t *off = swapped ? dptr<int32_t>(lists.m2l_swapped_off) : dptr<int32_t>(lists.m2l_off);
     const int32_t *src = swapped ? dptr<int32_t>(lists.m2l_swapped_src) : dptr<int32_t>(lists.m2l_src);
+    if (sizeof(T) == 8 && buf.p <= 8) {
+        // every pair: FP64 has the range for any scale ratio the tree produces
+        const unsigned grid = nblk(M * 32, 128);
+        const double4 *cen = dptr<double4>(tree.center), *hal = dptr<double4>(tree.half);
+        const double2 *Mx = dptr<double2>(buf.multipoles);
+        double2 *Lx = dptr<double2>(buf.locals);
+        switch (buf.p) {
+            case 1: return launch_m2l_fast64<1>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 2: return launch_m2l_fast64<2>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 3: return launch_m2l_fast64<3>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 4: return launch_m2l_fast64<4>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 5: return launch_m2l_fast64<5>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 6: return launch_m2l_fast64<6>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 7: return launch_m2l_fast64<7>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            default: return launch_m2l_fast64<8>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+        }
+    }
     if (sizeof(T) == 8) {
         k_m2l_generic<T><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, dptr<T4>(tree.center), dptr<T4>(tree.half),
                                                     dptr<Cplx<T>>(buf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p,

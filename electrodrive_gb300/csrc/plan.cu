@@ -121,6 +121,7 @@ int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_siz
         size_t esz = (dtype == EDFMM_F64 ? 16 : 8) * (size_t)p->fmm.nc_pad * (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
         rc = p->fmm.multipoles.reserve(esz);
         if (!rc) rc = p->fmm.locals.reserve(esz);
+        if (!rc) rc = p->fmm.translated.reserve(esz);
         if (!rc) {
             cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
             if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
@@ -166,8 +167,10 @@ int edfmm_plan_set_order(edfmm_plan *p, int expansion_order, void *stream) {
                  (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
     p->fmm.multipoles.release();
     p->fmm.locals.release();
+    p->fmm.translated.release();
     int rc = p->fmm.multipoles.reserve(esz);
     if (!rc) rc = p->fmm.locals.reserve(esz);
+    if (!rc) rc = p->fmm.translated.reserve(esz);
     if (rc) return rc;
     EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s));
     EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.locals.p, 0, esz, s));

@@ -63,20 +63,48 @@ def test_matvec_matches_oracle_fmm_fp32(cuda_lib, oracle, n, p):
         assert rel(v, d) < 1e-5
 
 
-def test_matvec_fp64_plan_matches_oracle(cuda_lib, oracle):
-    rng = np.random.default_rng(11)
-    n = 6000
-    pts = rng.random((n, 3))
+def _torus_points(n_u, n_v):
+    u = np.linspace(0, 2 * np.pi, n_u, endpoint=False)[:, None]
+    v = np.linspace(0, 2 * np.pi, n_v, endpoint=False)[None, :]
+    x = (1.0 + 0.35 * np.cos(v)) * np.cos(u)
+    y = (1.0 + 0.35 * np.cos(v)) * np.sin(u)
+    z = 0.35 * np.sin(v) + 0 * u
+    return np.stack([x, y, z], -1).reshape(-1, 3)
+
+
+@pytest.mark.parametrize("p", [3, 6, 8])
+@pytest.mark.parametrize("kind", ["cube", "torus"])
+def test_matvec_fp64_plan_matches_oracle(cuda_lib, oracle, p, kind):
+    rng = np.random.default_rng(11 + p)
+    pts = rng.random((6000, 3)) if kind == "cube" else _torus_points(120, 50)
+    n = pts.shape[0]
     sigma = rng.uniform(-1, 1, n)
     areas = rng.uniform(0.5, 1.5, n) / n
     si = rng.uniform(0, 1e3, n)
-    plan = _plan(pts, 48, 0.5, 8)
+    plan = _plan(pts, 48, 0.5, p)
     v = plan.matvec(torch.as_tensor(sigma).cuda(), torch.as_tensor(areas).cuda(), torch.as_tensor(si).cuda(),
                     k_e=K_E).cpu().numpy()
     t = oracle.build_tree(pts, 48, 32)
     lists = oracle.build_lists(t, 0.5)
-    ref = oracle.fmm_matvec(t, lists, pts, sigma, areas, si, p=8)
+    ref = oracle.fmm_matvec(t, lists, pts, sigma, areas, si, p=p)
     assert rel(v, ref) < 1e-10
+
+
+def test_matvec_fp32_surface_matches_oracle(cuda_lib, oracle):
+    """A torus surface grid: its tree has single-point nodes (radius 0),
+    which exercise the parent-relative expansion scale."""
+    rng = np.random.default_rng(5)
+    pts = _torus_points(200, 80).astype(np.float32)
+    n = pts.shape[0]
+    sigma = rng.uniform(-1, 1, n).astype(np.float32)
+    areas = np.full(n, 1.0 / n, np.float32)
+    plan = _plan(pts, 64, 0.5, 8)
+    v = plan.matvec(torch.as_tensor(sigma).cuda(), torch.as_tensor(areas).cuda(), None, k_e=1.0).cpu().numpy()
+    t = oracle.build_tree(pts, 64, 32)
+    lists = oracle.build_lists(t, 0.5)
+    ref = oracle.fmm_matvec(t, lists, pts, sigma, areas, None, p=8, ke=1.0)
+    assert rel(v, ref) < 2e-6
+    assert rel(v, oracle.direct(pts, sigma.astype(np.float64) * areas)) < 1e-5
 
 
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "fmm_*.npz"))),
