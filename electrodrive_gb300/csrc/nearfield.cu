@@ -88,39 +88,44 @@ template <typename T> struct NearParams {
     T *out;
 };
 
-template <typename T, int TPL, bool SELF>
-__device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *sp, int cnt, int sbase,
+template <typename T, int TPL, int G, bool SELF>
+__device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *sp, int cnt, int sbase, int part,
                                                  const typename Vec4<T>::type (&x)[2], const int (&ti)[2], T eps2,
                                                  T (&acc)[2]) {
     // per-chunk partial sums, then one add: two-level summation
-    T part[2] = {(T)0, (T)0};
+    T psum[2] = {(T)0, (T)0};
 #pragma unroll 8
-    for (int j = 0; j < cnt; ++j) {
+    for (int j = part; j < cnt; j += G) {
         const typename Vec4<T>::type q = sp[j];
 #pragma unroll
         for (int u = 0; u < TPL; ++u) {
             const T dx = x[u].x - q.x, dy = x[u].y - q.y, dz = x[u].z - q.z;
             T inv = inv_dist(dx * dx + dy * dy + dz * dz, eps2);
             if (SELF && sbase + j == ti[u]) inv = (T)0;
-            part[u] += q.w * inv;
+            psum[u] += q.w * inv;
         }
     }
 #pragma unroll
-    for (int u = 0; u < TPL; ++u) acc[u] += part[u];
+    for (int u = 0; u < TPL; ++u) acc[u] += psum[u];
 }
 
-template <typename T, int TPL>
+// One block of up to 32 * TPL / G targets of leaf t.  With G > 1 (small
+// leaves) G lanes share a target, each taking every G-th source of a chunk,
+// and their sums are combined with a fixed shuffle tree.
+template <typename T, int TPL, int G>
 __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb, int te, typename Vec4<T>::type *sp,
                                            const Cplx<T> *sL) {
+    static_assert(G == 1 || TPL == 1, "lane groups are used for single-target lanes only");
     using T4 = typename Vec4<T>::type;
     const int lane = threadIdx.x & 31;
+    const int part = lane % G;
     T4 x[2];
     int ti[2];
     bool valid[2];
     T acc[2] = {(T)0, (T)0};
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        ti[u] = tb + lane + 32 * u;
+        ti[u] = tb + lane / G + 32 * u;
         valid[u] = u < TPL && ti[u] < te;
         x[u] = valid[u] ? P.pts[ti[u]] : P.pts[tb];
     }
@@ -135,12 +140,15 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
                 if (lane < cnt) sp[lane] = P.pts[sb + lane];
                 __syncwarp();
                 if (s == t)
-                    accumulate_chunk<T, TPL, true>(sp, cnt, sb, x, ti, P.eps2, acc);
+                    accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
                 else
-                    accumulate_chunk<T, TPL, false>(sp, cnt, sb, x, ti, P.eps2, acc);
+                    accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
             }
         }
     }
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
+    if (part != 0) return;
     T4 c;
     T ia = (T)1;
     if (P.far) {
@@ -178,10 +186,15 @@ template <typename T> __global__ void __launch_bounds__(128) k_p2p_l2p(const Nea
         __syncwarp();
     }
     const int2 rg = P.range[t];
-    if (rg.y - rg.x <= 32) {
-        leaf_block<T, 1>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
+    const int nt = rg.y - rg.x;
+    if (nt <= 8) {
+        leaf_block<T, 1, 4>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
+    } else if (nt <= 16) {
+        leaf_block<T, 1, 2>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
+    } else if (nt <= 32) {
+        leaf_block<T, 1, 1>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
     } else {
-        for (int tb = rg.x; tb < rg.y; tb += 64) leaf_block<T, 2>(P, t, tb, min(rg.y, tb + 64), sp[wl], sL[wl]);
+        for (int tb = rg.x; tb < rg.y; tb += 64) leaf_block<T, 2, 1>(P, t, tb, min(rg.y, tb + 64), sp[wl], sL[wl]);
     }
 }
 
