@@ -56,9 +56,12 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["fmm_matvec", "sphere_solve", "torus_solve"], default="fmm_matvec",
+    ap.add_argument("--workload", choices=["fmm_matvec", "sphere_solve", "torus_solve", "batch_solve"],
+                    default="fmm_matvec",
                     help="fmm_matvec: the headline operator benchmark; sphere_solve: 5,120-panel icosphere dense "
-                         "FP64 solve; torus_solve: 200,000-panel torus, FMM + near correction, mixed-precision solve")
+                         "FP64 solve; torus_solve: 200,000-panel torus, FMM + near correction, mixed-precision solve; "
+                         "batch_solve: 256 sphere dimers of 2k-40k panels solved together")
+    ap.add_argument("--batch", type=int, default=256, help="instances of the batch_solve workload")
     return ap.parse_args()
 
 
@@ -196,33 +199,6 @@ def _solve_case(name):
     return torus_mesh(1.0, 0.35, 500, 200), spec, dict(depth_self=4, near=True, kind="fmm")
 
 
-def _solve_system(mesh, spec, opts, dev, dtypes):
-    """Device-resident operator(s), right-hand side, Jacobi diagonal and x0
-    exactly as bem_solve assembles them."""
-    import numpy as np
-    import torch
-
-    from electrodrive_gb300.core.bem import bc_vector, build_operator, point_charges
-    from electrodrive_gb300.core.bem_near import NearCorrection, point_charge_potential, self_integrals
-
-    PV = mesh.vertices[mesh.triangles]
-    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
-    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
-    I_self = self_integrals(PV, mesh.centroids, order=2, depth=opts["depth_self"], device=dev)
-    A_dev = A64.to(dev)
-    self_corr = I_self / A_dev.clamp_min(torch.finfo(torch.float64).tiny)
-    ops = {}
-    for dt in dtypes:
-        near = (NearCorrection(mesh.centroids, mesh.areas, PV, distance_factor=1.5, order=2, depth=3, dtype=dt,
-                               device=dev) if opts["near"] else None)
-        ops[dt] = build_operator(C64, A64, self_corr.to(dt), dtype=dt, kind=opts["kind"], near=near, device=dev)
-    V_free = point_charge_potential(C64.to(dev), point_charges(spec))
-    b = torch.as_tensor(bc_vector(spec, mesh), dtype=torch.float64, device=dev) - V_free
-    diag = I_self.clamp_min(1e-18)
-    return dict(ops=ops, b=b, diag=diag, x0=b / diag, A=A_dev, C=C64, n=mesh.n_panels,
-                near_pairs=0 if not opts["near"] else ops[dtypes[0]].near.n_pairs)
-
-
 def _time_cuda(fn, dev, stream, flush, warmup, steps):
     import torch
 
@@ -318,7 +294,9 @@ def run_solve_workload(args, rank, world, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     t_setup = time.perf_counter()
     dtypes = [torch.float64] if name == "sphere_solve" else [torch.float64, torch.float32]
-    sysd = _solve_system(mesh, spec, opts, dev, dtypes)
+    from electrodrive_gb300.core.bem import assemble_system
+
+    sysd = assemble_system(mesh, spec, kind=opts["kind"], dtypes=tuple(dtypes), near=opts["near"], device=dev)
     torch.cuda.synchronize(dev)
     t_setup = time.perf_counter() - t_setup
     op64 = sysd["ops"][torch.float64]
@@ -329,12 +307,22 @@ def run_solve_workload(args, rank, world, local):
     if name == "sphere_solve":
         def step():
             result["x"], result["info"] = gmres_restart(op64, b, restart=50, tol=1e-8, maxiter=2000, precond="jacobi",
-                                                        areas=sysd["A"], A_diag=diag, x0=x0, use_graph=True)
+                                                        areas=sysd["areas"], A_diag=diag, x0=x0, use_graph=True)
     else:
         op32 = sysd["ops"][torch.float32]
+        net = geom = None
+        weights = os.path.join(ROOT, "electrodrive_gb300", "data", "pcn_weights.npz")
+        if os.path.exists(weights):
+            from electrodrive_gb300.core.warm_start import PointCloudNet, panel_geometry, warm_start
+
+            net = PointCloudNet.load(weights, device=dev)
+            geom = panel_geometry(mesh, dev)
 
         def step():
-            result["x"], result["info"] = solve_mixed(op64, op32, b, A_diag=diag, x0=x0, rtol=1e-6,
+            # the learned warm start (features, network, one FP32 operator application) is part of the step
+            xs = warm_start(net, geom, b, op32) if net is not None else x0
+            result["x0"] = xs
+            result["x"], result["info"] = solve_mixed(op64, op32, b, A_diag=diag, x0=xs, rtol=1e-6,
                                                       inner_restart=40)
 
     warm = max(args.warmup, 3)
@@ -377,7 +365,8 @@ def run_solve_workload(args, rank, world, local):
         u = u / u.norm(dim=1, keepdim=True)
         r = 1.2 + 1.8 * torch.rand(1000, 1, generator=g, dtype=torch.float64)
         pts = (u * r).numpy()
-        sol = BEMSolution(centroids=sysd["C"].to(dev), areas=sysd["A"], sigma=x.double(), charges=[(1.0, (0, 0, 2.0))])
+        sol = BEMSolution(centroids=sysd["centroids"].to(dev), areas=sysd["areas"], sigma=x.double(),
+                          charges=[(1.0, (0, 0, 2.0))])
         v = sol.eval(torch.as_tensor(pts, device=dev)).cpu().numpy()
         from electrodrive_gb300.utils.config import K_E
 
@@ -395,7 +384,7 @@ def run_solve_workload(args, rank, world, local):
 
         def plain_solve():
             plain["x"], plain["info"] = gmres_restart(op64, b, restart=256, tol=1e-6 * bn / r0, maxiter=4000,
-                                                      precond="jacobi", areas=sysd["A"], A_diag=diag, x0=x0,
+                                                      precond="jacobi", areas=sysd["areas"], A_diag=diag, x0=x0,
                                                       use_graph=True)
         t_plain = _time_cuda(plain_solve, dev, stream, flush, 0, 1)[0]
         pinfo = plain["info"]
@@ -403,7 +392,7 @@ def run_solve_workload(args, rank, world, local):
         p64 = op64.base.plan
         p32 = op32.base.plan
         fp32_peak = _lib.measure_fp32_peak()
-        p32.set_charges(sig.float() * sysd["A"].float())
+        p32.set_charges(sig.float() * sysd["areas"].float())
         m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 2, 5))
         achieved = p32.info.n_m2l_pairs * M2L_FLOPS_PER_PAIR / (m2l_ms * 1e-3) / 1e12
         roof = {"kernel": "k_m2l_fast (M2L of the FP32 inner operator)", "bound": "fp32", "achieved": achieved,
@@ -421,6 +410,20 @@ def run_solve_workload(args, rank, world, local):
                  "n_p2p_pairs_fp32": p32.info.n_p2p_pairs, "p2p_interactions_fp32": p32.info.p2p_interactions,
                  "n_m2l_pairs_fp64": p64.info.n_m2l_pairs, "m2l_fp32_ms": m2l_ms}
         plain_matvecs = pinfo["iters"] + pinfo["iters"] // 256 + 2
+        # the same mixed solver from the cold start (x0 = b / I_self)
+        cold = {}
+
+        def cold_solve():
+            cold["x"], cold["info"] = solve_mixed(op64, op32, b, A_diag=diag, x0=x0, rtol=1e-6, inner_restart=40)
+        t_cold = statistics.median(_time_cuda(cold_solve, dev, stream, flush, 1, 2))
+        extra["mixed_cold_start"] = {"ms": t_cold, "solves_per_s": 1e3 / t_cold, "outer_iters": cold["info"]["outer"],
+                                     "inner_iters": cold["info"]["inner_iters"]}
+        extra["warm_start"] = "learned (electrodrive_gb300/data/pcn_weights.npz)" if net is not None else "none"
+        if net is not None:
+            from electrodrive_gb300.core.warm_start import relative_error
+
+            extra["start_rel_error"] = {"learned": relative_error(result["x0"], plain["x"], sysd["areas"]),
+                                        "cold": relative_error(x0, plain["x"], sysd["areas"])}
         cfg = BEMConfig(use_near_quadrature_matvec=True)
         e2e_call = lambda: bem_solve(spec, cfg, mesh=mesh, operator="fmm", self_integral="quadrature", mixed=True,
                                      mixed_rtol=1e-6, inner_restart=40)
@@ -462,11 +465,140 @@ def run_solve_workload(args, rank, world, local):
         print(json.dumps(out), flush=True)
 
 
+def run_batch_workload(args, rank, world, local):
+    """batch_solve: K sphere dimers (seeds 10 + i, 2k-40k panels each, grounded,
+    one point charge each) solved together to a 1e-6 relative true residual
+    per instance; one step = one batched solve of all K (solves/s = K / t)."""
+    import numpy as np
+
+    from electrodrive_gb300.core.batch import dimer_case
+
+    K = args.batch
+    cases = [dimer_case(10 + i) for i in range(K)]
+    n_total = sum(m.n_panels for m, _ in cases)
+    workload = (f"batch_solve_{K}_sphere_dimers_seeds10+i_2k-40k_panels_{n_total}_total_fmm_p8_"
+                "mixed_fp32_inner_autotuned_fp64_refinement_rtol1e-6_per_instance")
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle as O
+
+        O.lib()
+        m0, _ = cases[0]
+        t = O.build_tree(m0.centroids, 64, 32)
+        lists = O.build_lists(t, 0.5)
+        sig = np.ones(m0.n_panels)
+        t0 = time.perf_counter()
+        O.fmm_matvec(t, lists, m0.centroids, sig, m0.areas, None, p=8)
+        dt = time.perf_counter() - t0
+        # plain method: about 40 operator applications per instance (measured on the GPU path)
+        val = K / (dt * n_total / m0.n_panels * 40)
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * K / val,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": {"workload": workload, "n_panels": n_total},
+                          "cpu_baseline": {"value": val, "unit": "solves/s", "cores": O.num_threads(), "kind": "port",
+                                           "sample": f"one FP64 FMM matvec of the oracle on instance 0 "
+                                                     f"({m0.n_panels} panels, {dt:.2f} s) scaled to all {n_total} "
+                                                     "panels x 40 operator applications per solve"},
+                          "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+
+    import torch
+
+    from electrodrive_gb300 import _lib
+    from electrodrive_gb300.core.batch import BatchSystem, autotune_inner, plain_fp64_solve
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    t0 = time.perf_counter()
+    system = BatchSystem(cases, device=dev)
+    torch.cuda.synchronize(dev)
+    t_setup = time.perf_counter() - t0
+    tune = autotune_inner(system)
+    result = {}
+
+    def step():
+        result["x"], result["info"] = system.solve()
+
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        step()
+    torch.cuda.synchronize(dev)
+    l0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        times = _time_cuda(step, dev, stream, flush, 0, args.steps)
+    launches = _lib.launch_count() - l0
+    ms = sum(times) / len(times)
+    value = world * K * 1e3 / ms
+    info = result["info"]
+    per = system.residuals(result["x"]).cpu().numpy()
+    mv = {"float64": statistics.median(_time_cuda(lambda: system.op64(system.x0_cold), dev, stream, flush, 1, 3)),
+          "float32": statistics.median(_time_cuda(lambda: system.op32(system.x0_cold.float()), dev, stream, flush,
+                                                  1, 3))}
+    p32 = system.op32.plan
+    p32.set_charges(system.x0_cold.float() * system.areas.float())
+    m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 1, 3))
+    fp32_peak = _lib.measure_fp32_peak()
+    from electrodrive_gb300.core.batch import plain_fp64_solve as _plain
+
+    sub = min(8, K)
+    plain = [_plain(*cases[i], device=dev) for i in range(sub)]
+    n_sub = sum(p["n"] for p in plain)
+    t_plain_all = sum(p["seconds"] for p in plain) * n_total / n_sub
+    # end to end: host meshes -> batched set-up -> solve -> sigma on the host
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sys2 = BatchSystem(cases, device=dev, inner_leaf_size=tune["leaf_size"],
+                       inner_expansion_order=tune["expansion_order"])
+    x2, _ = sys2.solve()
+    x2.cpu()
+    e2e_ms = 1e3 * (time.perf_counter() - t0)
+    del sys2
+    if rank == 0:
+        order = tune["expansion_order"]
+        flops_pair = 4 * 45 * 81 + 2 * 8 * 45 + 6 * 153 if order == 8 else None
+        ach = p32.info.n_m2l_pairs * flops_pair / (m2l_ms * 1e-3) / 1e12 if flops_pair else None
+        out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+               "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32+f64", "data": "synthetic",
+               "config": {"workload": workload, "instances": K, "n_panels": n_total, "setup_s": t_setup,
+                          "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
+                          "inner_operator": {k: tune[k] for k in ("leaf_size", "expansion_order", "ms")}},
+               "solve": {"code": info["code"], "outer_iters": info["outer"], "inner_iters": info["inner_iters"],
+                         "fp64_matvecs": info["matvec64"], "max_instance_rel_resid": float(per.max()),
+                         "instances_converged": int((per <= 1e-6 * (1 + 1e-9)).sum()),
+                         "plain_fp64_per_instance": {"instances_timed": sub, "panels_timed": n_sub,
+                                                     "mean_iters": float(np.mean([p["iters"] for p in plain])),
+                                                     "seconds_timed": sum(p["seconds"] for p in plain),
+                                                     "seconds_all_extrapolated_by_panels": t_plain_all,
+                                                     "solves_per_s": K / t_plain_all},
+                         "speedup_vs_plain_fp64": t_plain_all / (ms * 1e-3)},
+               "autotune_trials": tune["trials"], "matvec_ms": mv,
+               "e2e": {"value": world * K * 1e3 / e2e_ms, "unit": "solves/s",
+                       "h2d_bytes_per_step": int(n_total * 8 * (3 + 1 + 9)), "d2h_bytes_per_step": int(8 * n_total),
+                       "ms_per_step": e2e_ms, "includes": "batched set-up from the host meshes (trees, lists, "
+                                                           "self integrals, rhs), the solve and the read-back"},
+               "gpu_launches": int(launches), "clocks": clk.summary(),
+               "roofline": {"kernel": "k_m2l_fast (M2L of the FP32 inner operator)", "bound": "fp32",
+                            "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                            "frac": ach / fp32_peak if ach else None, "traffic": None,
+                            "peak_source": "FP32 FMA probe measured in this run"},
+               "cpu_baseline": None}
+        print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "batch_solve":
+        run_batch_workload(args, rank, world, local)
+        return
     if args.workload != "fmm_matvec":
         run_solve_workload(args, rank, world, local)
         return

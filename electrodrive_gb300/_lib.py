@@ -68,6 +68,7 @@ def _declare(L):
         "edfmm_version": (C.c_char_p, []),
         "edfmm_launch_count": (i64, []),
         "edfmm_plan_create": (i32, [_vp, i64, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
+        "edfmm_plan_create_batch": (i32, [_vp, C.POINTER(i64), i32, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_destroy": (i32, [_vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
@@ -85,6 +86,13 @@ def _declare(L):
         "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
         "edfmm_measure_fp64_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
+        "edfmm_pcn_num_params": (i64, []),
+        "edfmm_pcn_workspace_bytes": (C.c_size_t, [i64]),
+        "edfmm_pcn_features": (i32, [_vp, _vp, _vp, _vp, i64, _vp, _vp, C.c_size_t, _vp]),
+        "edfmm_pcn_forward": (i32, [_vp, _vp, i64, _vp, _vp, C.c_size_t, _vp]),
+        "edfmm_pcn_backward": (i32, [_vp, i64, _vp, _vp, _vp, C.c_size_t, _vp]),
+        "edfmm_pcn_loss": (i32, [_vp, _vp, _vp, _vp, i64, _vp, _vp, _vp]),
+        "edfmm_pcn_adam": (i32, [_vp, _vp, _vp, _vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, i32, _vp]),
         "edfmm_dense_matvec": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_matvec_noalloc": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_workspace_bytes": (C.c_size_t, [i64, i32]),
@@ -213,7 +221,10 @@ class Plan:
     """Owns an edfmm_plan: device octree + interaction lists + expansion buffers."""
 
     def __init__(self, points: torch.Tensor, *, leaf_size: int = 64, max_depth: int = 32,
-                 mac_theta: float = 0.5, expansion_order: int = 8):
+                 mac_theta: float = 0.5, expansion_order: int = 8, instance_offsets=None):
+        """``instance_offsets`` (K + 1 row offsets) makes a batched plan: K
+        independent point sets, each with its own tree and lists, applied as
+        one block-diagonal operator."""
         L = load_library()
         if points.ndim != 2 or points.shape[-1] != 3:
             raise ValueError(f"points must have shape (N, 3), got {tuple(points.shape)}")
@@ -223,9 +234,21 @@ class Plan:
         self.device = pts.device
         self.dtype = pts.dtype
         h = _vp()
+        self.instance_offsets = None
         with torch.cuda.device(self.device):
-            rc = L.edfmm_plan_create(ptr(pts), pts.shape[0], dtype_code(pts.dtype), int(leaf_size), int(max_depth),
-                                     float(mac_theta), int(expansion_order), stream_handle(self.device), C.byref(h))
+            if instance_offsets is None:
+                rc = L.edfmm_plan_create(ptr(pts), pts.shape[0], dtype_code(pts.dtype), int(leaf_size),
+                                         int(max_depth), float(mac_theta), int(expansion_order),
+                                         stream_handle(self.device), C.byref(h))
+            else:
+                off = [int(x) for x in instance_offsets]
+                if off[-1] != pts.shape[0]:
+                    raise ValueError("instance_offsets must end at the number of points")
+                arr = (C.c_int64 * len(off))(*off)
+                rc = L.edfmm_plan_create_batch(ptr(pts), arr, len(off) - 1, dtype_code(pts.dtype), int(leaf_size),
+                                               int(max_depth), float(mac_theta), int(expansion_order),
+                                               stream_handle(self.device), C.byref(h))
+                self.instance_offsets = off
         check(rc, "edfmm_plan_create")
         self._h = h
         self._lib = L

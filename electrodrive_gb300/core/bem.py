@@ -212,22 +212,70 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
                                          gmres_iters=info["iters"])], boundary_samples=None, sample_points=None)
 
 
+def assemble_system(mesh: TriMesh, spec: Any, *, kind: str = "dense", dtypes=(torch.float64,), near: bool = False,
+                    self_integral: str = "quadrature", device=None) -> Dict[str, Any]:
+    """The pieces bem_solve assembles, on the device: one operator per dtype
+    (with the near correction when ``near``), the FP64 right-hand side
+    b = bc - V_free, the Jacobi diagonal I_self and the reference's x0 = b / I_self."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    PV = mesh.vertices[mesh.triangles]
+    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
+    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
+    depth_self, depth_near = quad_depths(spec)
+    if self_integral == "quadrature":
+        I_self = self_integrals(PV, mesh.centroids, order=2, depth=depth_self, device=dev)
+    else:
+        a = np.clip(mesh.areas, 0.0, None)
+        I_self = torch.as_tensor(np.where(mesh.areas > 0, 2.0 * np.pi * K_E * np.sqrt(a / np.pi), 0.0),
+                                 dtype=torch.float64, device=dev)
+    A_dev = A64.to(dev)
+    self_corr = I_self / A_dev.clamp_min(torch.finfo(torch.float64).tiny)
+    ops = {}
+    for dt in dtypes:
+        nc = (NearCorrection(mesh.centroids, mesh.areas, PV, distance_factor=1.5, order=2, depth=depth_near, dtype=dt,
+                             device=dev) if near and mesh.n_panels > 1 else None)
+        ops[dt] = build_operator(C64, A64, self_corr.to(dt), dtype=dt, kind=kind, near=nc, device=dev)
+    charges = point_charges(spec)
+    V_free = point_charge_potential(C64.to(dev), charges) if charges else torch.zeros(mesh.n_panels, dtype=torch.float64,
+                                                                                       device=dev)
+    b = torch.as_tensor(bc_vector(spec, mesh), dtype=torch.float64, device=dev) - V_free
+    diag = I_self.clamp_min(1e-18)
+    return dict(ops=ops, b=b, diag=diag, x0=b / diag, areas=A_dev, centroids=C64, n=mesh.n_panels,
+                near_pairs=0 if not near else next(iter(ops.values())).near.n_pairs, charges=charges)
+
+
+def segment_norms(v: Tensor, offsets: Optional[List[int]]) -> Tensor:
+    """2-norm of each slice [offsets[k], offsets[k+1]) of v (FP64)."""
+    v2 = v.to(torch.float64) ** 2
+    if offsets is None:
+        return torch.sqrt(v2.sum()).reshape(1)
+    c = torch.cat([torch.zeros(1, dtype=torch.float64, device=v.device), torch.cumsum(v2, 0)])
+    o = torch.as_tensor(offsets, device=v.device)
+    return torch.sqrt((c[o[1:]] - c[o[:-1]]).clamp_min(0.0))
+
+
 def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: Optional[Tensor] = None,
-                rtol: float = 1e-6, inner_restart: int = 40, inner_tol: float = 1e-4, inner_maxiter: int = 400,
-                max_outer: int = 30, use_graph: bool = True, inner_early_exit: Optional[int] = 8
+                rtol: float = 1e-6, inner_restart: int = 40, inner_tol: Optional[float] = None,
+                inner_tol_floor: float = 1e-5, inner_maxiter: int = 400, max_outer: int = 30, use_graph: bool = True,
+                inner_early_exit: Optional[int] = 8, segments: Optional[List[int]] = None
                 ) -> Tuple[Tensor, Dict[str, Any]]:
     """FP32 GMRES corrections inside FP64 iterative refinement.
 
-    Stops when ||b - A64 x|| / ||b|| <= rtol (FP64 true residual).  The FP32
-    inner solve is left-preconditioned by Jacobi with ``A_diag``; its cycles
-    may end early on the inner estimate (checked every ``inner_early_exit``
-    steps; None runs full cycles).
+    Stops when ||b - A64 x|| / ||b|| <= rtol (FP64 true residual; with
+    ``segments``, the row offsets of independent instances, every instance's
+    own relative residual must meet rtol).  The FP32 inner solve is
+    left-preconditioned by Jacobi with ``A_diag``; its cycles may end early on
+    the inner estimate (checked every ``inner_early_exit`` steps; None runs
+    full cycles).  Each inner solve aims at the reduction the outer target
+    still needs, 0.3 rtol / (current relative residual), but at most
+    ``inner_tol_floor`` (about what the FP32 operator can deliver against the
+    FP64 one); a fixed ``inner_tol`` overrides that.
     """
     dev = b.device
     b64 = b.to(torch.float64)
     x = torch.zeros_like(b64) if x0 is None else x0.to(torch.float64).clone()
-    bn = float(torch.linalg.norm(b64))
-    bn = bn if bn > 0 else 1.0
+    bseg = segment_norms(b64, segments)
+    bseg = torch.where(bseg > 0, bseg, torch.ones_like(bseg))
     d32 = None if A_diag is None else A_diag.to(dev, torch.float32)
     hist = []
     inner_total = 0
@@ -235,7 +283,7 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
     r = b64 - op64(x)
     matvec64 += 1
     for it in range(max_outer + 1):
-        rel = float(torch.linalg.norm(r)) / bn
+        rel = float((segment_norms(r, segments) / bseg).max())
         hist.append(rel)
         if not math.isfinite(rel):
             return x, dict(success=False, code=6, outer=it, inner_iters=inner_total, rel_resid=rel, history=hist,
@@ -245,8 +293,9 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
                            matvec64=matvec64)
         if it == max_outer:
             break
+        tol_k = inner_tol if inner_tol is not None else min(0.1, max(inner_tol_floor, 0.3 * rtol / rel))
         r32 = r.to(torch.float32)
-        d, info = gmres_restart(op32, r32, restart=inner_restart, tol=inner_tol, maxiter=inner_maxiter,
+        d, info = gmres_restart(op32, r32, restart=inner_restart, tol=tol_k, maxiter=inner_maxiter,
                                 precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph,
                                 early_exit=inner_early_exit)
         inner_total += info["iters"]
@@ -257,5 +306,5 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
                    matvec64=matvec64)
 
 
-__all__ = ["BEMOperator", "BEMSolution", "bem_solve", "build_operator", "bc_vector", "point_charges", "quad_depths",
-           "solve_mixed"]
+__all__ = ["BEMOperator", "BEMSolution", "assemble_system", "bem_solve", "build_operator", "bc_vector", "point_charges",
+           "quad_depths", "segment_norms", "solve_mixed"]

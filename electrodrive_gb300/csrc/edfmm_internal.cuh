@@ -148,6 +148,9 @@ struct DevLists {
 };
 
 int lists_build(const DevTree &tree, double theta, DevLists &lists, cudaStream_t s);
+// pack per-instance trees and lists into one (batch.cu)
+int pack_batch(std::vector<DevTree> &trees, std::vector<DevLists> &lists, int dtype, DevTree &T, DevLists &L,
+               cudaStream_t s);
 int lists_build_swapped(const DevTree &tree, DevLists &lists, cudaStream_t s);
 
 // ---------------------------------------------------------------------------

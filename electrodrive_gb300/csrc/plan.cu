@@ -137,6 +137,62 @@ int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_siz
     return EDFMM_OK;
 }
 
+int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int n_instances, int dtype, int leaf_size,
+                            int max_depth, double mac_theta, int expansion_order, void *stream, edfmm_plan **plan_out) {
+    if (!plan_out) return fail(EDFMM_ERR_ARG, "plan_out is NULL");
+    *plan_out = nullptr;
+    if (n_instances <= 0 || !offsets || !points_dev) return fail(EDFMM_ERR_ARG, "need points, offsets and >= 1 instance");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (leaf_size <= 0) return fail(EDFMM_ERR_ARG, "leaf_size must be positive");
+    if (max_depth <= 0 || max_depth > 64) return fail(EDFMM_ERR_ARG, "max_depth must be in [1, 64]");
+    if (!(mac_theta > 0.0 && mac_theta < 1.0)) return fail(EDFMM_ERR_ARG, "mac_theta must be in (0, 1)");
+    if (expansion_order < 1 || expansion_order > 10)
+        return fail(EDFMM_ERR_UNSUPPORTED, "expansion_order must be in [1, 10]");
+    if (offsets[0] != 0) return fail(EDFMM_ERR_ARG, "offsets[0] must be 0");
+    for (int i = 0; i < n_instances; ++i)
+        if (offsets[i + 1] <= offsets[i]) return fail(EDFMM_ERR_ARG, "every instance needs at least one point");
+    int rc = upload_tables();
+    if (rc) return rc;
+    cudaStream_t s = S(stream);
+    const size_t esz_pt = (dtype == EDFMM_F64 ? 8 : 4) * 3;
+    std::vector<DevTree> trees(n_instances);
+    std::vector<DevLists> lists(n_instances);
+    for (int i = 0; i < n_instances; ++i) {
+        const void *pts = static_cast<const char *>(points_dev) + esz_pt * offsets[i];
+        if ((rc = tree_build(pts, offsets[i + 1] - offsets[i], dtype, leaf_size, max_depth, trees[i], s))) return rc;
+        if ((rc = lists_build(trees[i], mac_theta, lists[i], s))) return rc;
+    }
+    edfmm_plan *p = new edfmm_plan();
+    cudaGetDevice(&p->device);
+    p->mac_theta = mac_theta;
+    p->leaf_size = leaf_size;
+    p->max_depth = max_depth;
+    rc = pack_batch(trees, lists, dtype, p->tree, p->lists, s);
+    trees.clear();
+    lists.clear();
+    if (!rc) {
+        p->fmm.p = expansion_order;
+        p->fmm.nc = num_coeffs(expansion_order);
+        p->fmm.nc_pad = (p->fmm.nc + 1) & ~1;
+        size_t esz = (dtype == EDFMM_F64 ? 16 : 8) * (size_t)p->fmm.nc_pad * (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
+        rc = p->fmm.multipoles.reserve(esz);
+        if (!rc) rc = p->fmm.locals.reserve(esz);
+        if (!rc) rc = p->fmm.translated.reserve(esz);
+        if (!rc) {
+            cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("plan set-up: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *plan_out = p;
+    return EDFMM_OK;
+}
+
 int edfmm_plan_destroy(edfmm_plan *plan) {
     delete plan;
     return EDFMM_OK;

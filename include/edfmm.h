@@ -85,6 +85,19 @@ EDFMM_API const char *edfmm_version(void);
 EDFMM_API int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth,
                       double mac_theta, int expansion_order, void *stream, edfmm_plan **plan_out);
 
+/*
+ * Batched plan (no counterpart in the reference, which solves one geometry at
+ * a time): points_dev holds n_instances independent point sets back to back,
+ * instance k at rows [offsets[k], offsets[k+1]) (offsets: host array of
+ * n_instances + 1 values, offsets[0] = 0, every instance non-empty).  Each
+ * instance gets the tree and lists edfmm_plan_create would build for it
+ * alone; they are packed into one plan whose matvec is the block-diagonal
+ * operator (no interaction between instances), one launch per stage for the
+ * whole batch.
+ */
+EDFMM_API int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int n_instances, int dtype,
+                                      int leaf_size, int max_depth, double mac_theta, int expansion_order,
+                                      void *stream, edfmm_plan **plan_out);
 EDFMM_API int edfmm_plan_destroy(edfmm_plan *plan);
 
 /*
@@ -302,6 +315,36 @@ EDFMM_API int64_t edfmm_launch_count(void);
  * No counterpart in the reference (it has no GPU kernels for the FMM).
  */
 EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_out);
+
+/*
+ * Point-cloud warm-start network (no counterpart in the reference: it maps
+ * per-panel features to an initial surface charge density for the GMRES
+ * start).  Width 128, 16 input features (8 used), BF16 weights/activations on
+ * the tensor cores, FP32 accumulation.  Parameters are one FP32 block of
+ * edfmm_pcn_num_params() values: W1[128x16] b1[128] W2[128x128] V2[128x128]
+ * b2[128] W3[128x128] b3[128] w4[128] b4.  The workspace holds the
+ * activations of one forward pass, which edfmm_pcn_backward reuses (call it
+ * with the same workspace right after the forward).  All pointers are device
+ * pointers; the calls are stream-ordered and deterministic.
+ */
+#define EDFMM_PCN_WIDTH 128
+#define EDFMM_PCN_INPUTS 16
+EDFMM_API int64_t edfmm_pcn_num_params(void);
+EDFMM_API size_t edfmm_pcn_workspace_bytes(int64_t n);
+/* features (n x 16 FP32): centroid relative to the mean centroid over the
+ * RMS radius R, unit normal, log(area / R^2), rhs / RMS rhs, zeros */
+EDFMM_API int edfmm_pcn_features(const double *centroids_dev, const double *normals_dev, const double *areas_dev,
+                                 const double *rhs_dev, int64_t n, float *features_dev, void *ws_dev, size_t ws_bytes,
+                                 void *stream);
+EDFMM_API int edfmm_pcn_forward(const float *params_dev, const float *features_dev, int64_t n, float *y_dev,
+                                void *ws_dev, size_t ws_bytes, void *stream);
+EDFMM_API int edfmm_pcn_backward(const float *params_dev, int64_t n, const float *dy_dev, float *grads_dev,
+                                 void *ws_dev, size_t ws_bytes, void *stream);
+/* L = sum_i A_i (s_i (1 + y_i) - sigma_i)^2 / sum_i A_i sigma_i^2 and dL/dy */
+EDFMM_API int edfmm_pcn_loss(const float *y_dev, const double *scale_dev, const double *sigma_dev,
+                             const double *areas_dev, int64_t n, float *dy_dev, double *loss_dev, void *stream);
+EDFMM_API int edfmm_pcn_adam(float *params_dev, const float *grads_dev, float *m_dev, float *v_dev, int64_t count,
+                             float lr, float beta1, float beta2, float eps, int step, void *stream);
 
 /*
  * Measured FP64 FMA throughput (TFLOP/s): the roofline denominator of the
