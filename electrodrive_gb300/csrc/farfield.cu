@@ -163,22 +163,23 @@ __global__ void __launch_bounds__(128) k_m2m(const int32_t *__restrict__ nodes, 
 // Output split for the register budget: at high order the 45 accumulators,
 // the 45 source coefficients and one harmonics column do not fit in 255
 // registers together, so the target coefficients are divided by m-column
-// into two sets of nearly equal work (greedy on the per-column cost P+1-m)
-// and each set is computed by its own pass.  SET 0 = all columns.
+// into sets of nearly equal work (greedy on the per-column cost P+1-m) and
+// each set is computed by its own pass.  SET 0 = all columns; SET 1, 2 = the
+// two-way split; SET 10 k + j = part j (1-based) of a k-way split.
 template <int P> __host__ __device__ constexpr bool m_in_set(int m, int set) {
     if (set == 0) return true;
-    int wa = 0, wb = 0;
-    bool in_a = false;
+    const int ns = set >= 10 ? set / 10 : 2;
+    const int which = set >= 10 ? set % 10 : set;
+    int load[4] = {0, 0, 0, 0};
+    int bin = 0;
     for (int mm = 0; mm <= P; ++mm) {
-        const int w = P + 1 - mm;
-        const bool a = wa <= wb;
-        if (a)
-            wa += w;
-        else
-            wb += w;
-        if (mm == m) in_a = a;
+        int b = 0;
+        for (int k = 1; k < ns; ++k)
+            if (load[k] < load[b]) b = k;
+        load[b] += P + 1 - mm;
+        if (mm == m) bin = b;
     }
-    return set == 1 ? in_a : !in_a;
+    return bin + 1 == which;
 }
 template <int P> constexpr int m2l_passes() { return P >= 7 ? 2 : 1; }
 
@@ -333,7 +334,7 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
 }
 
 template <int P, int SET>
-__global__ void __launch_bounds__(128) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
+__global__ void __launch_bounds__(128, (SET >= 30 ? 3 : 1)) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
                                                    const int32_t *__restrict__ src, const float4 *__restrict__ center,
                                                    const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
                                                    float2 *__restrict__ Lexp, int nc_pad) {
@@ -1151,8 +1152,18 @@ int build_extreme(const DevTree &tree, const int32_t *off, const int32_t *src, E
 template <int P>
 void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const float4 *cen,
                      const float4 *hal, const float2 *Mx, float2 *Lx, int nc_pad, cudaStream_t s) {
+    static const bool three = [] {
+        const char *v = getenv("EDFMM_M2L_SETS");
+        return v && v[0] == '3';
+    }();
     if constexpr (m2l_passes<P>() == 1) {
         k_m2l_fast<P, 0><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+    } else if (three && P == 8) {
+        k_m2l_fast<P, 31><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        count_launch();
+        k_m2l_fast<P, 32><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        count_launch();
+        k_m2l_fast<P, 33><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
     } else {
         k_m2l_fast<P, 1><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
         count_launch();

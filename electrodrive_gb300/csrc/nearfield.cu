@@ -109,6 +109,40 @@ __device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *s
     for (int u = 0; u < TPL; ++u) acc[u] += psum[u];
 }
 
+// FP32 form: the chunk is staged as separate x / y / z / q arrays and
+// sources are taken two at a time, so the distance and the accumulation run
+// as packed FP32 pairs (FADD2 / FMUL2 / FFMA2) and only the reciprocal square
+// roots and the eps clamp are scalar.  An odd chunk is padded with a
+// zero-charge source.
+template <int TPL, int G, bool SELF>
+__device__ __forceinline__ void accumulate_pairs(const float *sx, const float *sy, const float *sz, const float *sw,
+                                                 int cnt, int sbase, int part, const float2 (&nx)[2],
+                                                 const float2 (&ny)[2], const float2 (&nz)[2], const int (&ti)[2],
+                                                 float eps2, float (&acc)[2]) {
+    float2 ps[2] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+    const int np = (cnt + 1) >> 1;
+#pragma unroll 4
+    for (int j = part; j < np; j += G) {
+        const float2 qx = *reinterpret_cast<const float2 *>(sx + 2 * j);
+        const float2 qy = *reinterpret_cast<const float2 *>(sy + 2 * j);
+        const float2 qz = *reinterpret_cast<const float2 *>(sz + 2 * j);
+        const float2 qw = *reinterpret_cast<const float2 *>(sw + 2 * j);
+#pragma unroll
+        for (int u = 0; u < TPL; ++u) {
+            const float2 dx = __fadd2_rn(qx, nx[u]), dy = __fadd2_rn(qy, ny[u]), dz = __fadd2_rn(qz, nz[u]);
+            const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+            float i0 = rsqrtf(fmaxf(r2.x, eps2)), i1 = rsqrtf(fmaxf(r2.y, eps2));
+            if (SELF) {
+                if (sbase + 2 * j == ti[u]) i0 = 0.0f;
+                if (sbase + 2 * j + 1 == ti[u]) i1 = 0.0f;
+            }
+            ps[u] = __ffma2_rn(qw, make_float2(i0, i1), ps[u]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < TPL; ++u) acc[u] += ps[u].x + ps[u].y;
+}
+
 // One block of up to 32 * TPL / G targets of leaf t.  With G > 1 (small
 // leaves) G lanes share a target, each taking every G-th source of a chunk,
 // and their sums are combined with a fixed shuffle tree.
@@ -129,6 +163,13 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
         valid[u] = u < TPL && ti[u] < te;
         x[u] = valid[u] ? P.pts[ti[u]] : P.pts[tb];
     }
+    float2 nx[2], ny[2], nz[2];  // -x of each target, broadcast to both halves (FP32 path)
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        nx[u] = make_float2(-(float)x[u].x, -(float)x[u].x);
+        ny[u] = make_float2(-(float)x[u].y, -(float)x[u].y);
+        nz[u] = make_float2(-(float)x[u].z, -(float)x[u].z);
+    }
     if (P.near) {
         const int e = P.off[t + 1];
         for (int k = P.off[t]; k < e; ++k) {
@@ -137,12 +178,26 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
             for (int sb = sr.x; sb < sr.y; sb += 32) {
                 const int cnt = min(32, sr.y - sb);
                 __syncwarp();
-                if (lane < cnt) sp[lane] = P.pts[sb + lane];
-                __syncwarp();
-                if (s == t)
-                    accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
-                else
-                    accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
+                if constexpr (sizeof(T) == 4) {
+                    float *sx = reinterpret_cast<float *>(sp), *sy = sx + 32, *sz = sx + 64, *sw = sx + 96;
+                    const T4 q = lane < cnt ? P.pts[sb + lane] : T4{0.0f, 0.0f, 0.0f, 0.0f};
+                    sx[lane] = q.x;
+                    sy[lane] = q.y;
+                    sz[lane] = q.z;
+                    sw[lane] = q.w;
+                    __syncwarp();
+                    if (s == t)
+                        accumulate_pairs<TPL, G, true>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
+                    else
+                        accumulate_pairs<TPL, G, false>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
+                } else {
+                    if (lane < cnt) sp[lane] = P.pts[sb + lane];
+                    __syncwarp();
+                    if (s == t)
+                        accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
+                    else
+                        accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
+                }
             }
         }
     }
