@@ -70,6 +70,11 @@ def _declare(L):
         "edfmm_plan_create": (i32, [_vp, i64, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_create_batch": (i32, [_vp, C.POINTER(i64), i32, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_destroy": (i32, [_vp]),
+        "edfmm_targets_create": (i32, [_vp, _vp, i64, _vp, C.POINTER(_vp)]),
+        "edfmm_targets_destroy": (i32, [_vp]),
+        "edfmm_targets_info": (i32, [_vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+        "edfmm_targets_export_lists": (i32, [_vp, _vp, _vp, _vp]),
+        "edfmm_targets_potential": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
         "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
@@ -310,6 +315,11 @@ class Plan:
                 ptr(out["node_ranges"]), ptr(out["node_is_leaf"]), stream_handle(dev)), "edfmm_plan_export_tree")
         return out
 
+    def targets(self, points: torch.Tensor) -> "Targets":
+        """FMM evaluation at arbitrary points (a tree of the points plus the
+        interaction lists between this plan's tree and it)."""
+        return Targets(self, points)
+
     def export_lists(self):
         dev = self.device
         p2p = torch.empty(self.info.n_p2p_pairs, 2, dtype=torch.int64, device=dev)
@@ -371,3 +381,54 @@ class Plan:
         out = torch.empty(self.info.n_points, dtype=self.dtype, device=self.device)
         self.stage("l2p", ptr(out))
         return out
+
+
+class Targets:
+    """Owns an edfmm_targets: evaluation points of a plan's charges."""
+
+    def __init__(self, plan: "Plan", points: torch.Tensor):
+        if points.ndim != 2 or points.shape[-1] != 3 or not points.is_cuda:
+            raise ValueError("targets must be CUDA points of shape (M, 3)")
+        pts = points.to(plan.dtype).contiguous()
+        self.plan = plan  # keeps the source plan alive
+        self.device = plan.device
+        self.n = int(pts.shape[0])
+        L = plan._lib
+        self._lib = L
+        h = _vp()
+        with torch.cuda.device(self.device):
+            check(L.edfmm_targets_create(plan.handle, ptr(pts), self.n, stream_handle(self.device), C.byref(h)),
+                  "edfmm_targets_create")
+        self._h = h
+        v = [C.c_int64() for _ in range(4)]
+        check(L.edfmm_targets_info(h, *[C.byref(x) for x in v]), "edfmm_targets_info")
+        self.n_nodes, self.n_p2p_pairs, self.n_m2l_pairs, self.p2p_interactions = (int(x.value) for x in v)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.edfmm_targets_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def export_lists(self):
+        p2p = torch.empty(self.n_p2p_pairs, 2, dtype=torch.int64, device=self.device)
+        m2l = torch.empty(self.n_m2l_pairs, 2, dtype=torch.int64, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_targets_export_lists(self._h, ptr(p2p), ptr(m2l), stream_handle(self.device)),
+                  "edfmm_targets_export_lists")
+        return p2p, m2l
+
+    def potential(self, sigma: torch.Tensor, areas: torch.Tensor, *, k_e: float = 1.0, out=None, flags: int = 0):
+        dt = self.plan.dtype
+        s = sigma.to(self.device, dt).contiguous()
+        a = areas.to(self.device, dt).contiguous()
+        o = torch.empty(self.n, dtype=dt, device=self.device) if out is None else out
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_targets_potential(self._h, ptr(s), ptr(a), float(k_e), ptr(o), int(flags),
+                                                    stream_handle(self.device)), "edfmm_targets_potential")
+        return o

@@ -31,6 +31,9 @@ NVCC_FLAGS = [
     "-fvisibility=hidden",
     "--expt-relaxed-constexpr",
     "-DEDFMM_BUILD",
+    # device optimisation of the fully unrolled FMM kernels split over the
+    # host's cores (the far-field unit alone takes minutes serially)
+    "-split-compile=0",
 ]
 
 
@@ -42,7 +45,9 @@ def nvcc_path() -> str:
 
 
 def sources() -> list[str]:
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    """CUDA sources, the slowest to compile first."""
+    srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(srcs, key=lambda f: -os.path.getsize(f))
 
 
 def lib_path() -> str:

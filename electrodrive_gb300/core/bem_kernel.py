@@ -79,4 +79,32 @@ def bem_matvec_gpu(sigma: Tensor, src_centroids: Tensor, areas: Tensor, *, tile_
     return _dense(sigma, src_centroids, areas, self_integrals)
 
 
-__all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu"]
+def bem_potential_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor, sigma: Tensor, *,
+                          tile_size: int = 1024, method: str = "auto", fmm_threshold: int = 20000,
+                          leaf_size: int = 64, expansion_order: int = 8, mac_theta: float = 0.5) -> Tensor:
+    """Induced potential K_E sum_j sigma_j A_j / |x - c_j| at targets
+    (electrodrive/core/bem_kernel.py:233-335).  ``method`` "dense" is the
+    reference's direct sum (r^2 clamped at 1e-24); "fmm" builds a plan of the
+    panels and a target tree (distances clamped at the dtype's epsilon);
+    "auto" takes the FMM when panels x targets exceeds fmm_threshold^2."""
+    from ..utils.config import K_E
+    from .bem_near import potential_at_targets
+
+    _ensure_tile_size(tile_size)
+    if targets.ndim != 2 or targets.shape[-1] != 3:
+        raise ValueError("targets must have shape (M, 3)")
+    n, m = int(sigma.shape[0]), int(targets.shape[0])
+    if method not in ("auto", "dense", "fmm"):
+        raise ValueError(f"unknown method {method!r}")
+    use_fmm = method == "fmm" or (method == "auto" and n * m > fmm_threshold * fmm_threshold)
+    if not use_fmm:
+        return potential_at_targets(targets, src_centroids, sigma, areas)
+    dev = sigma.device if sigma.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    dt = sigma.dtype
+    plan = _lib.Plan(src_centroids.to(dev, dt).contiguous(), leaf_size=leaf_size, mac_theta=mac_theta,
+                     expansion_order=expansion_order)
+    tg = plan.targets(targets.to(dev, dt))
+    return tg.potential(sigma.to(dev, dt), areas.to(dev, dt), k_e=K_E)
+
+
+__all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu", "bem_potential_targets"]

@@ -152,6 +152,9 @@ int lists_build(const DevTree &tree, double theta, DevLists &lists, cudaStream_t
 int pack_batch(std::vector<DevTree> &trees, std::vector<DevLists> &lists, int dtype, DevTree &T, DevLists &L,
                cudaStream_t s);
 int lists_build_swapped(const DevTree &tree, DevLists &lists, cudaStream_t s);
+// lists between two trees: rows = target-tree nodes, sources = source-tree nodes
+// (the reference's build_interaction_lists(source_tree, target_tree))
+int lists_build_two(const DevTree &src_tree, const DevTree &tgt_tree, double theta, DevLists &lists, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // FMM stages (farfield.cu, nearfield.cu)
@@ -180,6 +183,8 @@ int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaS
 int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s);
+int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
+                FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 
 struct NearArgs {
@@ -191,6 +196,9 @@ struct NearArgs {
     bool scatter = false;             // write out[index_map[i]] with k_e, self term, clamp
     bool near = true;                 // include P2P
     bool far = true;                  // include L2P
+    // sources of the P2P when they are another tree's points (targets
+    // evaluated against a source plan): no self exclusion then
+    const struct DevTree *src_tree = nullptr;
 };
 int run_p2p_l2p(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
                 const NearArgs &args, cudaStream_t s);

@@ -335,15 +335,16 @@ __device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, fl
 
 template <int P, int SET>
 __global__ void __launch_bounds__(128, (SET >= 30 ? 3 : 1)) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
-                                                   const int32_t *__restrict__ src, const float4 *__restrict__ center,
+                                                   const int32_t *__restrict__ src, const float4 *__restrict__ tcenter,
+                                                   const float4 *__restrict__ thalf, const float4 *__restrict__ center,
                                                    const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
                                                    float2 *__restrict__ Lexp, int nc_pad) {
     constexpr int NC = ncoef(P);
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= n_nodes) return;
-    const float4 ct = center[t];
-    const float aL = half[t].w;
+    const float4 ct = tcenter[t];
+    const float aL = thalf[t].w;
     const float iaL = 1.0f / aL;
     float Ar[NC], Ai[NC];
 #pragma unroll
@@ -722,6 +723,8 @@ constexpr size_t m2l64_smem_bytes() {
 template <int P, int SET>
 __global__ void __launch_bounds__(128) k_m2l_fast64(int64_t n_nodes, const int32_t *__restrict__ off,
                                                     const int32_t *__restrict__ src,
+                                                    const double4 *__restrict__ tcenter,
+                                                    const double4 *__restrict__ thalf,
                                                     const double4 *__restrict__ center,
                                                     const double4 *__restrict__ half,
                                                     const double2 *__restrict__ Mexp, double2 *__restrict__ Lexp,
@@ -733,8 +736,8 @@ __global__ void __launch_bounds__(128) k_m2l_fast64(int64_t n_nodes, const int32
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= n_nodes) return;
-    const double4 ct = center[t];
-    const double aL = half[t].w;
+    const double4 ct = tcenter[t];
+    const double aL = thalf[t].w;
     const double iaL = 1.0 / aL;
 #pragma unroll
     for (int q = 0; q < NC; ++q) sA[q * 128] = make_double2(0.0, 0.0);
@@ -830,6 +833,8 @@ __global__ void __launch_bounds__(128) k_m2l_fast64(int64_t n_nodes, const int32
 template <typename T>
 __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32_t *__restrict__ row_ids,
                                                      const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+                                                     const typename Vec4<T>::type *__restrict__ tcenter,
+                                                     const typename Vec4<T>::type *__restrict__ thalf,
                                                      const typename Vec4<T>::type *__restrict__ center,
                                                      const typename Vec4<T>::type *__restrict__ half,
                                                      const Cplx<T> *__restrict__ Mexp, Cplx<T> *Lexp, int p, int nc_pad,
@@ -841,8 +846,8 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
     if (w >= n_rows) return;
     const int t = row_ids ? row_ids[w] : (int)w;
     const int nc = ncoef(p);
-    const typename Vec4<T>::type ct = center[t];
-    const T aL = half[t].w;
+    const typename Vec4<T>::type ct = tcenter[t];
+    const T aL = thalf[t].w;
     Cplx<T> acc[3] = {{0, 0}, {0, 0}, {0, 0}};
     for (int k = off[t]; k < off[t + 1]; ++k) {
         const int s = src[k];
@@ -930,23 +935,23 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
 }
 
 // extreme pairs (source radius > 256x target radius) as a CSR by target
-__global__ void k_extreme_flags(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *half,
-                                int32_t *row_cnt) {
+__global__ void k_extreme_flags(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *thalf,
+                                const float4 *half, int32_t *row_cnt) {
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= n_nodes) return;
-    const float iaL = 1.0f / half[t].w;
+    const float iaL = 1.0f / thalf[t].w;
     int c = 0;
     for (int k = off[t] + lane; k < off[t + 1]; k += 32) c += (half[src[k]].w * iaL > kExtremeRatio) ? 1 : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (lane == 0) row_cnt[t] = c;
 }
-__global__ void k_extreme_fill(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *half,
-                               const int32_t *eoff, int32_t *esrc) {
+__global__ void k_extreme_fill(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *thalf,
+                               const float4 *half, const int32_t *eoff, int32_t *esrc) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_nodes) return;
-    const float iaL = 1.0f / half[t].w;
+    const float iaL = 1.0f / thalf[t].w;
     int j = eoff[t];
     for (int k = off[t]; k < off[t + 1]; ++k)
         if (half[src[k]].w * iaL > kExtremeRatio) esrc[j++] = src[k];
@@ -1112,14 +1117,16 @@ template <typename T> int l2l_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
 }
 
 // extreme-pair CSR for one orientation (float plans only)
-int build_extreme(const DevTree &tree, const int32_t *off, const int32_t *src, ExtremeRows &ext, cudaStream_t s) {
+int build_extreme(const DevTree &tree, const DevTree &stree, const int32_t *off, const int32_t *src, ExtremeRows &ext,
+                  cudaStream_t s) {
     int rc;
     const int64_t M = tree.n_nodes;
     DevBuf cnt, tmp, total, flag, pos;
     if ((rc = cnt.reserve(sizeof(int32_t) * M)) || (rc = ext.off.reserve(sizeof(int32_t) * (M + 1))) ||
         (rc = tmp.reserve(scan_tmp_bytes(M))) || (rc = total.reserve(sizeof(int64_t))))
         return rc;
-    k_extreme_flags<<<nblk(M * 32, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<int32_t>(cnt));
+    k_extreme_flags<<<nblk(M * 32, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<float4>(stree.half),
+                                                      dptr<int32_t>(cnt));
     EDFMM_LAUNCH_CHECK("k_extreme_flags");
     if ((rc = scan_exclusive(dptr<int32_t>(cnt), dptr<int32_t>(ext.off), M, dptr<int64_t>(total), tmp.p, s))) return rc;
     k_set_last<<<1, 1, 0, s>>>(dptr<int32_t>(ext.off), M, dptr<int64_t>(total));
@@ -1134,8 +1141,8 @@ int build_extreme(const DevTree &tree, const int32_t *off, const int32_t *src, E
     if ((rc = ext.src.reserve(sizeof(int32_t) * n_ext)) || (rc = flag.reserve(sizeof(int32_t) * M)) ||
         (rc = pos.reserve(sizeof(int32_t) * M)) || (rc = ext.rows.reserve(sizeof(int32_t) * M)))
         return rc;
-    k_extreme_fill<<<nblk(M, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<int32_t>(ext.off),
-                                                 dptr<int32_t>(ext.src));
+    k_extreme_fill<<<nblk(M, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<float4>(stree.half),
+                                                 dptr<int32_t>(ext.off), dptr<int32_t>(ext.src));
     EDFMM_LAUNCH_CHECK("k_extreme_fill");
     k_flag_nonzero<<<nblk(M, 256), 256, 0, s>>>(M, dptr<int32_t>(cnt), dptr<int32_t>(flag));
     EDFMM_LAUNCH_CHECK("k_flag_nonzero");
@@ -1150,30 +1157,31 @@ int build_extreme(const DevTree &tree, const int32_t *off, const int32_t *src, E
 }
 
 template <int P>
-void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const float4 *cen,
-                     const float4 *hal, const float2 *Mx, float2 *Lx, int nc_pad, cudaStream_t s) {
-    static const bool three = [] {
-        const char *v = getenv("EDFMM_M2L_SETS");
-        return v && v[0] == '3';
-    }();
+void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const float4 *tcen,
+                     const float4 *thal, const float4 *cen, const float4 *hal, const float2 *Mx, float2 *Lx, int nc_pad,
+                     cudaStream_t s) {
     if constexpr (m2l_passes<P>() == 1) {
-        k_m2l_fast<P, 0><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
-    } else if (three && P == 8) {
-        k_m2l_fast<P, 31><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast<P, 0><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
+    } else if constexpr (P == 8) {
+        // three passes of ~15 output coefficients, capped at 168 registers:
+        // 12 warps/SM instead of 8 (measured 3% faster than two passes on
+        // the uniform cube, 8% on a surface)
+        k_m2l_fast<P, 31><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
         count_launch();
-        k_m2l_fast<P, 32><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast<P, 32><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
         count_launch();
-        k_m2l_fast<P, 33><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast<P, 33><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
     } else {
-        k_m2l_fast<P, 1><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast<P, 1><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
         count_launch();
-        k_m2l_fast<P, 2><<<grid, 128, 0, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast<P, 2><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
     }
 }
 
 template <int P>
-int launch_m2l_fast64(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const double4 *cen,
-                      const double4 *hal, const double2 *Mx, double2 *Lx, int nc_pad, cudaStream_t s) {
+int launch_m2l_fast64(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const double4 *tcen,
+                      const double4 *thal, const double4 *cen, const double4 *hal, const double2 *Mx, double2 *Lx,
+                      int nc_pad, cudaStream_t s) {
     constexpr size_t smem = m2l64_smem_bytes<P>();
     static const cudaError_t attr = [] {
         cudaError_t e = cudaSuccess;
@@ -1189,54 +1197,60 @@ int launch_m2l_fast64(unsigned grid, int64_t M, const int32_t *off, const int32_
     if (attr != cudaSuccess)
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_fast64 shared memory attribute: ") + cudaGetErrorString(attr));
     if constexpr (m2l_passes<P>() == 1) {
-        k_m2l_fast64<P, 0><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast64<P, 0><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
     } else {
-        k_m2l_fast64<P, 1><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast64<P, 1><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
         count_launch();
-        k_m2l_fast64<P, 2><<<grid, 128, smem, s>>>(M, off, src, cen, hal, Mx, Lx, nc_pad);
+        k_m2l_fast64<P, 2><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
     }
     EDFMM_LAUNCH_CHECK("k_m2l_fast64");
     return EDFMM_OK;
 }
 
+// M2L from the source tree's multipoles (sbuf) into the target tree's locals
+// (tbuf); for one tree, tree == stree and sbuf == tbuf.
 template <typename T>
-int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s) {
+int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, const FmmBuffers &sbuf,
+             FmmBuffers &buf, bool swapped, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
     const int64_t M = tree.n_nodes;
-    if (M == 0) return EDFMM_OK;
+    if (M == 0 || stree.n_nodes == 0) return EDFMM_OK;
     const int32_t *off = swapped ? dptr<int32_t>(lists.m2l_swapped_off) : dptr<int32_t>(lists.m2l_off);
     const int32_t *src = swapped ? dptr<int32_t>(lists.m2l_swapped_src) : dptr<int32_t>(lists.m2l_src);
     if (sizeof(T) == 8 && buf.p <= 8) {
         // every pair: FP64 has the range for any scale ratio the tree produces
         const unsigned grid = nblk(M * 32, 128);
-        const double4 *cen = dptr<double4>(tree.center), *hal = dptr<double4>(tree.half);
-        const double2 *Mx = dptr<double2>(buf.multipoles);
+        const double4 *tc = dptr<double4>(tree.center), *th = dptr<double4>(tree.half);
+        const double4 *cen = dptr<double4>(stree.center), *hal = dptr<double4>(stree.half);
+        const double2 *Mx = dptr<double2>(sbuf.multipoles);
         double2 *Lx = dptr<double2>(buf.locals);
         switch (buf.p) {
-            case 1: return launch_m2l_fast64<1>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 2: return launch_m2l_fast64<2>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 3: return launch_m2l_fast64<3>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 4: return launch_m2l_fast64<4>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 5: return launch_m2l_fast64<5>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 6: return launch_m2l_fast64<6>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 7: return launch_m2l_fast64<7>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
-            default: return launch_m2l_fast64<8>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 1: return launch_m2l_fast64<1>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 2: return launch_m2l_fast64<2>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 3: return launch_m2l_fast64<3>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 4: return launch_m2l_fast64<4>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 5: return launch_m2l_fast64<5>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 6: return launch_m2l_fast64<6>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            case 7: return launch_m2l_fast64<7>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
+            default: return launch_m2l_fast64<8>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
         }
     }
     if (sizeof(T) == 8) {
         k_m2l_generic<T><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, dptr<T4>(tree.center), dptr<T4>(tree.half),
-                                                    dptr<Cplx<T>>(buf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p,
+                                                    dptr<T4>(stree.center), dptr<T4>(stree.half),
+                                                    dptr<Cplx<T>>(sbuf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p,
                                                     buf.nc_pad, 0);
         EDFMM_LAUNCH_CHECK("k_m2l_generic");
         return EDFMM_OK;
     }
     const unsigned grid = nblk(M * 32, 128);
-    const float4 *cen = dptr<float4>(tree.center), *hal = dptr<float4>(tree.half);
-    const float2 *Mx = dptr<float2>(buf.multipoles);
+    const float4 *tc = dptr<float4>(tree.center), *th = dptr<float4>(tree.half);
+    const float4 *cen = dptr<float4>(stree.center), *hal = dptr<float4>(stree.half);
+    const float2 *Mx = dptr<float2>(sbuf.multipoles);
     float2 *Lx = dptr<float2>(buf.locals);
-#define EDFMM_M2L_CASE(PP)                                                          \
-    case PP:                                                                        \
-        launch_m2l_fast<PP>(grid, M, off, src, cen, hal, Mx, Lx, buf.nc_pad, s);    \
+#define EDFMM_M2L_CASE(PP)                                                                   \
+    case PP:                                                                                 \
+        launch_m2l_fast<PP>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);     \
         break;
     switch (buf.p) {
         EDFMM_M2L_CASE(1)
@@ -1249,7 +1263,8 @@ int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool s
         EDFMM_M2L_CASE(8)
         default:
             // orders above 8 would not fit the register-resident formulation
-            k_m2l_generic<float><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, cen, hal, dptr<Cplx<float>>(buf.multipoles),
+            k_m2l_generic<float><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, tc, th, cen, hal,
+                                                            dptr<Cplx<float>>(sbuf.multipoles),
                                                             dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 0);
             EDFMM_LAUNCH_CHECK("k_m2l_generic");
             return EDFMM_OK;
@@ -1258,13 +1273,13 @@ int m2l_impl(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool s
     EDFMM_LAUNCH_CHECK("k_m2l_fast");
     ExtremeRows &ext = swapped ? buf.extreme_swapped : buf.extreme;
     if (!ext.built) {
-        int rc = build_extreme(tree, off, src, ext, s);
+        int rc = build_extreme(tree, stree, off, src, ext, s);
         if (rc) return rc;
     }
     if (ext.n_pairs > 0) {
         k_m2l_generic<float><<<nblk(ext.n_rows, 4), 128, 0, s>>>(
-            ext.n_rows, dptr<int32_t>(ext.rows), dptr<int32_t>(ext.off), dptr<int32_t>(ext.src), cen, hal,
-            dptr<Cplx<float>>(buf.multipoles), dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 1);
+            ext.n_rows, dptr<int32_t>(ext.rows), dptr<int32_t>(ext.off), dptr<int32_t>(ext.src), tc, th, cen, hal,
+            dptr<Cplx<float>>(sbuf.multipoles), dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 1);
         EDFMM_LAUNCH_CHECK("k_m2l_generic");
     }
     return EDFMM_OK;
@@ -1293,8 +1308,13 @@ int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     return tree.dtype == EDFMM_F64 ? m2m_impl<double>(tree, buf, s) : m2m_impl<float>(tree, buf, s);
 }
 int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s) {
-    return tree.dtype == EDFMM_F64 ? m2l_impl<double>(tree, lists, buf, swapped, s)
-                                   : m2l_impl<float>(tree, lists, buf, swapped, s);
+    return tree.dtype == EDFMM_F64 ? m2l_impl<double>(tree, tree, lists, buf, buf, swapped, s)
+                                   : m2l_impl<float>(tree, tree, lists, buf, buf, swapped, s);
+}
+int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
+                FmmBuffers &tgt_buf, cudaStream_t s) {
+    return tgt_tree.dtype == EDFMM_F64 ? m2l_impl<double>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s)
+                                       : m2l_impl<float>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s);
 }
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     return tree.dtype == EDFMM_F64 ? l2l_impl<double>(tree, buf, s) : l2l_impl<float>(tree, buf, s);

@@ -35,13 +35,17 @@ __device__ __forceinline__ double rn_sqrt(double a) { return __dsqrt_rn(a); }
 
 enum : uint8_t { kM2L = 0, kP2P = 1, kRefineSrc = 2, kRefineTgt = 3 };
 
+// s indexes the source tree (sc, sleaf, srange), t the target tree; `same`
+// marks the single-tree case, where a node is never paired with itself by M2L.
 template <typename T>
-__device__ __forceinline__ uint8_t classify(int s, int t, const typename Vec4<T>::type *__restrict__ center,
-                                            const uint8_t *__restrict__ is_leaf, const int2 *__restrict__ range,
-                                            double theta) {
-    typename Vec4<T>::type cs = center[s], ct = center[t];
+__device__ __forceinline__ uint8_t classify(int s, int t, const typename Vec4<T>::type *__restrict__ sc,
+                                            const uint8_t *__restrict__ sleaf, const int2 *__restrict__ srange,
+                                            const typename Vec4<T>::type *__restrict__ tc,
+                                            const uint8_t *__restrict__ tleaf, const int2 *__restrict__ trange,
+                                            int same, double theta) {
+    typename Vec4<T>::type cs = sc[s], ct = tc[t];
     double ds = (double)rn_mul((T)2, cs.w), dt = (double)rn_mul((T)2, ct.w);
-    if (s != t) {
+    if (!(same && s == t)) {
         T dx = rn_sub(cs.x, ct.x), dy = rn_sub(cs.y, ct.y), dz = rn_sub(cs.z, ct.z);
         double dist = (double)rn_sqrt(rn_fma(dz, dz, rn_fma(dy, dy, rn_mul(dx, dx))));
         if (dist != 0.0) {
@@ -49,15 +53,23 @@ __device__ __forceinline__ uint8_t classify(int s, int t, const typename Vec4<T>
             if (__ddiv_rn(mx, dist) < theta) return kM2L;
         }
     }
-    bool sl = is_leaf[s], tl = is_leaf[t];
+    bool sl = sleaf[s], tl = tleaf[t];
     if (sl && tl) return kP2P;
     if (sl) return kRefineTgt;
     if (tl) return kRefineSrc;
     if (ds > __dmul_rn(dt, 1.01)) return kRefineSrc;
     if (dt > __dmul_rn(ds, 1.01)) return kRefineTgt;
-    int ns = range[s].y - range[s].x, nt = range[t].y - range[t].x;
+    int ns = srange[s].y - srange[s].x, nt = trange[t].y - trange[t].x;
     return ns >= nt ? kRefineSrc : kRefineTgt;
 }
+
+// the arrays of one tree that the traversal reads
+template <typename T> struct TravTree {
+    const typename Vec4<T>::type *center;
+    const uint8_t *is_leaf;
+    const int2 *range;
+    const int32_t *children;
+};
 
 __device__ __forceinline__ int n_children(const int32_t *children, int node) {
     int c = 0;
@@ -67,22 +79,21 @@ __device__ __forceinline__ int n_children(const int32_t *children, int node) {
 }
 
 template <typename T>
-__global__ void k_classify(const int2 *__restrict__ front, int64_t nf, const typename Vec4<T>::type *center,
-                           const uint8_t *is_leaf, const int2 *range, const int32_t *children, double theta,
-                           uint8_t *code, int32_t *c_m2l, int32_t *c_p2p, int32_t *c_next) {
+__global__ void k_classify(const int2 *__restrict__ front, int64_t nf, TravTree<T> S, TravTree<T> Tt, int same,
+                           double theta, uint8_t *code, int32_t *c_m2l, int32_t *c_p2p, int32_t *c_next) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
     int2 pr = front[i];
-    uint8_t c = classify<T>(pr.x, pr.y, center, is_leaf, range, theta);
+    uint8_t c = classify<T>(pr.x, pr.y, S.center, S.is_leaf, S.range, Tt.center, Tt.is_leaf, Tt.range, same, theta);
     code[i] = c;
     c_m2l[i] = c == kM2L;
     c_p2p[i] = c == kP2P;
-    c_next[i] = c == kRefineSrc ? n_children(children, pr.x) : (c == kRefineTgt ? n_children(children, pr.y) : 0);
+    c_next[i] = c == kRefineSrc ? n_children(S.children, pr.x) : (c == kRefineTgt ? n_children(Tt.children, pr.y) : 0);
 }
 
-__global__ void k_emit(const int2 *__restrict__ front, int64_t nf, const uint8_t *code, const int32_t *children,
-                       const int32_t *o_m2l, const int32_t *o_p2p, const int32_t *o_next, int2 *m2l, int64_t m2l_base,
-                       int2 *p2p, int64_t p2p_base, int2 *next) {
+__global__ void k_emit(const int2 *__restrict__ front, int64_t nf, const uint8_t *code, const int32_t *s_children,
+                       const int32_t *t_children, const int32_t *o_m2l, const int32_t *o_p2p, const int32_t *o_next,
+                       int2 *m2l, int64_t m2l_base, int2 *p2p, int64_t p2p_base, int2 *next) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
     int2 pr = front[i];
@@ -92,6 +103,7 @@ __global__ void k_emit(const int2 *__restrict__ front, int64_t nf, const uint8_t
     } else if (c == kP2P) {
         p2p[p2p_base + o_p2p[i]] = pr;
     } else {
+        const int32_t *children = c == kRefineSrc ? s_children : t_children;
         int node = c == kRefineSrc ? pr.x : pr.y;
         int j = o_next[i];
         for (int o = 0; o < 8; ++o) {
@@ -126,12 +138,13 @@ __global__ void k_max_count(const int32_t *cnt, int64_t rows, int *mx) {
     if ((threadIdx.x & 31) == 0) atomicMax(mx, v);
 }
 // sum over P2P pairs of n_s * n_t
-__global__ void k_interactions(const int2 *pairs, int64_t np, const int2 *range, unsigned long long *acc) {
+__global__ void k_interactions(const int2 *pairs, int64_t np, const int2 *srange, const int2 *trange,
+                               unsigned long long *acc) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long v = 0;
     if (i < np) {
         int2 p = pairs[i];
-        v = (unsigned long long)(range[p.x].y - range[p.x].x) * (unsigned long long)(range[p.y].y - range[p.y].x);
+        v = (unsigned long long)(srange[p.x].y - srange[p.x].x) * (unsigned long long)(trange[p.y].y - trange[p.y].x);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -196,12 +209,18 @@ int build_csr(const int2 *pairs, int64_t np, int64_t rows, int key_x, DevBuf &of
     return sort_csr_rows(dptr<int32_t>(off), dptr<int32_t>(vals), rows, max_row, s);
 }
 
-template <typename T> int lists_impl(const DevTree &tree, double theta, DevLists &L, cudaStream_t s) {
+template <typename T>
+int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists &L, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
     int rc;
-    const int64_t M = tree.n_nodes;
+    const int64_t M = tree.n_nodes;  // rows: target-tree nodes
+    const int same = &stree == &tree ? 1 : 0;
+    const TravTree<T> S{dptr<T4>(stree.center), dptr<uint8_t>(stree.is_leaf), dptr<int2>(stree.range),
+                        dptr<int32_t>(stree.children)};
+    const TravTree<T> Tt{dptr<T4>(tree.center), dptr<uint8_t>(tree.is_leaf), dptr<int2>(tree.range),
+                         dptr<int32_t>(tree.children)};
     L = DevLists();
-    if (M == 0) {
+    if (M == 0 || stree.n_nodes == 0) {
         if ((rc = L.p2p_off.reserve(sizeof(int32_t))) || (rc = L.m2l_off.reserve(sizeof(int32_t))) ||
             (rc = L.p2p_src.reserve(4)) || (rc = L.m2l_src.reserve(4)))
             return rc;
@@ -220,9 +239,8 @@ template <typename T> int lists_impl(const DevTree &tree, double theta, DevLists
             (rc = om.reserve(4 * nf)) || (rc = op.reserve(4 * nf)) || (rc = on.reserve(4 * nf)) ||
             (rc = tmp.reserve(scan_tmp_bytes(nf))))
             return rc;
-        k_classify<T><<<nblk(nf, 256), 256, 0, s>>>(dptr<int2>(front), nf, dptr<T4>(tree.center), dptr<uint8_t>(tree.is_leaf),
-                                                     dptr<int2>(tree.range), dptr<int32_t>(tree.children), theta,
-                                                     dptr<uint8_t>(code), dptr<int32_t>(cm), dptr<int32_t>(cp), dptr<int32_t>(cn));
+        k_classify<T><<<nblk(nf, 256), 256, 0, s>>>(dptr<int2>(front), nf, S, Tt, same, theta, dptr<uint8_t>(code),
+                                                     dptr<int32_t>(cm), dptr<int32_t>(cp), dptr<int32_t>(cn));
         EDFMM_LAUNCH_CHECK("k_classify");
         int64_t *t3 = dptr<int64_t>(tot);
         if ((rc = scan_exclusive(dptr<int32_t>(cm), dptr<int32_t>(om), nf, t3, tmp.p, s)) ||
@@ -237,7 +255,7 @@ template <typename T> int lists_impl(const DevTree &tree, double theta, DevLists
         if ((rc = m2l.ensure(m2l.n + h[0], s)) || (rc = p2p.ensure(p2p.n + h[1], s)) ||
             (rc = next.reserve(sizeof(int2) * std::max<int64_t>(h[2], 1))))
             return rc;
-        k_emit<<<nblk(nf, 256), 256, 0, s>>>(dptr<int2>(front), nf, dptr<uint8_t>(code), dptr<int32_t>(tree.children),
+        k_emit<<<nblk(nf, 256), 256, 0, s>>>(dptr<int2>(front), nf, dptr<uint8_t>(code), S.children, Tt.children,
                                               dptr<int32_t>(om), dptr<int32_t>(op), dptr<int32_t>(on), dptr<int2>(m2l.buf),
                                               m2l.n, dptr<int2>(p2p.buf), p2p.n, dptr<int2>(next));
         EDFMM_LAUNCH_CHECK("k_emit");
@@ -255,8 +273,8 @@ template <typename T> int lists_impl(const DevTree &tree, double theta, DevLists
     if ((rc = acc.reserve(sizeof(unsigned long long)))) return rc;
     EDFMM_CUDA_TRY(cudaMemsetAsync(acc.p, 0, sizeof(unsigned long long), s));
     if (p2p.n > 0) {
-        k_interactions<<<nblk(p2p.n, 256), 256, 0, s>>>(dptr<int2>(p2p.buf), p2p.n, dptr<int2>(tree.range),
-                                                         dptr<unsigned long long>(acc));
+        k_interactions<<<nblk(p2p.n, 256), 256, 0, s>>>(dptr<int2>(p2p.buf), p2p.n, dptr<int2>(stree.range),
+                                                         dptr<int2>(tree.range), dptr<unsigned long long>(acc));
         EDFMM_LAUNCH_CHECK("k_interactions");
     }
     unsigned long long hi = 0;
@@ -269,8 +287,14 @@ template <typename T> int lists_impl(const DevTree &tree, double theta, DevLists
 }  // namespace
 
 int lists_build(const DevTree &tree, double theta, DevLists &lists, cudaStream_t s) {
-    if (tree.dtype == EDFMM_F64) return lists_impl<double>(tree, theta, lists, s);
-    return lists_impl<float>(tree, theta, lists, s);
+    if (tree.dtype == EDFMM_F64) return lists_impl<double>(tree, tree, theta, lists, s);
+    return lists_impl<float>(tree, tree, theta, lists, s);
+}
+
+int lists_build_two(const DevTree &src_tree, const DevTree &tgt_tree, double theta, DevLists &lists, cudaStream_t s) {
+    if (src_tree.dtype != tgt_tree.dtype) return fail(EDFMM_ERR_ARG, "source and target trees differ in dtype");
+    if (src_tree.dtype == EDFMM_F64) return lists_impl<double>(src_tree, tgt_tree, theta, lists, s);
+    return lists_impl<float>(src_tree, tgt_tree, theta, lists, s);
 }
 
 int lists_build_swapped(const DevTree &tree, DevLists &L, cudaStream_t s) {

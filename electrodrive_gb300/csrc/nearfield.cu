@@ -68,8 +68,11 @@ template <typename T> struct NearParams {
     int64_t n_leaves;
     const int32_t *off;
     const int32_t *src;
-    const typename Vec4<T>::type *pts;
-    const int2 *range;
+    const typename Vec4<T>::type *pts;   // targets
+    const int2 *range;                   // target leaves' point ranges
+    const typename Vec4<T>::type *spts;  // sources (== pts for one tree)
+    const int2 *srange;
+    int same;                            // one tree: drop i == j in self pairs
     const typename Vec4<T>::type *center;
     const typename Vec4<T>::type *half;
     const Cplx<T> *Lexp;
@@ -174,26 +177,26 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
         const int e = P.off[t + 1];
         for (int k = P.off[t]; k < e; ++k) {
             const int s = P.src[k];
-            const int2 sr = P.range[s];
+            const int2 sr = P.srange[s];
             for (int sb = sr.x; sb < sr.y; sb += 32) {
                 const int cnt = min(32, sr.y - sb);
                 __syncwarp();
                 if constexpr (sizeof(T) == 4) {
                     float *sx = reinterpret_cast<float *>(sp), *sy = sx + 32, *sz = sx + 64, *sw = sx + 96;
-                    const T4 q = lane < cnt ? P.pts[sb + lane] : T4{0.0f, 0.0f, 0.0f, 0.0f};
+                    const T4 q = lane < cnt ? P.spts[sb + lane] : T4{0.0f, 0.0f, 0.0f, 0.0f};
                     sx[lane] = q.x;
                     sy[lane] = q.y;
                     sz[lane] = q.z;
                     sw[lane] = q.w;
                     __syncwarp();
-                    if (s == t)
+                    if (P.same && s == t)
                         accumulate_pairs<TPL, G, true>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
                     else
                         accumulate_pairs<TPL, G, false>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
                 } else {
-                    if (lane < cnt) sp[lane] = P.pts[sb + lane];
+                    if (lane < cnt) sp[lane] = P.spts[sb + lane];
                     __syncwarp();
-                    if (s == t)
+                    if (P.same && s == t)
                         accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
                     else
                         accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
@@ -285,6 +288,9 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     P.src = dptr<int32_t>(lists.p2p_src);
     P.pts = dptr<T4>(tree.pts);
     P.range = dptr<int2>(tree.range);
+    P.spts = a.src_tree ? dptr<T4>(a.src_tree->pts) : P.pts;
+    P.srange = a.src_tree ? dptr<int2>(a.src_tree->range) : P.range;
+    P.same = a.src_tree ? 0 : 1;
     P.center = dptr<T4>(tree.center);
     P.half = dptr<T4>(tree.half);
     P.Lexp = dptr<Cplx<T>>(buf.locals);

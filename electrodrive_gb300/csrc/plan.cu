@@ -393,4 +393,102 @@ int edfmm_plan_matvec(edfmm_plan *p, const void *sigma, const void *areas, const
     return run_p2p_l2p(p->tree, p->lists, p->fmm, a, s);
 }
 
+struct edfmm_targets {
+    edfmm_plan *plan = nullptr;  // source plan (not owned)
+    DevTree tree;                // tree of the target points
+    DevLists lists;              // rows: target nodes; sources: source-plan nodes
+    FmmBuffers buf;              // target locals
+};
+
+int edfmm_targets_create(edfmm_plan *p, const void *targets_dev, int64_t m, void *stream, edfmm_targets **out) {
+    if (!out) return fail(EDFMM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (int rc = check_plan(p)) return rc;
+    if (m < 0 || (m > 0 && !targets_dev)) return fail(EDFMM_ERR_ARG, "need m >= 0 target points");
+    cudaStream_t s = S(stream);
+    edfmm_targets *t = new edfmm_targets();
+    t->plan = p;
+    int rc = tree_build(targets_dev, m, p->tree.dtype, p->leaf_size, p->max_depth, t->tree, s);
+    if (!rc) rc = lists_build_two(p->tree, t->tree, p->mac_theta, t->lists, s);
+    if (!rc) {
+        t->buf.p = p->fmm.p;
+        t->buf.nc = p->fmm.nc;
+        t->buf.nc_pad = p->fmm.nc_pad;
+        const size_t esz = (p->tree.dtype == EDFMM_F64 ? 16 : 8) * (size_t)t->buf.nc_pad *
+                           (size_t)std::max<int64_t>(t->tree.n_nodes, 1);
+        rc = t->buf.locals.reserve(esz);
+        if (!rc) {
+            cudaError_t e = cudaMemsetAsync(t->buf.locals.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("target set-up: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc) {
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return EDFMM_OK;
+}
+
+int edfmm_targets_destroy(edfmm_targets *t) {
+    delete t;
+    return EDFMM_OK;
+}
+
+int edfmm_targets_info(const edfmm_targets *t, int64_t *n_nodes, int64_t *n_p2p_pairs, int64_t *n_m2l_pairs,
+                       int64_t *p2p_interactions) {
+    if (!t) return fail(EDFMM_ERR_ARG, "targets is NULL");
+    if (n_nodes) *n_nodes = t->tree.n_nodes;
+    if (n_p2p_pairs) *n_p2p_pairs = t->lists.n_p2p;
+    if (n_m2l_pairs) *n_m2l_pairs = t->lists.n_m2l;
+    if (p2p_interactions) *p2p_interactions = t->lists.p2p_interactions;
+    return EDFMM_OK;
+}
+
+int edfmm_targets_export_lists(const edfmm_targets *t, int64_t *p2p_pairs, int64_t *m2l_pairs, void *stream) {
+    if (!t) return fail(EDFMM_ERR_ARG, "targets is NULL");
+    const int64_t M = t->tree.n_nodes;
+    if (M == 0) return EDFMM_OK;
+    dim3 blk(32, 8);
+    if (p2p_pairs && t->lists.n_p2p > 0) {
+        k_export_pairs<<<nblk(M, 8), blk, 0, S(stream)>>>(M, dptr<int32_t>(t->lists.p2p_off),
+                                                           dptr<int32_t>(t->lists.p2p_src), p2p_pairs);
+        EDFMM_LAUNCH_CHECK("k_export_pairs");
+    }
+    if (m2l_pairs && t->lists.n_m2l > 0) {
+        k_export_pairs<<<nblk(M, 8), blk, 0, S(stream)>>>(M, dptr<int32_t>(t->lists.m2l_off),
+                                                           dptr<int32_t>(t->lists.m2l_src), m2l_pairs);
+        EDFMM_LAUNCH_CHECK("k_export_pairs");
+    }
+    return EDFMM_OK;
+}
+
+int edfmm_targets_potential(edfmm_targets *t, const void *sigma, const void *areas, double k_e, void *out, int flags,
+                            void *stream) {
+    if (!t) return fail(EDFMM_ERR_ARG, "targets is NULL");
+    edfmm_plan *p = t->plan;
+    if (int rc = check_plan(p)) return rc;
+    if (t->tree.n_points == 0) return EDFMM_OK;
+    if (!sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "sigma, areas and out must be non-NULL");
+    cudaStream_t s = S(stream);
+    const bool far = (flags & EDFMM_NO_FARFIELD) == 0;
+    const bool near = (flags & EDFMM_NO_NEARFIELD) == 0;
+    int rc;
+    if ((rc = set_charges(p->tree, sigma, areas, s))) return rc;
+    if (far) {
+        if ((rc = run_p2m(p->tree, p->fmm, s)) || (rc = run_m2m(p->tree, p->fmm, s)) ||
+            (rc = run_m2l_two(t->tree, p->tree, t->lists, p->fmm, t->buf, s)) || (rc = run_l2l(t->tree, t->buf, s)))
+            return rc;
+    }
+    NearArgs a;
+    a.k_e = k_e;
+    a.out = out;
+    a.scatter = true;
+    a.near = near;
+    a.far = far;
+    a.src_tree = &p->tree;
+    return run_p2p_l2p(t->tree, t->lists, t->buf, a, s);
+}
+
 }  // extern "C"

@@ -317,6 +317,31 @@ EDFMM_API int64_t edfmm_launch_count(void);
 EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_out);
 
 /*
+ * Potential of a plan's panel charges at arbitrary target points by FMM
+ * (replaces bem_potential_targets, electrodrive/core/bem_kernel.py:233-270,
+ * for large panel and target counts).  edfmm_targets_create builds a tree of
+ * the targets (the plan's leaf size and depth) and the interaction lists
+ * between the plan's tree and it, as the reference's
+ * build_interaction_lists(source_tree, target_tree) does
+ * (electrodrive/fmm3d/interaction_lists.py:374-577).
+ * edfmm_targets_potential writes out[i] = k_e * sum_j sigma_j A_j / |x_i - c_j|
+ * (FMM, p of the plan; distances clamped at the dtype's epsilon) in the
+ * targets' original order.  The targets object keeps a pointer to the plan,
+ * which must outlive it.  The electric field is not provided.
+ */
+typedef struct edfmm_targets edfmm_targets;
+EDFMM_API int edfmm_targets_create(edfmm_plan *plan, const void *targets_dev, int64_t m, void *stream,
+                                   edfmm_targets **targets_out);
+EDFMM_API int edfmm_targets_destroy(edfmm_targets *targets);
+EDFMM_API int edfmm_targets_info(const edfmm_targets *targets, int64_t *n_nodes, int64_t *n_p2p_pairs,
+                                 int64_t *n_m2l_pairs, int64_t *p2p_interactions);
+/* (src, tgt) node pairs, sorted by (tgt, src), as edfmm_plan_export_lists */
+EDFMM_API int edfmm_targets_export_lists(const edfmm_targets *targets, int64_t *p2p_pairs_dev, int64_t *m2l_pairs_dev,
+                                         void *stream);
+EDFMM_API int edfmm_targets_potential(edfmm_targets *targets, const void *sigma_dev, const void *areas_dev, double k_e,
+                                      void *out_dev, int flags, void *stream);
+
+/*
  * Point-cloud warm-start network (no counterpart in the reference: it maps
  * per-panel features to an initial surface charge density for the GMRES
  * start).  Width 128, 16 input features (8 used), BF16 weights/activations on

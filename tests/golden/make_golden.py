@@ -287,8 +287,35 @@ def save_icosphere_solve():
     print(f"icosphere solve: iters={info['iters']} code={info['code']} setup {t1 - t0:.1f}s solve {t2 - t1:.1f}s")
 
 
+def save_targets_cases():
+    """electrodrive/fmm3d/interaction_lists.py:531 build_interaction_lists
+    between a source tree and a separate target tree."""
+    out = {}
+    cases = {
+        "shifted_f32": ("uniform", 2000, 21, "uniform", 900, 22, torch.float32, 32, 0.5, 0.6),
+        "sphere_in_cube_f64": ("sphere", 1500, 23, "uniform", 700, 24, torch.float64, 24, 0.5, -0.5),
+    }
+    for name, (ks, ns, ss, kt, nt, st, dtype, leaf, theta, shift) in cases.items():
+        src = gen_points(ks, ns, ss, dtype)
+        tgt = gen_points(kt, nt, st, dtype) * 2.0 + shift
+        tgt = tgt.to(dtype)
+        stree = build_fmm_tree(src, leaf_size=leaf)
+        ttree = build_fmm_tree(tgt, leaf_size=leaf)
+        lists = build_interaction_lists(stree, ttree, mac_theta=theta)
+        out[f"{name}__sources"] = src.numpy()
+        out[f"{name}__targets"] = tgt.numpy()
+        out[f"{name}__meta"] = np.array([leaf, theta])
+        out[f"{name}__p2p_pairs"] = np.asarray(lists.p2p_pairs, dtype=np.int32).reshape(-1, 2)
+        out[f"{name}__m2l_pairs"] = np.asarray(lists.m2l_pairs, dtype=np.int32).reshape(-1, 2)
+        out[f"{name}__target_index_map"] = ttree.index_map.numpy().astype(np.int32)
+        print(f"targets {name}: p2p={len(lists.p2p_pairs)} m2l={len(lists.m2l_pairs)}")
+    np.savez_compressed(os.path.join(HERE, "targets_cases.npz"), **out)
+
+
 def main():
-    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets"]
+    if "targets" in which:
+        save_targets_cases()
     if "near" in which:
         save_near_cases()
     if "solve" in which:
