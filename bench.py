@@ -33,15 +33,18 @@ sys.path.insert(0, ROOT)
 METRIC = "BEM solves/s to 1e-6 residual, mixed+learned vs plain FP64 GMRES; FMM Mpts/s"
 N_DEFAULT = 1 << 20
 WORKLOAD = "fmm_matvec_uniform_unit_cube_N1048576_p8_leaf64_theta0.5_fp32"
-# algorithmic FP32 flops of one M2L pair at p = 8 in the azimuth-factored
-# form the kernel evaluates: 45 x 81 real-by-complex multiply-adds (4 flops),
-# two azimuthal rotations of 45 coefficients (complex multiply, 8 flops
-# each) and 153 real harmonics by a 3-term recurrence (6 flops each)
-M2L_FLOPS_PER_PAIR = 4 * 45 * 81 + 2 * 8 * 45 + 6 * 153
-# DRAM bytes one M2L pass moves per pair (ncu --set full of k_m2l_fast<8, SET>
-# at N = 262,144: 44.6 MB for 9,091,877 pairs; traffic grows with the pair
-# count, so it is scaled to the benchmark's pair count)
-M2L_DRAM_BYTES_PER_PAIR_PER_PASS = 44.6e6 / 9_091_877
+# algorithmic FP32 flops of one M2L pair at p = 8 in the rotation-based form
+# the kernel evaluates (k_m2l_rot): 4 fixed quarter-turn matrices with 988
+# non-zeros in all (2 flops each), 4 azimuthal phase rotations of 36
+# coefficient pairs (6 flops each), the axial translation (81 real + 204
+# complex terms: 978 flops), scaling, phase and 1/rho powers (217 flops) and
+# the accumulation (81)
+M2L_FLOPS_PER_PAIR = 2 * 988 + 4 * 36 * 6 + 978 + 89 + 96 + 32 + 81
+# DRAM bytes one M2L launch moves per pair: the source index (4 B) and one read
+# of the source's multipole row (the rows stay in L2 across a target's pairs);
+# taken from an ncu capture of the earlier contraction kernel at N = 262,144
+# (44.6 MB per pass for 9,091,877 pairs), which reads the same data
+M2L_DRAM_BYTES_PER_PAIR = 44.6e6 / 9_091_877
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
 # as the reference FLOP model's 20 flops (autotune.py:622-667)
 P2P_FLOPS_PER_INTERACTION = 20
@@ -402,9 +405,9 @@ def run_solve_workload(args, rank, world, local):
         p32.set_charges(sig.float() * sysd["areas"].float())
         m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 2, 5))
         achieved = p32.info.n_m2l_pairs * M2L_FLOPS_PER_PAIR / (m2l_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_m2l_fast (M2L of the FP32 inner operator)", "bound": "fp32", "achieved": achieved,
+        roof = {"kernel": "k_m2l_rot<float, 8> (M2L of the FP32 inner operator)", "bound": "fp32", "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
-                "traffic": 2 * M2L_DRAM_BYTES_PER_PAIR_PER_PASS * p32.info.n_m2l_pairs,
+                "traffic": M2L_DRAM_BYTES_PER_PAIR * p32.info.n_m2l_pairs,
                 "traffic_note": "scaled from an ncu capture of the same kernel at N=262,144 (uniform cube)",
                 "peak_source": "FP32 FMA probe measured in this run (edfmm_measure_fp32_peak)"}
         extra = {"plain_fp64_gmres": {"solves_per_s": 1e3 / t_plain if t_plain else None, "ms": t_plain,
@@ -568,7 +571,7 @@ def run_batch_workload(args, rank, world, local):
     del sys2
     if rank == 0:
         order = tune["expansion_order"]
-        flops_pair = 4 * 45 * 81 + 2 * 8 * 45 + 6 * 153 if order == 8 else None
+        flops_pair = M2L_FLOPS_PER_PAIR if order == 8 else None
         ach = p32.info.n_m2l_pairs * flops_pair / (m2l_ms * 1e-3) / 1e12 if flops_pair else None
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -591,7 +594,7 @@ def run_batch_workload(args, rank, world, local):
                        "ms_per_step": e2e_ms, "includes": "batched set-up from the host meshes (trees, lists, "
                                                            "self integrals, rhs), the solve and the read-back"},
                "gpu_launches": int(launches), "clocks": clk.summary(),
-               "roofline": {"kernel": "k_m2l_fast (M2L of the FP32 inner operator)", "bound": "fp32",
+               "roofline": {"kernel": "k_m2l_rot<float, 8> (M2L of the FP32 inner operator)", "bound": "fp32",
                             "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                             "frac": ach / fp32_peak if ach else None, "traffic": None,
                             "peak_source": "FP32 FMA probe measured in this run"},
@@ -752,10 +755,10 @@ def main():
                     "ms_per_step": e2e_ms},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
-            "roofline": {"kernel": "k_m2l_fast (M2L stage: two passes over split output sets)", "bound": "fp32",
+            "roofline": {"kernel": "k_m2l_rot<float, 8> (rotation-based M2L stage)", "bound": "fp32",
                          "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None,
-                         "traffic": 2 * M2L_DRAM_BYTES_PER_PAIR_PER_PASS * info.n_m2l_pairs,
+                         "traffic": M2L_DRAM_BYTES_PER_PAIR * info.n_m2l_pairs,
                          "traffic_note": "DRAM bytes of the M2L stage, scaled from an ncu capture at N=262,144",
                          "peak_source": "FP32 FMA probe measured in this run (edfmm_measure_fp32_peak)",
                          "flops_per_pair": M2L_FLOPS_PER_PAIR},

@@ -183,6 +183,10 @@ int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaS
 int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s);
+// rotation-based M2L (m2l_rot.cu), orders 1..8, FP32 and FP64
+int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
+                   const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
+                   cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
                 FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);

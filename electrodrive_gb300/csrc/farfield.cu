@@ -30,6 +30,7 @@ namespace edfmm {
 namespace {
 
 constexpr float kExtremeRatio = 256.0f;
+constexpr int kRotPMaxUsed = 8;  // rotation-based M2L (m2l_rot.cu) for p <= 8
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -158,46 +159,8 @@ __global__ void __launch_bounds__(128) k_m2m(const int32_t *__restrict__ nodes, 
 }
 
 // ---------------------------------------------------------------------------
-// M2L fast path (FP32, compile-time order)
+// packed FP32 pair helpers (FFMA2: the re and im halves in one instruction)
 // ---------------------------------------------------------------------------
-// Output split for the register budget: at high order the 45 accumulators,
-// the 45 source coefficients and one harmonics column do not fit in 255
-// registers together, so the target coefficients are divided by m-column
-// into sets of nearly equal work (greedy on the per-column cost P+1-m) and
-// each set is computed by its own pass.  SET 0 = all columns; SET 1, 2 = the
-// two-way split; SET 10 k + j = part j (1-based) of a k-way split.
-template <int P> __host__ __device__ constexpr bool m_in_set(int m, int set) {
-    if (set == 0) return true;
-    const int ns = set >= 10 ? set / 10 : 2;
-    const int which = set >= 10 ? set % 10 : set;
-    int load[4] = {0, 0, 0, 0};
-    int bin = 0;
-    for (int mm = 0; mm <= P; ++mm) {
-        int b = 0;
-        for (int k = 1; k < ns; ++k)
-            if (load[k] < load[b]) b = k;
-        load[b] += P + 1 - mm;
-        if (mm == m) bin = b;
-    }
-    return bin + 1 == which;
-}
-template <int P> constexpr int m2l_passes() { return P >= 7 ? 2 : 1; }
-
-// The fast M2L factors the azimuth out of the translation.  With
-// v = (c_L - c_M) / a_L = (s cos phi, s sin phi, z) and the irregular
-// harmonics R_j^mu := I_j^mu(s, 0, z) (real: the recurrence with y = 0),
-//   I_j^mu(v) = e^{i mu phi} R_j^mu,   R_j^{-mu} = (-1)^mu R_j^mu,
-// so, with the source rotated, Mt_k^l = Mhat_k^l (a_M/a_L)^k e^{i l phi},
-//   S_n^m = sum_{k,l} Mt_k^l R_{n+k}^{l-m}   (real coefficients)
-//   A_n^m += e^{-i m phi} S_n^m,   Lhat_n^m = (-1)^(n+m) A_n^m / a_L.
-// Each term is a real x complex multiply-add, issued as one packed FP32 pair
-// FMA (FFMA2: the re and im halves in one instruction), against 4 FMAs for
-// the unfactored complex contraction.  The harmonic R_j^mu is broadcast to
-// both halves; the sign patterns a term can carry ((-1)^mu, and the
-// conjugate of a negative-order source coefficient) become the pairs (c,c),
-// (-c,-c), (c,-c), (-c,c), formed once per degree.  Columns mu and degrees j
-// are visited by template recursion (constant register indices) and only
-// one degree's pairs are live at a time.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 // (sr, si) += (xr, xi) * c as one packed FMA on coefficients held in separate
 // re / im register arrays.
@@ -205,185 +168,6 @@ __device__ __forceinline__ void fma2_into(float &sr, float &si, float xr, float 
     const float2 r = __ffma2_rn(f2(xr, xi), c, f2(sr, si));
     sr = r.x;
     si = r.y;
-}
-
-// one degree j of column mu: R_j^mu by the recurrence, then every term with
-// n + k = j (template recursion over j keeps all register indices constant)
-template <int P, int SET, int MU, int J>
-__device__ __forceinline__ void m2l_degree(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float z,
-                                            float ir2, float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
-                                            float (&Si)[ncoef(P)]) {
-    float c;
-    if constexpr (J == MU) {
-        c = diag;
-    } else if constexpr (J == MU + 1) {
-        c = ((float)(2 * J - 1) * z * ir2) * cm1;
-    } else {
-        constexpr float b = (float)((J - 1 + MU) * (J - 1 - MU));
-        c = ((float)(2 * J - 1) * z * cm1 - b * cm2) * ir2;
-    }
-    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
-#pragma unroll
-    for (int n = 0; n <= P; ++n) {
-        const int k = J - n;
-        if (k < 0 || k > P) continue;
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > n || !m_in_set<P>(m, SET)) continue;
-            {  // l - m = +mu
-                const int l = m + MU;
-                if (l <= P && k >= l) fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, l)], mi[tri(k, l)], cpp);
-            }
-            if (MU > 0) {
-                const int l = m - MU;
-                if (l >= 0) {  // (-1)^mu Mt_k^l R
-                    if (k >= l)
-                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, l)], mi[tri(k, l)], (MU & 1) ? cnn : cpp);
-                } else {  // (-1)^m conj(Mt_k^|l|) R
-                    const int al = -l;
-                    if (al <= P && k >= al)
-                        fma2_into(Sr[tri(n, m)], Si[tri(n, m)], mr[tri(k, al)], mi[tri(k, al)], (m & 1) ? cnp : cpn);
-                }
-            }
-        }
-    }
-    if constexpr (J < 2 * P) m2l_degree<P, SET, MU, J + 1>(mr, mi, z, ir2, diag, c, cm1, Sr, Si);
-}
-
-template <int P, int SET, int MU>
-__device__ __forceinline__ void m2l_column(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float s, float z,
-                                            float ir2, float &diag, float (&Sr)[ncoef(P)], float (&Si)[ncoef(P)]) {
-    if constexpr (MU > 0) diag *= -(float)(2 * MU - 1) * s * ir2;  // R_mu^mu
-    m2l_degree<P, SET, MU, MU>(mr, mi, z, ir2, diag, 0.0f, 0.0f, Sr, Si);
-    if constexpr (MU < 2 * P) m2l_column<P, SET, MU + 1>(mr, mi, s, z, ir2, diag, Sr, Si);
-}
-
-template <int P, int SET>
-__device__ __forceinline__ void m2l_accumulate(const float4 *__restrict__ M4, float c, float vx, float vy, float vz,
-                                                float (&Ar)[ncoef(P)], float (&Ai)[ncoef(P)]) {
-    constexpr int NC = ncoef(P);
-    const float s2 = vx * vx + vy * vy;
-    const float r2 = s2 + vz * vz;
-    const float ir2 = __frcp_rn(r2);
-    const float s = sqrtf(s2);
-    float ec = 1.0f, es = 0.0f;  // e^{i phi}
-    if (s2 > 0.0f) {
-        const float is = 1.0f / s;
-        ec = vx * is;
-        es = vy * is;
-    }
-    float mr[NC], mi[NC];
-#pragma unroll
-    for (int q = 0; q < (NC + 1) / 2; ++q) {
-        const float4 v = __ldg(M4 + q);
-        mr[2 * q] = v.x;
-        mi[2 * q] = v.y;
-        if (2 * q + 1 < NC) {
-            mr[2 * q + 1] = v.z;
-            mi[2 * q + 1] = v.w;
-        }
-    }
-    {
-        float wr = 1.0f, wi = 0.0f;  // e^{i l phi}
-#pragma unroll
-        for (int l = 0; l <= P; ++l) {
-            if (l > 0) {
-                const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
-                wr = nr;
-                wi = ni;
-            }
-            float ck = 1.0f;
-#pragma unroll
-            for (int k = 0; k <= P; ++k) {
-                if (k >= l) {
-                    const float fr = wr * ck, fi = wi * ck;
-                    const float2 x = f2(mr[tri(k, l)], mi[tri(k, l)]);
-                    // (xr fr - xi fi, xi fr + xr fi)
-                    const float2 y = __ffma2_rn(f2(x.y, x.x), f2(-fi, fi), __fmul2_rn(x, f2(fr, fr)));
-                    mr[tri(k, l)] = y.x;
-                    mi[tri(k, l)] = y.y;
-                }
-                ck *= c;
-            }
-        }
-    }
-    float Sr[NC], Si[NC];
-#pragma unroll
-    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
-    float diag = sqrtf(ir2);  // R_0^0 = 1 / |v|
-    m2l_column<P, SET, 0>(mr, mi, s, vz, ir2, diag, Sr, Si);
-    // rotate back: A_n^m += e^{-i m phi} S_n^m = (xr wr + xi wi, xi wr - xr wi)
-    float wr = 1.0f, wi = 0.0f;
-#pragma unroll
-    for (int m = 0; m <= P; ++m) {
-        if (m > 0) {
-            const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
-            wr = nr;
-            wi = ni;
-        }
-        if (!m_in_set<P>(m, SET)) continue;
-#pragma unroll
-        for (int n = 0; n <= P; ++n) {
-            if (n < m) continue;
-            const float2 x = f2(Sr[tri(n, m)], Si[tri(n, m)]);
-            const float2 a = __ffma2_rn(f2(x.y, x.x), f2(wi, -wi), __ffma2_rn(x, f2(wr, wr), f2(Ar[tri(n, m)], Ai[tri(n, m)])));
-            Ar[tri(n, m)] = a.x;
-            Ai[tri(n, m)] = a.y;
-        }
-    }
-}
-
-template <int P, int SET>
-__global__ void __launch_bounds__(128, (SET >= 30 ? 3 : 1)) k_m2l_fast(int64_t n_nodes, const int32_t *__restrict__ off,
-                                                   const int32_t *__restrict__ src, const float4 *__restrict__ tcenter,
-                                                   const float4 *__restrict__ thalf, const float4 *__restrict__ center,
-                                                   const float4 *__restrict__ half, const float2 *__restrict__ Mexp,
-                                                   float2 *__restrict__ Lexp, int nc_pad) {
-    constexpr int NC = ncoef(P);
-    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (t >= n_nodes) return;
-    const float4 ct = tcenter[t];
-    const float aL = thalf[t].w;
-    const float iaL = 1.0f / aL;
-    float Ar[NC], Ai[NC];
-#pragma unroll
-    for (int k = 0; k < NC; ++k) Ar[k] = Ai[k] = 0.0f;
-    const int e = off[t + 1];
-    for (int k = off[t] + lane; k < e; k += 32) {
-        const int s = __ldg(src + k);
-        const float4 cs = __ldg(center + s);
-        const float c = __ldg(&half[s].w) * iaL;
-        if (c > kExtremeRatio) continue;  // translated by k_m2l_generic
-        m2l_accumulate<P, SET>(reinterpret_cast<const float4 *>(Mexp + (int64_t)s * nc_pad), c, (ct.x - cs.x) * iaL,
-                                (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL, Ar, Ai);
-    }
-#pragma unroll
-    for (int n = 0; n <= P; ++n) {
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > n || !m_in_set<P>(m, SET)) continue;
-            const int k = tri(n, m);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                Ar[k] += __shfl_xor_sync(0xffffffffu, Ar[k], o);
-                Ai[k] += __shfl_xor_sync(0xffffffffu, Ai[k], o);
-            }
-        }
-    }
-    float2 *out = Lexp + t * nc_pad;
-#pragma unroll
-    for (int n = 0; n <= P; ++n) {
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > n || !m_in_set<P>(m, SET)) continue;
-            const int k = tri(n, m);
-            if ((k & 31) == lane) {
-                const float sg = ((n + m) & 1) ? -iaL : iaL;
-                out[k] = f2(sg * Ar[k], sg * Ai[k]);
-            }
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -635,195 +419,6 @@ __global__ void __launch_bounds__(128) k_l2l_fast(const int32_t *__restrict__ no
         o4[q] = make_float4(cr[2 * q] + Sr[2 * q], ci[2 * q] + Si[2 * q],
                             2 * q + 1 < NC ? cr[2 * q + 1] + Sr[2 * q + 1] : 0.0f,
                             2 * q + 1 < NC ? ci[2 * q + 1] + Si[2 * q + 1] : 0.0f);
-}
-
-// ---------------------------------------------------------------------------
-// M2L fast path, FP64.  The same azimuth-factored algebra as the FP32 kernel.
-// On this part the FP64 FMA pipe is ~70x slower than the FP32 one, so FP64
-// FMAs are the whole cost and shared-memory traffic is free by comparison:
-// each lane keeps its pair's rotated source coefficients and its target
-// accumulators in its own shared-memory slots ([coef][lane], conflict-free),
-// and only the per-pair accumulators of the pass's output set in registers.
-// ---------------------------------------------------------------------------
-// A shared-memory load the compiler may not hoist or merge: the contraction
-// re-reads each rotated coefficient where it is used instead of keeping all
-// 45 of them live in registers.
-__device__ __forceinline__ double2 lds_f64x2(const double2 *p) {
-    double2 v;
-    asm volatile("ld.volatile.shared.v2.f64 {%0, %1}, [%2];"
-                 : "=d"(v.x), "=d"(v.y)
-                 : "r"((unsigned)__cvta_generic_to_shared(p)));
-    return v;
-}
-
-template <int P, int SET, int MU, int J>
-__device__ __forceinline__ void m2l64_degree(const double2 *__restrict__ sM, double z, double ir2, double diag,
-                                             double cm1, double cm2, double (&Sr)[ncoef(P)], double (&Si)[ncoef(P)]) {
-    double c;
-    if constexpr (J == MU) {
-        c = diag;
-    } else if constexpr (J == MU + 1) {
-        c = ((double)(2 * J - 1) * z * ir2) * cm1;
-    } else {
-        constexpr double b = (double)((J - 1 + MU) * (J - 1 - MU));
-        c = ((double)(2 * J - 1) * z * cm1 - b * cm2) * ir2;
-    }
-#pragma unroll
-    for (int n = 0; n <= P; ++n) {
-        const int k = J - n;
-        if (k < 0 || k > P) continue;
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > n || !m_in_set<P>(m, SET)) continue;
-            {  // l - m = +mu
-                const int l = m + MU;
-                if (l <= P && k >= l) {
-                    const double2 x = lds_f64x2(sM + tri(k, l) * 128);
-                    Sr[tri(n, m)] = fma(x.x, c, Sr[tri(n, m)]);
-                    Si[tri(n, m)] = fma(x.y, c, Si[tri(n, m)]);
-                }
-            }
-            if (MU > 0) {
-                const int l = m - MU;
-                if (l >= 0) {  // (-1)^mu Mt_k^l R
-                    if (k >= l) {
-                        const double2 x = lds_f64x2(sM + tri(k, l) * 128);
-                        const double cs = (MU & 1) ? -c : c;
-                        Sr[tri(n, m)] = fma(x.x, cs, Sr[tri(n, m)]);
-                        Si[tri(n, m)] = fma(x.y, cs, Si[tri(n, m)]);
-                    }
-                } else {  // (-1)^m conj(Mt_k^|l|) R
-                    const int al = -l;
-                    if (al <= P && k >= al) {
-                        const double2 x = lds_f64x2(sM + tri(k, al) * 128);
-                        const double cs = (m & 1) ? -c : c;
-                        Sr[tri(n, m)] = fma(x.x, cs, Sr[tri(n, m)]);
-                        Si[tri(n, m)] = fma(-x.y, cs, Si[tri(n, m)]);
-                    }
-                }
-            }
-        }
-    }
-    if constexpr (J < 2 * P) m2l64_degree<P, SET, MU, J + 1>(sM, z, ir2, diag, c, cm1, Sr, Si);
-}
-
-template <int P, int SET, int MU>
-__device__ __forceinline__ void m2l64_column(const double2 *__restrict__ sM, double s, double z, double ir2,
-                                             double &diag, double (&Sr)[ncoef(P)], double (&Si)[ncoef(P)]) {
-    if constexpr (MU > 0) diag *= -(double)(2 * MU - 1) * s * ir2;  // R_mu^mu
-    m2l64_degree<P, SET, MU, MU>(sM, z, ir2, diag, 0.0, 0.0, Sr, Si);
-    if constexpr (MU < 2 * P) m2l64_column<P, SET, MU + 1>(sM, s, z, ir2, diag, Sr, Si);
-}
-
-template <int P>
-constexpr size_t m2l64_smem_bytes() {
-    return (size_t)2 * ncoef(P) * 128 * sizeof(double2);
-}
-
-template <int P, int SET>
-__global__ void __launch_bounds__(128) k_m2l_fast64(int64_t n_nodes, const int32_t *__restrict__ off,
-                                                    const int32_t *__restrict__ src,
-                                                    const double4 *__restrict__ tcenter,
-                                                    const double4 *__restrict__ thalf,
-                                                    const double4 *__restrict__ center,
-                                                    const double4 *__restrict__ half,
-                                                    const double2 *__restrict__ Mexp, double2 *__restrict__ Lexp,
-                                                    int nc_pad) {
-    constexpr int NC = ncoef(P);
-    extern __shared__ double2 smem64[];
-    double2 *sM = smem64 + threadIdx.x;            // rotated source coefficients, slot stride 128
-    double2 *sA = smem64 + NC * 128 + threadIdx.x;  // target accumulators
-    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (t >= n_nodes) return;
-    const double4 ct = tcenter[t];
-    const double aL = thalf[t].w;
-    const double iaL = 1.0 / aL;
-#pragma unroll
-    for (int q = 0; q < NC; ++q) sA[q * 128] = make_double2(0.0, 0.0);
-    const int e = off[t + 1];
-    for (int k = off[t] + lane; k < e; k += 32) {
-        const int s = __ldg(src + k);
-        const double4 cs = center[s];
-        const double c = half[s].w * iaL;
-        const double vx = (ct.x - cs.x) * iaL, vy = (ct.y - cs.y) * iaL, vz = (ct.z - cs.z) * iaL;
-        const double s2 = vx * vx + vy * vy;
-        const double r2 = s2 + vz * vz;
-        const double ir2 = 1.0 / r2;
-        const double sr = sqrt(s2);
-        double ec = 1.0, es = 0.0;  // e^{i phi}
-        if (s2 > 0.0) {
-            const double is = 1.0 / sr;
-            ec = vx * is;
-            es = vy * is;
-        }
-        const double2 *Mrow = Mexp + (int64_t)s * nc_pad;
-        {
-            double wr = 1.0, wi = 0.0;  // e^{i l phi}
-#pragma unroll
-            for (int l = 0; l <= P; ++l) {
-                if (l > 0) {
-                    const double nr = wr * ec - wi * es, ni = wr * es + wi * ec;
-                    wr = nr;
-                    wi = ni;
-                }
-                double ck = 1.0;
-#pragma unroll
-                for (int kk = 0; kk <= P; ++kk) {
-                    if (kk >= l) {
-                        const double fr = wr * ck, fi = wi * ck;
-                        const double2 x = Mrow[tri(kk, l)];
-                        sM[tri(kk, l) * 128] = make_double2(x.x * fr - x.y * fi, x.x * fi + x.y * fr);
-                    }
-                    ck *= c;
-                }
-            }
-        }
-        double Sr[NC], Si[NC];
-#pragma unroll
-        for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0;
-        double diag = sqrt(ir2);  // R_0^0 = 1 / |v|
-        m2l64_column<P, SET, 0>(sM, sr, vz, ir2, diag, Sr, Si);
-        // rotate back: A_n^m += e^{-i m phi} S_n^m
-        double wr = 1.0, wi = 0.0;
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > 0) {
-                const double nr = wr * ec - wi * es, ni = wr * es + wi * ec;
-                wr = nr;
-                wi = ni;
-            }
-            if (!m_in_set<P>(m, SET)) continue;
-#pragma unroll
-            for (int n = 0; n <= P; ++n) {
-                if (n < m) continue;
-                const double xr = Sr[tri(n, m)], xi = Si[tri(n, m)];
-                double2 a = sA[tri(n, m) * 128];
-                a.x += xr * wr + xi * wi;
-                a.y += xi * wr - xr * wi;
-                sA[tri(n, m) * 128] = a;
-            }
-        }
-    }
-    double2 *out = Lexp + t * nc_pad;
-#pragma unroll
-    for (int n = 0; n <= P; ++n) {
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-            if (m > n || !m_in_set<P>(m, SET)) continue;
-            const int q = tri(n, m);
-            double2 a = sA[q * 128];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-                a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-            }
-            if ((q & 31) == lane) {
-                const double sg = ((n + m) & 1) ? -iaL : iaL;
-                out[q] = make_double2(sg * a.x, sg * a.y);
-            }
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1156,57 +751,6 @@ int build_extreme(const DevTree &tree, const DevTree &stree, const int32_t *off,
     return EDFMM_OK;
 }
 
-template <int P>
-void launch_m2l_fast(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const float4 *tcen,
-                     const float4 *thal, const float4 *cen, const float4 *hal, const float2 *Mx, float2 *Lx, int nc_pad,
-                     cudaStream_t s) {
-    if constexpr (m2l_passes<P>() == 1) {
-        k_m2l_fast<P, 0><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-    } else if constexpr (P == 8) {
-        // three passes of ~15 output coefficients, capped at 168 registers:
-        // 12 warps/SM instead of 8 (measured 3% faster than two passes on
-        // the uniform cube, 8% on a surface)
-        k_m2l_fast<P, 31><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-        count_launch();
-        k_m2l_fast<P, 32><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-        count_launch();
-        k_m2l_fast<P, 33><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-    } else {
-        k_m2l_fast<P, 1><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-        count_launch();
-        k_m2l_fast<P, 2><<<grid, 128, 0, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-    }
-}
-
-template <int P>
-int launch_m2l_fast64(unsigned grid, int64_t M, const int32_t *off, const int32_t *src, const double4 *tcen,
-                      const double4 *thal, const double4 *cen, const double4 *hal, const double2 *Mx, double2 *Lx,
-                      int nc_pad, cudaStream_t s) {
-    constexpr size_t smem = m2l64_smem_bytes<P>();
-    static const cudaError_t attr = [] {
-        cudaError_t e = cudaSuccess;
-        if constexpr (m2l_passes<P>() == 1) {
-            e = cudaFuncSetAttribute(k_m2l_fast64<P, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        } else {
-            e = cudaFuncSetAttribute(k_m2l_fast64<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_m2l_fast64<P, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        }
-        return e;
-    }();
-    if (attr != cudaSuccess)
-        return fail(EDFMM_ERR_CUDA, std::string("k_m2l_fast64 shared memory attribute: ") + cudaGetErrorString(attr));
-    if constexpr (m2l_passes<P>() == 1) {
-        k_m2l_fast64<P, 0><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-    } else {
-        k_m2l_fast64<P, 1><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-        count_launch();
-        k_m2l_fast64<P, 2><<<grid, 128, smem, s>>>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad);
-    }
-    EDFMM_LAUNCH_CHECK("k_m2l_fast64");
-    return EDFMM_OK;
-}
-
 // M2L from the source tree's multipoles (sbuf) into the target tree's locals
 // (tbuf); for one tree, tree == stree and sbuf == tbuf.
 template <typename T>
@@ -1217,25 +761,8 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
     if (M == 0 || stree.n_nodes == 0) return EDFMM_OK;
     const int32_t *off = swapped ? dptr<int32_t>(lists.m2l_swapped_off) : dptr<int32_t>(lists.m2l_off);
     const int32_t *src = swapped ? dptr<int32_t>(lists.m2l_swapped_src) : dptr<int32_t>(lists.m2l_src);
-    if (sizeof(T) == 8 && buf.p <= 8) {
-        // every pair: FP64 has the range for any scale ratio the tree produces
-        const unsigned grid = nblk(M * 32, 128);
-        const double4 *tc = dptr<double4>(tree.center), *th = dptr<double4>(tree.half);
-        const double4 *cen = dptr<double4>(stree.center), *hal = dptr<double4>(stree.half);
-        const double2 *Mx = dptr<double2>(sbuf.multipoles);
-        double2 *Lx = dptr<double2>(buf.locals);
-        switch (buf.p) {
-            case 1: return launch_m2l_fast64<1>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 2: return launch_m2l_fast64<2>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 3: return launch_m2l_fast64<3>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 4: return launch_m2l_fast64<4>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 5: return launch_m2l_fast64<5>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 6: return launch_m2l_fast64<6>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            case 7: return launch_m2l_fast64<7>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-            default: return launch_m2l_fast64<8>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);
-        }
-    }
-    if (sizeof(T) == 8) {
+    if (buf.p > kRotPMaxUsed) {
+        // orders above 8: the shared-memory kernel (scales by the larger radius)
         k_m2l_generic<T><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, dptr<T4>(tree.center), dptr<T4>(tree.half),
                                                     dptr<T4>(stree.center), dptr<T4>(stree.half),
                                                     dptr<Cplx<T>>(sbuf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p,
@@ -1243,34 +770,14 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
         EDFMM_LAUNCH_CHECK("k_m2l_generic");
         return EDFMM_OK;
     }
-    const unsigned grid = nblk(M * 32, 128);
+    if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, tree.center.p,
+                                tree.half.p, stree.center.p, stree.half.p, sbuf.multipoles.p, buf.locals.p,
+                                buf.nc_pad, s))
+        return rc;
+    if (sizeof(T) == 8) return EDFMM_OK;  // FP64 has the range for any scale ratio the tree produces
+    // FP32: pairs whose source scale exceeds 256x the target's, skipped above
     const float4 *tc = dptr<float4>(tree.center), *th = dptr<float4>(tree.half);
     const float4 *cen = dptr<float4>(stree.center), *hal = dptr<float4>(stree.half);
-    const float2 *Mx = dptr<float2>(sbuf.multipoles);
-    float2 *Lx = dptr<float2>(buf.locals);
-#define EDFMM_M2L_CASE(PP)                                                                   \
-    case PP:                                                                                 \
-        launch_m2l_fast<PP>(grid, M, off, src, tc, th, cen, hal, Mx, Lx, buf.nc_pad, s);     \
-        break;
-    switch (buf.p) {
-        EDFMM_M2L_CASE(1)
-        EDFMM_M2L_CASE(2)
-        EDFMM_M2L_CASE(3)
-        EDFMM_M2L_CASE(4)
-        EDFMM_M2L_CASE(5)
-        EDFMM_M2L_CASE(6)
-        EDFMM_M2L_CASE(7)
-        EDFMM_M2L_CASE(8)
-        default:
-            // orders above 8 would not fit the register-resident formulation
-            k_m2l_generic<float><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, tc, th, cen, hal,
-                                                            dptr<Cplx<float>>(sbuf.multipoles),
-                                                            dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 0);
-            EDFMM_LAUNCH_CHECK("k_m2l_generic");
-            return EDFMM_OK;
-    }
-#undef EDFMM_M2L_CASE
-    EDFMM_LAUNCH_CHECK("k_m2l_fast");
     ExtremeRows &ext = swapped ? buf.extreme_swapped : buf.extreme;
     if (!ext.built) {
         int rc = build_extreme(tree, stree, off, src, ext, s);

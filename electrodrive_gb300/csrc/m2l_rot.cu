@@ -1,0 +1,306 @@
+// Rotation-based M2L ("point and shoot").
+//
+// With d = (c_L - c_M) / a_L at polar angle theta and azimuth phi, rotate the
+// frame so that d lies on +z, translate along z, rotate back:
+//   M' = conj T(Q) M,   L' = axial(M', |d|),   L = T(Q)^T L',
+//   Q = R_y(-theta) R_z(-phi),
+// where T(Q) maps the solid harmonics under the rotation,
+// R_n^m(Q v) = sum_m' T^n_{m m'}(Q) R_n^m'(v).  A z rotation is diagonal
+// (e^{i m a}), and a y rotation is R_y(b) = Q_m R_z(b) Q_p with the fixed
+// quarter turns Q_p, Q_m about x.  Their exact matrices (rotation_tables.h,
+// real block basis [Re X0, Re X1, Im X1, ...] per degree, about 25% non-zero)
+// are compile-time constants, so the zero entries cost nothing.  Along z,
+// I_j^mu(0, 0, rho) = delta_mu0 j! / rho^(j+1), so
+//   L'_n^m = (-1)^(n+m) sum_{k >= m} M'_k^m (n+k)! / rho^(n+k+1).
+// Per pair this is about 2,300 multiply-adds at p = 8, against 7,300 for the
+// azimuth-factored contraction.  One lane per (target, source) pair, one
+// warp per target row; each lane accumulates its translated locals in
+// private shared-memory slots, reduced over the warp at the end (fixed order).
+#include "edfmm_internal.cuh"
+#include "harmonics.cuh"
+#include "rotation_tables.h"
+
+namespace edfmm {
+namespace {
+
+constexpr float kRotExtremeRatio = 256.0f;  // FP32: beyond this (a_M/a_L)^k may overflow
+
+template <int TAB> __host__ __device__ constexpr double rot_entry(int i) {
+    return TAB == 0 ? kRotFwdP[i] : TAB == 1 ? kRotFwdM[i] : TAB == 2 ? kRotBwdP[i] : kRotBwdM[i];
+}
+
+// y[I] = sum_J G[I][J] x[J] over the non-zero entries of table TAB, degree block at OFF
+template <typename T, int TAB, int N, int OFF, int I, int J>
+__device__ __forceinline__ void rot_dot(const T (&x)[N], T &acc) {
+    constexpr double g = rot_entry<TAB>(OFF + I * N + J);
+    if constexpr (g != 0.0) acc = fma((T)g, x[J], acc);
+    if constexpr (J + 1 < N) rot_dot<T, TAB, N, OFF, I, J + 1>(x, acc);
+}
+template <typename T, int TAB, int N, int OFF, int I>
+__device__ __forceinline__ void rot_apply(const T (&x)[N], T (&y)[N]) {
+    T acc = T(0);
+    rot_dot<T, TAB, N, OFF, I, 0>(x, acc);
+    y[I] = acc;
+    if constexpr (I + 1 < N) rot_apply<T, TAB, N, OFF, I + 1>(x, y);
+}
+
+// X_m <- X_m e^{i m a} on a degree block: (c[m], s[m]) = (cos m a, sin m a)
+template <typename T, int N, int P>
+__device__ __forceinline__ void zrot(T (&b)[N], const T (&c)[P + 1], const T (&s)[P + 1], T sign) {
+#pragma unroll
+    for (int m = 1; 2 * m < N; ++m) {
+        const T re = b[2 * m - 1], im = b[2 * m], cm = c[m], sm = sign * s[m];
+        b[2 * m - 1] = re * cm - im * sm;
+        b[2 * m] = re * sm + im * cm;
+    }
+}
+
+template <typename T, int P> struct Frame {
+    T cp[P + 1], sp[P + 1];  // cos / sin (m phi)
+    T ct[P + 1], st[P + 1];  // cos / sin (m theta)
+};
+
+template <typename T, int P>
+__device__ __forceinline__ void powers(T c, T s, T (&cm)[P + 1], T (&sm)[P + 1]) {
+    cm[0] = T(1);
+    sm[0] = T(0);
+#pragma unroll
+    for (int m = 1; m <= P; ++m) {
+        cm[m] = cm[m - 1] * c - sm[m - 1] * s;
+        sm[m] = cm[m - 1] * s + sm[m - 1] * c;
+    }
+}
+
+// register store of the (P+1)^2 real coefficients, or private shared-memory slots
+template <typename T, int NV> struct RegV {
+    T v[NV];
+    __device__ __forceinline__ T get(int i) const { return v[i]; }
+    __device__ __forceinline__ void set(int i, T x) { v[i] = x; }
+};
+// Shared-memory loads the compiler may not hoist or merge, so the FP64 kernel
+// re-reads each coefficient where it is used instead of keeping them all in
+// registers (FP64 FMAs are the cost there; shared-memory traffic is free).
+__device__ __forceinline__ float lds_keep(const float *p) {
+    float v;
+    asm volatile("ld.volatile.shared.f32 %0, [%1];" : "=f"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ double lds_keep(const double *p) {
+    double v;
+    asm volatile("ld.volatile.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+template <typename T> struct SmemV {
+    T *base;  // this lane's slot 0; slot i at base[i * 128]
+    __device__ __forceinline__ T get(int i) const { return lds_keep(base + i * 128); }
+    __device__ __forceinline__ void set(int i, T x) { base[i * 128] = x; }
+};
+
+// forward rotation of degree n: scale by f^n, R_z(+phi), Q_p, R_z(+theta), Q_m
+template <typename T, int P, int n, typename V>
+__device__ __forceinline__ void forward(V &v, T f, T fn, const Frame<T, P> &F) {
+    constexpr int N = 2 * n + 1, OV = n * n, OFF = kRotOff[n];
+    T b[N], o[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) b[i] = v.get(OV + i) * fn;
+    zrot<T, N, P>(b, F.cp, F.sp, T(1));
+    rot_apply<T, 0, N, OFF, 0>(b, o);
+    zrot<T, N, P>(o, F.ct, F.st, T(1));
+    rot_apply<T, 1, N, OFF, 0>(o, b);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v.set(OV + i, b[i]);
+    if constexpr (n < P) forward<T, P, n + 1>(v, f, fn * f, F);
+}
+
+// backward rotation of degree n (transposes in reverse order), added to acc
+template <typename T, int P, int n, typename V, typename A>
+__device__ __forceinline__ void backward(V &v, A &acc, const Frame<T, P> &F) {
+    constexpr int N = 2 * n + 1, OV = n * n, OFF = kRotOff[n];
+    T b[N], o[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) b[i] = v.get(OV + i);
+    rot_apply<T, 3, N, OFF, 0>(b, o);
+    zrot<T, N, P>(o, F.ct, F.st, T(-1));
+    rot_apply<T, 2, N, OFF, 0>(o, b);
+    zrot<T, N, P>(b, F.cp, F.sp, T(-1));
+#pragma unroll
+    for (int i = 0; i < N; ++i) acc.set(OV + i, acc.get(OV + i) + b[i]);
+    if constexpr (n < P) backward<T, P, n + 1>(v, acc, F);
+}
+
+// L'_n^m = (-1)^(n+m) sum_{k=m..P} M'_k^m (n+k)! / rho^(n+k+1), in place
+template <typename T, int P, int m, typename V>
+__device__ __forceinline__ void axial(V &v, const T (&f)[2 * P + 1]) {
+    T ur[P + 1], ui[P + 1], wr[P + 1], wi[P + 1];
+#pragma unroll
+    for (int k = m; k <= P; ++k) {
+        ur[k] = v.get(k * k + (m == 0 ? 0 : 2 * m - 1));
+        ui[k] = m == 0 ? T(0) : v.get(k * k + 2 * m);
+    }
+#pragma unroll
+    for (int n = m; n <= P; ++n) {
+        T sr = T(0), si = T(0);
+#pragma unroll
+        for (int k = m; k <= P; ++k) {
+            sr = fma(ur[k], f[n + k], sr);
+            if (m > 0) si = fma(ui[k], f[n + k], si);
+        }
+        wr[n] = ((n + m) & 1) ? -sr : sr;
+        wi[n] = ((n + m) & 1) ? -si : si;
+    }
+#pragma unroll
+    for (int n = m; n <= P; ++n) {
+        v.set(n * n + (m == 0 ? 0 : 2 * m - 1), wr[n]);
+        if (m > 0) v.set(n * n + 2 * m, wi[n]);
+    }
+    if constexpr (m < P) axial<T, P, m + 1>(v, f);
+}
+
+template <typename T> struct Vec2 {};
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
+// One pair: translated locals of source s added to acc.
+template <typename T, int P, typename V, typename A>
+__device__ __forceinline__ void rot_pair(V &v, A &acc, const typename Vec2<T>::type *__restrict__ Mrow, T c, T dx, T dy,
+                                         T dz) {
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= n; ++m) {
+            const typename Vec2<T>::type x = Mrow[tri(n, m)];
+            if (m == 0) {
+                v.set(n * n, x.x);
+            } else {
+                v.set(n * n + 2 * m - 1, x.x);
+                v.set(n * n + 2 * m, x.y);
+            }
+        }
+    }
+    const T s2 = dx * dx + dy * dy, r2 = s2 + dz * dz;
+    const T s = sqrt(s2), rho = sqrt(r2), irho = T(1) / rho;
+    Frame<T, P> F;
+    T cphi = T(1), sphi = T(0);
+    if (s2 > T(0)) {
+        const T is = T(1) / s;
+        cphi = dx * is;
+        sphi = dy * is;
+    }
+    powers<T, P>(cphi, sphi, F.cp, F.sp);
+    powers<T, P>(dz * irho, s * irho, F.ct, F.st);
+    forward<T, P, 0>(v, c, T(1), F);
+    T f[2 * P + 1];
+    f[0] = irho;
+#pragma unroll
+    for (int j = 1; j <= 2 * P; ++j) f[j] = f[j - 1] * (T)j * irho;
+    axial<T, P, 0>(v, f);
+    backward<T, P, 0>(v, acc, F);
+}
+
+template <typename T, int P, bool V_IN_SMEM>
+__global__ void __launch_bounds__(128) k_m2l_rot(int64_t n_nodes, const int32_t *__restrict__ off,
+                                                 const int32_t *__restrict__ src,
+                                                 const typename Vec4<T>::type *__restrict__ tcenter,
+                                                 const typename Vec4<T>::type *__restrict__ thalf,
+                                                 const typename Vec4<T>::type *__restrict__ center,
+                                                 const typename Vec4<T>::type *__restrict__ half,
+                                                 const typename Vec2<T>::type *__restrict__ Mexp,
+                                                 typename Vec2<T>::type *__restrict__ Lexp, int nc_pad) {
+    constexpr int NV = (P + 1) * (P + 1);
+    extern __shared__ __align__(16) unsigned char rot_smem[];
+    T *sh = reinterpret_cast<T *>(rot_smem);
+    SmemV<T> acc{sh + threadIdx.x};
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= n_nodes) return;
+    const typename Vec4<T>::type ct = tcenter[t];
+    const T aL = thalf[t].w, iaL = T(1) / aL;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) acc.set(i, T(0));
+    const int e = off[t + 1];
+    for (int k = off[t] + lane; k < e; k += 32) {
+        const int s = __ldg(src + k);
+        const typename Vec4<T>::type cs = center[s];
+        const T c = half[s].w * iaL;
+        if (sizeof(T) == 4 && c > (T)kRotExtremeRatio) continue;  // translated by k_m2l_generic
+        const typename Vec2<T>::type *Mrow = Mexp + (int64_t)s * nc_pad;
+        if constexpr (V_IN_SMEM) {
+            SmemV<T> v{sh + NV * 128 + threadIdx.x};
+            rot_pair<T, P>(v, acc, Mrow, c, (ct.x - cs.x) * iaL, (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL);
+        } else {
+            RegV<T, NV> v;
+            rot_pair<T, P>(v, acc, Mrow, c, (ct.x - cs.x) * iaL, (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL);
+        }
+    }
+    typename Vec2<T>::type *out = Lexp + t * nc_pad;
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= n; ++m) {
+            T re = acc.get(n * n + (m == 0 ? 0 : 2 * m - 1));
+            T im = m == 0 ? T(0) : acc.get(n * n + 2 * m);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            const int q = tri(n, m);
+            if ((q & 31) == lane) {
+                typename Vec2<T>::type r;
+                r.x = re * iaL;
+                r.y = im * iaL;
+                out[q] = r;
+            }
+        }
+    }
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <typename T, int P, bool V_IN_SMEM>
+int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal, const void *cen,
+               const void *hal, const void *Mx, void *Lx, int nc_pad, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    using T2 = typename Vec2<T>::type;
+    constexpr int NV = (P + 1) * (P + 1);
+    constexpr size_t smem = (size_t)(V_IN_SMEM ? 2 : 1) * NV * 128 * sizeof(T);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_m2l_rot<T, P, V_IN_SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess)
+        return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot shared memory attribute: ") + cudaGetErrorString(attr));
+    k_m2l_rot<T, P, V_IN_SMEM><<<nblk(M * 32, 128), 128, smem, s>>>(
+        M, off, src, static_cast<const T4 *>(tcen), static_cast<const T4 *>(thal), static_cast<const T4 *>(cen),
+        static_cast<const T4 *>(hal), static_cast<const T2 *>(Mx), static_cast<T2 *>(Lx), nc_pad);
+    EDFMM_LAUNCH_CHECK("k_m2l_rot");
+    return EDFMM_OK;
+}
+
+}  // namespace
+
+// Rotation-based M2L for expansion orders 1..8 (FP32: pairs with a source
+// scale above 256x the target's are left to the caller's generic kernel).
+int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
+                   const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
+                   cudaStream_t s) {
+    if (M <= 0) return EDFMM_OK;
+#define EDFMM_ROT_CASE(PP)                                                                                    \
+    case PP:                                                                                                  \
+        return dtype == EDFMM_F64                                                                             \
+                   ? launch_rot<double, PP, true>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, s)       \
+                   : launch_rot<float, PP, false>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, s);
+    switch (p) {
+        EDFMM_ROT_CASE(1)
+        EDFMM_ROT_CASE(2)
+        EDFMM_ROT_CASE(3)
+        EDFMM_ROT_CASE(4)
+        EDFMM_ROT_CASE(5)
+        EDFMM_ROT_CASE(6)
+        EDFMM_ROT_CASE(7)
+        EDFMM_ROT_CASE(8)
+        default:
+            return fail(EDFMM_ERR_UNSUPPORTED, "rotation M2L supports orders 1..8");
+    }
+#undef EDFMM_ROT_CASE
+}
+
+}  // namespace edfmm
