@@ -33,6 +33,13 @@ sys.path.insert(0, ROOT)
 METRIC = "BEM solves/s to 1e-6 residual, mixed+learned vs plain FP64 GMRES; FMM Mpts/s"
 N_DEFAULT = 1 << 20
 WORKLOAD = "fmm_matvec_uniform_unit_cube_N1048576_p8_leaf64_theta0.5_fp32"
+
+
+def fmm_workload(n):
+    """Workload name of the FMM matvec at n points (the default run is N = 1,048,576)."""
+    return WORKLOAD.replace("N1048576", f"N{n}")
+
+
 # algorithmic FP32 flops of one M2L pair at p = 8 in the rotation-based form
 # the kernel evaluates (k_m2l_rot): 4 fixed quarter-turn matrices with 988
 # non-zeros in all (2 flops each), 4 azimuthal phase rotations of 36
@@ -42,9 +49,9 @@ WORKLOAD = "fmm_matvec_uniform_unit_cube_N1048576_p8_leaf64_theta0.5_fp32"
 M2L_FLOPS_PER_PAIR = 2 * 988 + 4 * 36 * 6 + 978 + 89 + 96 + 32 + 81
 # DRAM bytes one M2L launch moves per pair: the source index (4 B) and one read
 # of the source's multipole row (the rows stay in L2 across a target's pairs);
-# taken from an ncu capture of the earlier contraction kernel at N = 262,144
-# (44.6 MB per pass for 9,091,877 pairs), which reads the same data
-M2L_DRAM_BYTES_PER_PAIR = 44.6e6 / 9_091_877
+# taken from an ncu capture of k_m2l_rot<float, 8> at N = 262,144 (44.54 MB read
+# for 9,091,877 pairs)
+M2L_DRAM_BYTES_PER_PAIR = 44.54e6 / 9_091_877
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
 # as the reference FLOP model's 20 flops (autotune.py:622-667)
 P2P_FLOPS_PER_INTERACTION = 20
@@ -746,7 +753,7 @@ def main():
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_points": n, "expansion_order": 8, "leaf_size": 64,
+            "config": {"workload": fmm_workload(n), "n_points": n, "expansion_order": 8, "leaf_size": 64,
                        "mac_theta": 0.5, "n_nodes": info.n_nodes, "n_p2p_pairs": info.n_p2p_pairs,
                        "n_m2l_pairs": info.n_m2l_pairs, "p2p_interactions": info.p2p_interactions,
                        "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
