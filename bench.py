@@ -40,13 +40,24 @@ def fmm_workload(n):
     return WORKLOAD.replace("N1048576", f"N{n}")
 
 
-# algorithmic FP32 flops of one M2L pair at p = 8 in the rotation-based form
-# the kernel evaluates (k_m2l_rot): 4 fixed quarter-turn matrices with 988
-# non-zeros in all (2 flops each), 4 azimuthal phase rotations of 36
-# coefficient pairs (6 flops each), the axial translation (81 real + 204
-# complex terms: 978 flops), scaling, phase and 1/rho powers (217 flops) and
-# the accumulation (81)
-M2L_FLOPS_PER_PAIR = 2 * 988 + 4 * 36 * 6 + 978 + 89 + 96 + 32 + 81
+# non-zeros per degree of each of the four fixed quarter-turn tables
+# (electrodrive_gb300/csrc/rotation_tables.h)
+ROT_NNZ = [1, 3, 7, 13, 21, 31, 43, 57, 71]
+
+
+def m2l_flops_per_pair(p):
+    """Algorithmic flops of one M2L pair at order p in the rotation form the
+    kernel evaluates (k_m2l_rot): the 4 fixed quarter-turn matrices (2 flops per
+    non-zero), 4 azimuthal phase rotations of the m >= 1 coefficient pairs
+    (6 flops each), the axial translation (real m = 0 terms, complex m >= 1
+    terms), the scaling by the radius ratio, the phase and 1/rho powers and the
+    accumulation.  4,116 at p = 8."""
+    axial = 2 * (p + 1) ** 2 + 4 * sum(j * j for j in range(1, p + 1))
+    return (2 * 4 * sum(ROT_NNZ[:p + 1]) + 4 * (p * (p + 1) // 2) * 6 + axial + ((p + 1) ** 2 + p) + 12 * p
+            + 4 * p + (p + 1) ** 2)
+
+
+M2L_FLOPS_PER_PAIR = m2l_flops_per_pair(8)
 # DRAM bytes one M2L launch moves per pair: the source index (4 B) and one read
 # of the source's multipole row (the rows stay in L2 across a target's pairs);
 # taken from an ncu capture of k_m2l_rot<float, 8> at N = 262,144 (44.54 MB read
@@ -399,13 +410,26 @@ def run_solve_workload(args, rank, world, local):
             plain["x"], plain["info"] = gmres_restart(op64, b, restart=256, tol=1e-6 * bn / r0, maxiter=4000,
                                                       precond="jacobi", areas=sysd["areas"], A_diag=diag, x0=x0,
                                                       use_graph=True)
+        # the same plain FP64 GMRES with an early exit (cycles end once the
+        # preconditioned residual meets the tolerance, checked every 8 steps):
+        # the reference's solver always completes a 256-step cycle
+        plain_ee = {}
+
+        def plain_solve_ee():
+            plain_ee["x"], plain_ee["info"] = gmres_restart(op64, b, restart=256, tol=1e-6 * bn / r0, maxiter=4000,
+                                                            precond="jacobi", areas=sysd["areas"], A_diag=diag,
+                                                            x0=x0, use_graph=True, early_exit=8)
         if args.no_plain:  # profiling runs: the mixed solve stands in as the comparison solution
             t_plain, pinfo, plain_rel = None, {"iters": 0, "code": None}, None
+            t_plain_ee, pinfo_ee, plain_ee_rel = None, {"iters": 0, "code": None}, None
             plain["x"] = x.to(torch.float64)
         else:
             t_plain = _time_cuda(plain_solve, dev, stream, flush, 0, 1)[0]
             pinfo = plain["info"]
             plain_rel = float(torch.linalg.norm(b - op64(plain["x"])) / bn)
+            t_plain_ee = _time_cuda(plain_solve_ee, dev, stream, flush, 0, 1)[0]
+            pinfo_ee = plain_ee["info"]
+            plain_ee_rel = float(torch.linalg.norm(b - op64(plain_ee["x"])) / bn)
         p64 = op64.base.plan
         p32 = op32.base.plan
         fp32_peak = _lib.measure_fp32_peak()
@@ -421,6 +445,11 @@ def run_solve_workload(args, rank, world, local):
                                       "iters": pinfo["iters"], "code": pinfo["code"], "true_rel_resid": plain_rel,
                                       "restart": 256},
                  "mixed_speedup_vs_plain_fp64": t_plain / ms if t_plain else None,
+                 "plain_fp64_gmres_early_exit": {"solves_per_s": 1e3 / t_plain_ee if t_plain_ee else None,
+                                                 "ms": t_plain_ee, "iters": pinfo_ee["iters"],
+                                                 "code": pinfo_ee["code"], "true_rel_resid": plain_ee_rel,
+                                                 "restart": 256, "early_exit_every": 8},
+                 "mixed_speedup_vs_plain_fp64_early_exit": t_plain_ee / ms if t_plain_ee else None,
                  "sigma_rel_l2_mixed_vs_plain_fp64": float(torch.linalg.norm(x - plain["x"]) /
                                                            torch.linalg.norm(plain["x"])),
                  "outer_iters": info["outer"], "inner_iters": info["inner_iters"], "fp64_matvecs": info["matvec64"],
@@ -565,8 +594,10 @@ def run_batch_workload(args, rank, world, local):
 
     sub = min(8, K)
     plain = [_plain(*cases[i], device=dev) for i in range(sub)]
+    plain_ee = [_plain(*cases[i], device=dev, early_exit=8) for i in range(sub)]
     n_sub = sum(p["n"] for p in plain)
     t_plain_all = sum(p["seconds"] for p in plain) * n_total / n_sub
+    t_plain_ee_all = sum(p["seconds"] for p in plain_ee) * n_total / n_sub
     # end to end: host meshes -> batched set-up -> solve -> sigma on the host
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -578,7 +609,7 @@ def run_batch_workload(args, rank, world, local):
     del sys2
     if rank == 0:
         order = tune["expansion_order"]
-        flops_pair = M2L_FLOPS_PER_PAIR if order == 8 else None
+        flops_pair = m2l_flops_per_pair(order) if 1 <= order <= 8 else None
         ach = p32.info.n_m2l_pairs * flops_pair / (m2l_ms * 1e-3) / 1e12 if flops_pair else None
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -594,14 +625,22 @@ def run_batch_workload(args, rank, world, local):
                                                      "seconds_timed": sum(p["seconds"] for p in plain),
                                                      "seconds_all_extrapolated_by_panels": t_plain_all,
                                                      "solves_per_s": K / t_plain_all},
-                         "speedup_vs_plain_fp64": t_plain_all / (ms * 1e-3)},
+                         "speedup_vs_plain_fp64": t_plain_all / (ms * 1e-3),
+                         "plain_fp64_early_exit_per_instance": {
+                             "instances_timed": sub, "early_exit_every": 8,
+                             "mean_iters": float(np.mean([p["iters"] for p in plain_ee])),
+                             "max_rel_resid": float(max(p["rel_resid"] for p in plain_ee)),
+                             "seconds_timed": sum(p["seconds"] for p in plain_ee),
+                             "seconds_all_extrapolated_by_panels": t_plain_ee_all,
+                             "solves_per_s": K / t_plain_ee_all},
+                         "speedup_vs_plain_fp64_early_exit": t_plain_ee_all / (ms * 1e-3)},
                "autotune_trials": tune["trials"], "matvec_ms": mv,
                "e2e": {"value": world * K * 1e3 / e2e_ms, "unit": "solves/s",
                        "h2d_bytes_per_step": int(n_total * 8 * (3 + 1 + 9)), "d2h_bytes_per_step": int(8 * n_total),
                        "ms_per_step": e2e_ms, "includes": "batched set-up from the host meshes (trees, lists, "
                                                            "self integrals, rhs), the solve and the read-back"},
                "gpu_launches": int(launches), "clocks": clk.summary(),
-               "roofline": {"kernel": "k_m2l_rot<float, 8> (M2L of the FP32 inner operator)", "bound": "fp32",
+               "roofline": {"kernel": f"k_m2l_rot<float, {order}> (M2L of the FP32 inner operator)", "bound": "fp32",
                             "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                             "frac": ach / fp32_peak if ach else None, "traffic": None,
                             "peak_source": "FP32 FMA probe measured in this run"},

@@ -162,9 +162,12 @@ def autotune_inner(system: BatchSystem, leaf_sizes=(32, 64, 128), orders=(6, 7, 
 
 
 def plain_fp64_solve(mesh: TriMesh, spec: Dict[str, Any], *, rtol: float = 1e-6, restart: int = 256,
-                     device=None) -> Dict[str, Any]:
+                     device=None, early_exit: Optional[int] = None) -> Dict[str, Any]:
     """The plain method on one instance: FP64 FMM operator, Jacobi GMRES from
-    the cold start (b / I_self) to the same relative true residual."""
+    the cold start (b / I_self) to the same relative true residual.  With
+    ``early_exit=c`` a cycle ends once the preconditioned residual meets the
+    tolerance (checked every c steps); without it every cycle runs its full
+    ``restart`` steps, as the reference's solver does."""
     from .bem import assemble_system
     from .bem_solver import gmres_restart
 
@@ -176,7 +179,7 @@ def plain_fp64_solve(mesh: TriMesh, spec: Dict[str, Any], *, rtol: float = 1e-6,
     torch.cuda.synchronize(b.device)
     t0 = time.perf_counter()
     x, info = gmres_restart(op, b, restart=restart, tol=rtol * bn / r0, maxiter=4000, precond="jacobi",
-                            A_diag=sysd["diag"], x0=x0, use_graph=True)
+                            A_diag=sysd["diag"], x0=x0, use_graph=True, early_exit=early_exit)
     torch.cuda.synchronize(b.device)
     dt = time.perf_counter() - t0
     rel = float(torch.linalg.norm(b - op(x))) / bn

@@ -24,6 +24,7 @@ namespace edfmm {
 namespace {
 
 constexpr float kRotExtremeRatio = 256.0f;  // FP32: beyond this (a_M/a_L)^k may overflow
+constexpr int kRotThreads = 128;             // 4 warps; FP32: 3 blocks per SM at <= 168 registers
 
 template <int TAB> __host__ __device__ constexpr double rot_entry(int i) {
     return TAB == 0 ? kRotFwdP[i] : TAB == 1 ? kRotFwdM[i] : TAB == 2 ? kRotBwdP[i] : kRotBwdM[i];
@@ -90,10 +91,41 @@ __device__ __forceinline__ double lds_keep(const double *p) {
     asm volatile("ld.volatile.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
     return v;
 }
-template <typename T> struct SmemV {
-    T *base;  // this lane's slot 0; slot i at base[i * 128]
-    __device__ __forceinline__ T get(int i) const { return lds_keep(base + i * 128); }
-    __device__ __forceinline__ void set(int i, T x) { base[i * 128] = x; }
+template <typename T, int STRIDE> struct SmemV {
+    T *base;  // this lane's slot 0; slot i at base[i * STRIDE]
+    __device__ __forceinline__ T get(int i) const { return lds_keep(base + i * STRIDE); }
+    __device__ __forceinline__ void set(int i, T x) { base[i * STRIDE] = x; }
+};
+
+template <typename T> struct Vec2 {};
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
+__device__ __forceinline__ float2 lds_keep(const float2 *p) {
+    float2 v;
+    asm volatile("ld.volatile.shared.v2.f32 {%0, %1}, [%2];"
+                 : "=f"(v.x), "=f"(v.y)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ double2 lds_keep(const double2 *p) {
+    double2 v;
+    asm volatile("ld.volatile.shared.v2.f64 {%0, %1}, [%2];"
+                 : "=d"(v.x), "=d"(v.y)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// Per-lane accumulator of the translated locals: complex slot tri(n, m) at
+// base[tri(n, m) * STRIDE] (one 8- or 16-byte word per lane, so a warp's
+// access is conflict-free and each coefficient pair is one load and one store).
+template <typename T, int STRIDE> struct AccC {
+    using T2 = typename Vec2<T>::type;
+    T2 *base;
+    __device__ __forceinline__ T2 get(int q) const { return lds_keep(base + q * STRIDE); }
+    __device__ __forceinline__ void set(int q, T2 x) { base[q * STRIDE] = x; }
 };
 
 // forward rotation of degree n: scale by f^n, R_z(+phi), Q_p, R_z(+theta), Q_m
@@ -123,42 +155,65 @@ __device__ __forceinline__ void backward(V &v, A &acc, const Frame<T, P> &F) {
     zrot<T, N, P>(o, F.ct, F.st, T(-1));
     rot_apply<T, 2, N, OFF, 0>(o, b);
     zrot<T, N, P>(b, F.cp, F.sp, T(-1));
+    using T2 = typename Vec2<T>::type;
+    {
+        T2 a = acc.get(tri(n, 0));
+        a.x += b[0];
+        acc.set(tri(n, 0), a);
+    }
 #pragma unroll
-    for (int i = 0; i < N; ++i) acc.set(OV + i, acc.get(OV + i) + b[i]);
+    for (int m = 1; m <= n; ++m) {
+        T2 x;
+        x.x = b[2 * m - 1];
+        x.y = b[2 * m];
+        acc.set(tri(n, m), add2(acc.get(tri(n, m)), x));
+    }
     if constexpr (n < P) backward<T, P, n + 1>(v, acc, F);
 }
 
-// L'_n^m = (-1)^(n+m) sum_{k=m..P} M'_k^m (n+k)! / rho^(n+k+1), in place
+// L'_n^m = (-1)^(n+m) sum_{k=m..P} M'_k^m (n+k)! / rho^(n+k+1), in place.
+// FP32 runs the complex (m >= 1) terms as packed pairs: f2[j] = (f[j], f[j]).
 template <typename T, int P, int m, typename V>
-__device__ __forceinline__ void axial(V &v, const T (&f)[2 * P + 1]) {
-    T ur[P + 1], ui[P + 1], wr[P + 1], wi[P + 1];
+__device__ __forceinline__ void axial(V &v, const T (&f)[2 * P + 1], const float2 (&f2)[2 * P + 1]) {
+    if constexpr (m > 0 && sizeof(T) == 4) {
+        float2 u[P + 1];
 #pragma unroll
-    for (int k = m; k <= P; ++k) {
-        ur[k] = v.get(k * k + (m == 0 ? 0 : 2 * m - 1));
-        ui[k] = m == 0 ? T(0) : v.get(k * k + 2 * m);
-    }
+        for (int k = m; k <= P; ++k) u[k] = make_float2(v.get(k * k + 2 * m - 1), v.get(k * k + 2 * m));
 #pragma unroll
-    for (int n = m; n <= P; ++n) {
-        T sr = T(0), si = T(0);
+        for (int n = m; n <= P; ++n) {
+            float2 sum = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int k = m; k <= P; ++k) sum = __ffma2_rn(u[k], f2[n + k], sum);
+            const float sg = ((n + m) & 1) ? -1.0f : 1.0f;
+            v.set(n * n + 2 * m - 1, sg * sum.x);
+            v.set(n * n + 2 * m, sg * sum.y);
+        }
+    } else {
+        T ur[P + 1], ui[P + 1], wr[P + 1], wi[P + 1];
 #pragma unroll
         for (int k = m; k <= P; ++k) {
-            sr = fma(ur[k], f[n + k], sr);
-            if (m > 0) si = fma(ui[k], f[n + k], si);
+            ur[k] = v.get(k * k + (m == 0 ? 0 : 2 * m - 1));
+            ui[k] = m == 0 ? T(0) : v.get(k * k + 2 * m);
         }
-        wr[n] = ((n + m) & 1) ? -sr : sr;
-        wi[n] = ((n + m) & 1) ? -si : si;
-    }
 #pragma unroll
-    for (int n = m; n <= P; ++n) {
-        v.set(n * n + (m == 0 ? 0 : 2 * m - 1), wr[n]);
-        if (m > 0) v.set(n * n + 2 * m, wi[n]);
+        for (int n = m; n <= P; ++n) {
+            T sr = T(0), si = T(0);
+#pragma unroll
+            for (int k = m; k <= P; ++k) {
+                sr = fma(ur[k], f[n + k], sr);
+                if (m > 0) si = fma(ui[k], f[n + k], si);
+            }
+            wr[n] = ((n + m) & 1) ? -sr : sr;
+            wi[n] = ((n + m) & 1) ? -si : si;
+        }
+#pragma unroll
+        for (int n = m; n <= P; ++n) {
+            v.set(n * n + (m == 0 ? 0 : 2 * m - 1), wr[n]);
+            if (m > 0) v.set(n * n + 2 * m, wi[n]);
+        }
     }
-    if constexpr (m < P) axial<T, P, m + 1>(v, f);
+    if constexpr (m < P) axial<T, P, m + 1>(v, f, f2);
 }
-
-template <typename T> struct Vec2 {};
-template <> struct Vec2<float> { using type = float2; };
-template <> struct Vec2<double> { using type = double2; };
 
 // One pair: translated locals of source s added to acc.
 template <typename T, int P, typename V, typename A>
@@ -193,60 +248,84 @@ __device__ __forceinline__ void rot_pair(V &v, A &acc, const typename Vec2<T>::t
     f[0] = irho;
 #pragma unroll
     for (int j = 1; j <= 2 * P; ++j) f[j] = f[j - 1] * (T)j * irho;
-    axial<T, P, 0>(v, f);
+    float2 f2[2 * P + 1];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int j = 0; j <= 2 * P; ++j) f2[j] = make_float2((float)f[j], (float)f[j]);
+    }
+    axial<T, P, 0>(v, f, f2);
     backward<T, P, 0>(v, acc, F);
 }
 
+// One warp per target row, one lane per (target, source) pair.  The warps of
+// a block run the same number of rounds of pairs, with a barrier between
+// rounds, so that the warps of an SM walk the long straight-line pair code
+// close together and share its instruction fetches.
 template <typename T, int P, bool V_IN_SMEM>
-__global__ void __launch_bounds__(128) k_m2l_rot(int64_t n_nodes, const int32_t *__restrict__ off,
-                                                 const int32_t *__restrict__ src,
-                                                 const typename Vec4<T>::type *__restrict__ tcenter,
-                                                 const typename Vec4<T>::type *__restrict__ thalf,
-                                                 const typename Vec4<T>::type *__restrict__ center,
-                                                 const typename Vec4<T>::type *__restrict__ half,
-                                                 const typename Vec2<T>::type *__restrict__ Mexp,
-                                                 typename Vec2<T>::type *__restrict__ Lexp, int nc_pad) {
-    constexpr int NV = (P + 1) * (P + 1);
+__global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? 3 : 1)
+    k_m2l_rot(int64_t n_nodes, const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+              const typename Vec4<T>::type *__restrict__ tcenter, const typename Vec4<T>::type *__restrict__ thalf,
+              const typename Vec4<T>::type *__restrict__ center, const typename Vec4<T>::type *__restrict__ half,
+              const typename Vec2<T>::type *__restrict__ Mexp, typename Vec2<T>::type *__restrict__ Lexp,
+              int nc_pad) {
+    using T2 = typename Vec2<T>::type;
+    constexpr int NV = (P + 1) * (P + 1), NQ = (P + 1) * (P + 2) / 2, NT = kRotThreads;
     extern __shared__ __align__(16) unsigned char rot_smem[];
-    T *sh = reinterpret_cast<T *>(rot_smem);
-    SmemV<T> acc{sh + threadIdx.x};
-    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    __shared__ int max_rounds;
+    T2 *sq = reinterpret_cast<T2 *>(rot_smem);
+    AccC<T, NT> acc{sq + threadIdx.x};
+    const int64_t t = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (t >= n_nodes) return;
-    const typename Vec4<T>::type ct = tcenter[t];
-    const T aL = thalf[t].w, iaL = T(1) / aL;
+    const bool live = t < n_nodes;
+    typename Vec4<T>::type ct{};
+    T iaL = T(1);
+    int b = 0, e = 0;
+    if (live) {
+        ct = tcenter[t];
+        iaL = T(1) / thalf[t].w;
+        b = off[t];
+        e = off[t + 1];
+    }
 #pragma unroll
-    for (int i = 0; i < NV; ++i) acc.set(i, T(0));
-    const int e = off[t + 1];
-    for (int k = off[t] + lane; k < e; k += 32) {
+    for (int q = 0; q < NQ; ++q) acc.set(q, T2{});
+    if (threadIdx.x == 0) max_rounds = 0;
+    __syncthreads();
+    if (lane == 0) atomicMax(&max_rounds, (e - b + 31) >> 5);
+    __syncthreads();
+    const int rounds = max_rounds;
+    for (int r = 0; r < rounds; ++r) {
+        __syncthreads();
+        const int k = b + r * 32 + lane;
+        if (k >= e) continue;
         const int s = __ldg(src + k);
         const typename Vec4<T>::type cs = center[s];
         const T c = half[s].w * iaL;
         if (sizeof(T) == 4 && c > (T)kRotExtremeRatio) continue;  // translated by k_m2l_generic
-        const typename Vec2<T>::type *Mrow = Mexp + (int64_t)s * nc_pad;
+        const T2 *Mrow = Mexp + (int64_t)s * nc_pad;
         if constexpr (V_IN_SMEM) {
-            SmemV<T> v{sh + NV * 128 + threadIdx.x};
+            SmemV<T, NT> v{reinterpret_cast<T *>(sq + NQ * NT) + threadIdx.x};
             rot_pair<T, P>(v, acc, Mrow, c, (ct.x - cs.x) * iaL, (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL);
         } else {
             RegV<T, NV> v;
             rot_pair<T, P>(v, acc, Mrow, c, (ct.x - cs.x) * iaL, (ct.y - cs.y) * iaL, (ct.z - cs.z) * iaL);
         }
     }
-    typename Vec2<T>::type *out = Lexp + t * nc_pad;
+    if (!live) return;
+    T2 *out = Lexp + t * nc_pad;
 #pragma unroll
     for (int n = 0; n <= P; ++n) {
 #pragma unroll
         for (int m = 0; m <= n; ++m) {
-            T re = acc.get(n * n + (m == 0 ? 0 : 2 * m - 1));
-            T im = m == 0 ? T(0) : acc.get(n * n + 2 * m);
+            const int q = tri(n, m);
+            const T2 a = acc.get(q);
+            T re = a.x, im = a.y;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 re += __shfl_xor_sync(0xffffffffu, re, o);
                 im += __shfl_xor_sync(0xffffffffu, im, o);
             }
-            const int q = tri(n, m);
             if ((q & 31) == lane) {
-                typename Vec2<T>::type r;
+                T2 r;
                 r.x = re * iaL;
                 r.y = im * iaL;
                 out[q] = r;
@@ -262,13 +341,13 @@ int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tc
                const void *hal, const void *Mx, void *Lx, int nc_pad, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
     using T2 = typename Vec2<T>::type;
-    constexpr int NV = (P + 1) * (P + 1);
-    constexpr size_t smem = (size_t)(V_IN_SMEM ? 2 : 1) * NV * 128 * sizeof(T);
+    constexpr int NV = (P + 1) * (P + 1), NQ = (P + 1) * (P + 2) / 2, NT = kRotThreads;
+    constexpr size_t smem = (size_t)NQ * NT * sizeof(T2) + (V_IN_SMEM ? (size_t)NV * NT * sizeof(T) : 0);
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_m2l_rot<T, P, V_IN_SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr != cudaSuccess)
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot shared memory attribute: ") + cudaGetErrorString(attr));
-    k_m2l_rot<T, P, V_IN_SMEM><<<nblk(M * 32, 128), 128, smem, s>>>(
+    k_m2l_rot<T, P, V_IN_SMEM><<<nblk(M * 32, NT), NT, smem, s>>>(
         M, off, src, static_cast<const T4 *>(tcen), static_cast<const T4 *>(thal), static_cast<const T4 *>(cen),
         static_cast<const T4 *>(hal), static_cast<const T2 *>(Mx), static_cast<T2 *>(Lx), nc_pad);
     EDFMM_LAUNCH_CHECK("k_m2l_rot");

@@ -1,10 +1,13 @@
 // Near field (P2P) fused with the local-expansion evaluation (L2P) and the
 // matvec epilogue.
 //
-// One warp owns one target leaf: each lane holds one target point (two when
-// the leaf has more than 32 points).  Source leaves of the target's P2P row
-// are staged 32 points at a time in shared memory as (x, y, z, q) and read by
-// broadcast, so every 16-byte load feeds 32 (or 64) interactions.  The kernel
+// One warp owns one target leaf.  Source leaves of the target's P2P row are
+// staged in shared memory (FP32: 64 points at a time, the next chunk loaded
+// while the current one is computed; FP64: 32) and read by broadcast.  FP32
+// splits the leaf's targets into slots that each fill the warp (32 targets
+// with one lane each, 16 with two, 8 with four, 4 with eight) and runs the
+// distances as packed FP32 pairs; FP64 gives each lane one or two targets
+// (or lets 2 / 4 lanes share one on small leaves).  The kernel
 // is the reference's kernels_cpu.py:83-153 contribution
 //     q_s / max(|x_t - x_s|, eps)   (eps = machine epsilon of the dtype)
 // evaluated as q_s * rsqrt(max(r^2, eps^2)), with the diagonal dropped only
@@ -28,7 +31,6 @@ template <typename T> __device__ __forceinline__ T rdiv(int n, int m);
 template <> __device__ __forceinline__ float rdiv<float>(int n, int m) { return c_rdiv_f[n][m]; }
 template <> __device__ __forceinline__ double rdiv<double>(int n, int m) { return c_rdiv_d[n][m]; }
 
-__device__ __forceinline__ float inv_dist(float r2, float eps2) { return rsqrtf(fmaxf(r2, eps2)); }
 __device__ __forceinline__ double inv_dist(double r2, double eps2) { return rsqrt(fmax(r2, eps2)); }
 
 // Re sum_{n,m} L_n^m R_n^m(x, y, z) over m in [-n, n]
@@ -112,41 +114,195 @@ __device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *s
     for (int u = 0; u < TPL; ++u) acc[u] += psum[u];
 }
 
-// FP32 form: the chunk is staged as separate x / y / z / q arrays and
-// sources are taken two at a time, so the distance and the accumulation run
-// as packed FP32 pairs (FADD2 / FMUL2 / FFMA2) and only the reciprocal square
-// roots and the eps clamp are scalar.  An odd chunk is padded with a
-// zero-charge source.
-template <int TPL, int G, bool SELF>
-__device__ __forceinline__ void accumulate_pairs(const float *sx, const float *sy, const float *sz, const float *sw,
-                                                 int cnt, int sbase, int part, const float2 (&nx)[2],
-                                                 const float2 (&ny)[2], const float2 (&nz)[2], const int (&ti)[2],
-                                                 float eps2, float (&acc)[2]) {
-    float2 ps[2] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+// FP32 target slots.  A block of nt <= 64 targets of a leaf is split by the
+// binary digits of nt rounded up to a multiple of 4: up to two slots of 32
+// targets with one lane each, then 16 targets with 2 lanes each, 8 with 4
+// and 4 with 8.  Every slot fills the warp, so the lanes stay busy whatever
+// the leaf size; the lanes of a target take every G-th source pair of a
+// chunk and a fixed shuffle tree combines them.
+struct SlotF {
+    float2 nx, ny, nz;  // -x of the lane's target, in both halves
+    float2 ps;          // packed partial sums
+    int ti;             // target point index
+};
+
+template <int G, bool SELF>
+__device__ __forceinline__ void accumulate_slot(const float *sx, const float *sy, const float *sz, const float *sw,
+                                                int cnt, int sbase, int part, SlotF &S, float eps2) {
     const int np = (cnt + 1) >> 1;
+    float2 ps = S.ps;
 #pragma unroll 4
     for (int j = part; j < np; j += G) {
         const float2 qx = *reinterpret_cast<const float2 *>(sx + 2 * j);
         const float2 qy = *reinterpret_cast<const float2 *>(sy + 2 * j);
         const float2 qz = *reinterpret_cast<const float2 *>(sz + 2 * j);
         const float2 qw = *reinterpret_cast<const float2 *>(sw + 2 * j);
-#pragma unroll
-        for (int u = 0; u < TPL; ++u) {
-            const float2 dx = __fadd2_rn(qx, nx[u]), dy = __fadd2_rn(qy, ny[u]), dz = __fadd2_rn(qz, nz[u]);
-            const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-            float i0 = rsqrtf(fmaxf(r2.x, eps2)), i1 = rsqrtf(fmaxf(r2.y, eps2));
-            if (SELF) {
-                if (sbase + 2 * j == ti[u]) i0 = 0.0f;
-                if (sbase + 2 * j + 1 == ti[u]) i1 = 0.0f;
-            }
-            ps[u] = __ffma2_rn(qw, make_float2(i0, i1), ps[u]);
+        const float2 dx = __fadd2_rn(qx, S.nx), dy = __fadd2_rn(qy, S.ny), dz = __fadd2_rn(qz, S.nz);
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        float i0 = rsqrtf(fmaxf(r2.x, eps2)), i1 = rsqrtf(fmaxf(r2.y, eps2));
+        if (SELF) {
+            if (sbase + 2 * j == S.ti) i0 = 0.0f;
+            if (sbase + 2 * j + 1 == S.ti) i1 = 0.0f;
         }
+        ps = __ffma2_rn(qw, make_float2(i0, i1), ps);
     }
-#pragma unroll
-    for (int u = 0; u < TPL; ++u) acc[u] += ps[u].x + ps[u].y;
+    S.ps = ps;
 }
 
-// One block of up to 32 * TPL / G targets of leaf t.  With G > 1 (small
+template <int G>
+__device__ __forceinline__ void slot_init(const NearParams<float> &P, int tb, int te, int base, int lane, SlotF &S) {
+    const int ti = tb + base + lane / G;
+    S.ti = ti < te ? ti : -1;
+    const float4 x = P.pts[ti < te ? ti : tb];
+    S.nx = make_float2(-x.x, -x.x);
+    S.ny = make_float2(-x.y, -x.y);
+    S.nz = make_float2(-x.z, -x.z);
+    S.ps = make_float2(0.0f, 0.0f);
+}
+
+template <int G>
+__device__ __forceinline__ void slot_finish(SlotF &S, int lane, int tb, float *pot) {
+    float a = S.ps.x + S.ps.y;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane % G == 0 && S.ti >= 0) pot[S.ti - tb] = a;
+}
+
+template <bool SELF>
+__device__ __forceinline__ void accumulate_slots(const float *sx, const float *sy, const float *sz, const float *sw,
+                                                 int cnt, int sb, int lane, const bool (&on)[5], SlotF (&S)[5],
+                                                 float eps2) {
+    if (on[0]) accumulate_slot<1, SELF>(sx, sy, sz, sw, cnt, sb, 0, S[0], eps2);
+    if (on[1]) accumulate_slot<1, SELF>(sx, sy, sz, sw, cnt, sb, 0, S[1], eps2);
+    if (on[2]) accumulate_slot<2, SELF>(sx, sy, sz, sw, cnt, sb, lane % 2, S[2], eps2);
+    if (on[3]) accumulate_slot<4, SELF>(sx, sy, sz, sw, cnt, sb, lane % 4, S[3], eps2);
+    if (on[4]) accumulate_slot<8, SELF>(sx, sy, sz, sw, cnt, sb, lane % 8, S[4], eps2);
+}
+
+// Targets tb..te-1 (at most 64) of leaf t: near field by slots, then the
+// local expansion and the epilogue with one lane per target.
+__device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, int tb, int te, float4 *sp, float *pot,
+                                           const Cplx<float> *sL) {
+    const int lane = threadIdx.x & 31;
+    const int nt = te - tb;
+    bool on[5];
+    int base[5];
+    {
+        int rem = (nt + 3) & ~3, o = 0;
+        on[0] = rem >= 32;
+        base[0] = o;
+        if (on[0]) o += 32, rem -= 32;
+        on[1] = rem >= 32;
+        base[1] = o;
+        if (on[1]) o += 32, rem -= 32;
+        on[2] = (rem & 16) != 0;
+        base[2] = o;
+        if (on[2]) o += 16;
+        on[3] = (rem & 8) != 0;
+        base[3] = o;
+        if (on[3]) o += 8;
+        on[4] = (rem & 4) != 0;
+        base[4] = o;
+    }
+    SlotF S[5];
+    slot_init<1>(P, tb, te, base[0], lane, S[0]);
+    slot_init<1>(P, tb, te, base[1], lane, S[1]);
+    slot_init<2>(P, tb, te, base[2], lane, S[2]);
+    slot_init<4>(P, tb, te, base[3], lane, S[3]);
+    slot_init<8>(P, tb, te, base[4], lane, S[4]);
+    if (P.near) {
+        // Source chunks of up to 64 points (one leaf, or a 64-point piece of
+        // a larger one) staged as x / y / z / q arrays.  The leaf ids and
+        // ranges of the row are read 32 entries at a time (one per lane) and
+        // broadcast by shuffles, and the next chunk's points are loaded
+        // before the current chunk is computed, so the dependent global
+        // loads overlap the arithmetic.
+        float *sx = reinterpret_cast<float *>(sp), *sy = sx + 64, *sz = sx + 128, *sw = sx + 192;
+        const int kbeg = P.off[t], kend = P.off[t + 1];
+        int kb = kbeg, s_l = 0, sa_l = 0, se_l = 0;
+        auto load_batch = [&](int base) {
+            kb = base;
+            const int k = base + lane;
+            s_l = k < kend ? P.src[k] : 0;
+            const int2 r = k < kend ? P.srange[s_l] : make_int2(0, 0);
+            sa_l = r.x;
+            se_l = r.y;
+        };
+        auto fetch = [&](int sb, int se, int i) {
+            return i < se - sb ? P.spts[sb + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        };
+        if (kbeg < kend) {
+            load_batch(kbeg);
+            int k = kbeg;
+            int s = __shfl_sync(0xffffffffu, s_l, 0), sb = __shfl_sync(0xffffffffu, sa_l, 0),
+                se = __shfl_sync(0xffffffffu, se_l, 0);
+            float4 qa = fetch(sb, se, lane), qb = fetch(sb, se, lane + 32);
+            while (true) {
+                const int cs = s, csb = sb, cnt = min(64, se - sb);
+                __syncwarp();
+                sx[lane] = qa.x;
+                sy[lane] = qa.y;
+                sz[lane] = qa.z;
+                sw[lane] = qa.w;
+                sx[lane + 32] = qb.x;
+                sy[lane + 32] = qb.y;
+                sz[lane + 32] = qb.z;
+                sw[lane + 32] = qb.w;
+                __syncwarp();
+                bool more = true;
+                if (sb + 64 < se) {
+                    sb += 64;
+                } else if (++k >= kend) {
+                    more = false;
+                } else {
+                    if (k >= kb + 32) load_batch(k);
+                    s = __shfl_sync(0xffffffffu, s_l, k - kb);
+                    sb = __shfl_sync(0xffffffffu, sa_l, k - kb);
+                    se = __shfl_sync(0xffffffffu, se_l, k - kb);
+                }
+                if (more) {
+                    qa = fetch(sb, se, lane);
+                    qb = fetch(sb, se, lane + 32);
+                }
+                if (P.same && cs == t)
+                    accumulate_slots<true>(sx, sy, sz, sw, cnt, csb, lane, on, S, P.eps2);
+                else
+                    accumulate_slots<false>(sx, sy, sz, sw, cnt, csb, lane, on, S, P.eps2);
+                if (!more) break;
+            }
+        }
+    }
+    slot_finish<1>(S[0], lane, tb, pot);
+    slot_finish<1>(S[1], lane, tb, pot);
+    slot_finish<2>(S[2], lane, tb, pot);
+    slot_finish<4>(S[3], lane, tb, pot);
+    slot_finish<8>(S[4], lane, tb, pot);
+    __syncwarp();
+    float4 c;
+    float ia = 1.0f;
+    if (P.far) {
+        c = P.center[t];
+        ia = 1.0f / P.half[t].w;
+    }
+    for (int i = lane; i < nt; i += 32) {
+        const int ti = tb + i;
+        const float4 x = P.pts[ti];
+        float v = P.near ? pot[i] : 0.0f;
+        if (P.far) v += l2p_point<float>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
+        if (P.scatter) {
+            const int o = P.index_map[ti];
+            v = v * P.k_e;
+            if (P.self_int) v += P.self_int[o] * P.sigma[o] * P.areas[o];
+            if (!isfinite(v)) v = 0.0f;
+            P.out[o] = v;
+        } else {
+            P.out[ti] = v;
+        }
+    }
+    __syncwarp();
+}
+
+// FP64: one block of up to 32 * TPL / G targets of leaf t.  With G > 1 (small
 // leaves) G lanes share a target, each taking every G-th source of a chunk,
 // and their sums are combined with a fixed shuffle tree.
 template <typename T, int TPL, int G>
@@ -166,13 +322,6 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
         valid[u] = u < TPL && ti[u] < te;
         x[u] = valid[u] ? P.pts[ti[u]] : P.pts[tb];
     }
-    float2 nx[2], ny[2], nz[2];  // -x of each target, broadcast to both halves (FP32 path)
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        nx[u] = make_float2(-(float)x[u].x, -(float)x[u].x);
-        ny[u] = make_float2(-(float)x[u].y, -(float)x[u].y);
-        nz[u] = make_float2(-(float)x[u].z, -(float)x[u].z);
-    }
     if (P.near) {
         const int e = P.off[t + 1];
         for (int k = P.off[t]; k < e; ++k) {
@@ -181,26 +330,12 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
             for (int sb = sr.x; sb < sr.y; sb += 32) {
                 const int cnt = min(32, sr.y - sb);
                 __syncwarp();
-                if constexpr (sizeof(T) == 4) {
-                    float *sx = reinterpret_cast<float *>(sp), *sy = sx + 32, *sz = sx + 64, *sw = sx + 96;
-                    const T4 q = lane < cnt ? P.spts[sb + lane] : T4{0.0f, 0.0f, 0.0f, 0.0f};
-                    sx[lane] = q.x;
-                    sy[lane] = q.y;
-                    sz[lane] = q.z;
-                    sw[lane] = q.w;
-                    __syncwarp();
-                    if (P.same && s == t)
-                        accumulate_pairs<TPL, G, true>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
-                    else
-                        accumulate_pairs<TPL, G, false>(sx, sy, sz, sw, cnt, sb, part, nx, ny, nz, ti, P.eps2, acc);
-                } else {
-                    if (lane < cnt) sp[lane] = P.spts[sb + lane];
-                    __syncwarp();
-                    if (P.same && s == t)
-                        accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
-                    else
-                        accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
-                }
+                if (lane < cnt) sp[lane] = P.spts[sb + lane];
+                __syncwarp();
+                if (P.same && s == t)
+                    accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
+                else
+                    accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
             }
         }
     }
@@ -232,8 +367,9 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
 
 template <typename T> __global__ void __launch_bounds__(128) k_p2p_l2p(const NearParams<T> P) {
     using T4 = typename Vec4<T>::type;
-    __shared__ T4 sp[4][32];
+    __shared__ T4 sp[4][64];  // FP32: a staged chunk of up to 64 sources; FP64: up to 32
     __shared__ Cplx<T> sL[4][ncoef(kPMax)];
+    __shared__ float spot[4][64];  // FP32: the near-field sums of a block of targets
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t w = (int64_t)blockIdx.x * 4 + wl;
     if (w >= P.n_leaves) return;
@@ -245,7 +381,10 @@ template <typename T> __global__ void __launch_bounds__(128) k_p2p_l2p(const Nea
     }
     const int2 rg = P.range[t];
     const int nt = rg.y - rg.x;
-    if (nt <= 8) {
+    if constexpr (sizeof(T) == 4) {
+        for (int tb = rg.x; tb < rg.y; tb += 64)
+            leaf_slots(P, t, tb, min(rg.y, tb + 64), sp[wl], spot[wl], sL[wl]);
+    } else if (nt <= 8) {
         leaf_block<T, 1, 4>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
     } else if (nt <= 16) {
         leaf_block<T, 1, 2>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
