@@ -618,6 +618,9 @@ def run_batch_workload(args, rank, world, local):
                           "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
                           "inner_operator": {k: tune[k] for k in ("leaf_size", "expansion_order", "ms")}},
                "solve": {"code": info["code"], "outer_iters": info["outer"], "inner_iters": info["inner_iters"],
+                         "instance_inner_iters": ({"mean": float(np.mean(info["instance_inner_iters"])),
+                                                   "max": int(max(info["instance_inner_iters"]))}
+                                                  if info.get("instance_inner_iters") else None),
                          "fp64_matvecs": info["matvec64"], "max_instance_rel_resid": float(per.max()),
                          "instances_converged": int((per <= 1e-6 * (1 + 1e-9)).sum()),
                          "plain_fp64_per_instance": {"instances_timed": sub, "panels_timed": n_sub,

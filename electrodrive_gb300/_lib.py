@@ -116,6 +116,11 @@ def _declare(L):
         "edfmm_gmres_start": (i32, [i64, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "edfmm_gmres_arnoldi": (i32, [i64, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "edfmm_gmres_update": (i32, [i64, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "edfmm_bgmres_state_cols": (C.c_size_t, [i32]),
+        "edfmm_bgmres_work_bytes": (C.c_size_t, [i32, i32, i32]),
+        "edfmm_bgmres_start": (i32, [i64, i32, i32, _vp, i32, i32, _vp, _vp, _vp, _vp, _vp, i32, _vp, _vp, _vp]),
+        "edfmm_bgmres_arnoldi": (i32, [i64, i32, i32, _vp, i32, i32, i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "edfmm_bgmres_update": (i32, [i64, i32, i32, _vp, i32, i32, i32, _vp, _vp, _vp, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

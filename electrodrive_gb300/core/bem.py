@@ -29,7 +29,7 @@ from .. import _lib
 from ..utils.config import K_E, BEMConfig
 from .bem_mesh import TriMesh, generate_mesh
 from .bem_near import NearCorrection, point_charge_potential, potential_at_targets, self_integrals
-from .bem_solver import gmres_restart
+from .bem_solver import gmres_batched, gmres_restart
 from .operators import DenseOperator, FmmOperator
 
 
@@ -249,16 +249,16 @@ def segment_norms(v: Tensor, offsets: Optional[List[int]]) -> Tensor:
     v2 = v.to(torch.float64) ** 2
     if offsets is None:
         return torch.sqrt(v2.sum()).reshape(1)
-    c = torch.cat([torch.zeros(1, dtype=torch.float64, device=v.device), torch.cumsum(v2, 0)])
-    o = torch.as_tensor(offsets, device=v.device)
-    return torch.sqrt((c[o[1:]] - c[o[:-1]]).clamp_min(0.0))
+    o = torch.as_tensor(offsets, dtype=torch.int64)
+    lengths = (o[1:] - o[:-1]).to(v.device)
+    return torch.sqrt(torch.segment_reduce(v2, "sum", lengths=lengths))
 
 
 def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: Optional[Tensor] = None,
                 rtol: float = 1e-6, inner_restart: int = 40, inner_tol: Optional[float] = None,
                 inner_tol_floor: float = 1e-5, inner_maxiter: int = 400, max_outer: int = 30, use_graph: bool = True,
-                inner_early_exit: Optional[int] = 8, segments: Optional[List[int]] = None
-                ) -> Tuple[Tensor, Dict[str, Any]]:
+                inner_early_exit: Optional[int] = 8, segments: Optional[List[int]] = None,
+                batched: bool = True) -> Tuple[Tensor, Dict[str, Any]]:
     """FP32 GMRES corrections inside FP64 iterative refinement.
 
     Stops when ||b - A64 x|| / ||b|| <= rtol (FP64 true residual; with
@@ -269,7 +269,10 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
     full cycles).  Each inner solve aims at the reduction the outer target
     still needs, 0.3 rtol / (current relative residual), but at most
     ``inner_tol_floor`` (about what the FP32 operator can deliver against the
-    FP64 one); a fixed ``inner_tol`` overrides that.
+    FP64 one); a fixed ``inner_tol`` overrides that.  With ``segments`` and
+    ``batched`` the inner solve is ``gmres_batched``: every instance gets its
+    own Krylov space and its own inner tolerance (instances already at rtol
+    sit out), and the steps share one operator application.
     """
     dev = b.device
     b64 = b.to(torch.float64)
@@ -279,6 +282,7 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
     d32 = None if A_diag is None else A_diag.to(dev, torch.float32)
     hist = []
     inner_total = 0
+    inst_iters = None  # per-instance inner steps (batched inner solves)
     matvec64 = 0
     r = b64 - op64(x)
     matvec64 += 1
@@ -290,20 +294,32 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
                            matvec64=matvec64)
         if rel <= rtol:
             return x, dict(success=True, code=0, outer=it, inner_iters=inner_total, rel_resid=rel, history=hist,
-                           matvec64=matvec64)
+                           matvec64=matvec64, instance_inner_iters=inst_iters)
         if it == max_outer:
             break
-        tol_k = inner_tol if inner_tol is not None else min(0.1, max(inner_tol_floor, 0.3 * rtol / rel))
         r32 = r.to(torch.float32)
-        d, info = gmres_restart(op32, r32, restart=inner_restart, tol=tol_k, maxiter=inner_maxiter,
-                                precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph,
-                                early_exit=inner_early_exit)
+        if segments is not None and batched:
+            rel_i = segment_norms(r, segments) / bseg
+            if inner_tol is not None:
+                tol_i = torch.full_like(rel_i, float(inner_tol))
+            else:
+                tol_i = (0.3 * rtol / rel_i).clamp(min=inner_tol_floor, max=0.1)
+            tol_i = torch.where(rel_i > rtol, tol_i, torch.full_like(tol_i, -1.0))
+            d, info = gmres_batched(op32, r32, segments, restart=inner_restart, tol=tol_i, maxiter=inner_maxiter,
+                                    A_diag=d32, use_graph=use_graph, check_every=inner_early_exit or 8)
+            per = info["instance_iters"]
+            inst_iters = per if inst_iters is None else [u + v for u, v in zip(inst_iters, per)]
+        else:
+            tol_k = inner_tol if inner_tol is not None else min(0.1, max(inner_tol_floor, 0.3 * rtol / rel))
+            d, info = gmres_restart(op32, r32, restart=inner_restart, tol=tol_k, maxiter=inner_maxiter,
+                                    precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph,
+                                    early_exit=inner_early_exit)
         inner_total += info["iters"]
         x = x + d.to(torch.float64)
         r = b64 - op64(x)
         matvec64 += 1
     return x, dict(success=False, code=1, outer=max_outer, inner_iters=inner_total, rel_resid=hist[-1], history=hist,
-                   matvec64=matvec64)
+                   matvec64=matvec64, instance_inner_iters=inst_iters)
 
 
 __all__ = ["BEMOperator", "BEMSolution", "assemble_system", "bem_solve", "build_operator", "bc_vector", "point_charges",

@@ -26,7 +26,7 @@ from __future__ import annotations
 
 import math
 import time
-from typing import Any, Callable, Dict, Optional, Tuple, Union
+from typing import Any, Callable, Dict, List, Optional, Sequence, Tuple, Union
 
 import torch
 from torch import Tensor
@@ -345,4 +345,171 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
     return x.to(orig_dtype).to(orig_device), _info(total_iters, r_norm, False, 1, r_true_norm, tol_abs, used_pc)
 
 
-__all__ = ["DiagonalPreconditioner", "setup_preconditioner", "gmres_restart"]
+class _BatchKrylov:
+    """Device buffers of one batched GMRES run (K instances back to back)."""
+
+    ACTIVE, TOTAL, RTRUE, TOLABS, NONFIN = 8, 9, 0, 6, 3
+
+    def __init__(self, segments: List[int], restart: int, dtype: torch.dtype, device: torch.device):
+        L = _lib.load_library()
+        self.L = L
+        self.n = int(segments[-1])
+        self.K = len(segments) - 1
+        lens = [segments[i + 1] - segments[i] for i in range(self.K)]
+        if min(lens) <= 0:
+            raise ValueError("every instance must own at least one row")
+        self.max_seg = max(lens)
+        self.restart, self.dtype, self.device = restart, dtype, device
+        self.code = _lib.dtype_code(dtype)
+        self.soff = torch.tensor(segments, dtype=torch.int64, device=device)
+        self.V = torch.zeros(restart + 1, self.n, dtype=dtype, device=device)
+        self.w = torch.zeros(self.n, dtype=dtype, device=device)
+        cols = int(L.edfmm_bgmres_state_cols(restart))
+        self.state = torch.zeros(self.K, cols, dtype=torch.float64, device=device)
+        nbytes = int(L.edfmm_bgmres_work_bytes(self.K, self.max_seg, restart))
+        self.work = torch.zeros((nbytes + 7) // 8, dtype=torch.float64, device=device)
+
+    def _head(self):
+        return (self.n, self.code, self.K, _lib.ptr(self.soff), self.max_seg, self.restart)
+
+    def start(self, b: Tensor, ax: Tensor, pinv: Optional[Tensor], tol: Tensor, first: bool):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_bgmres_start(*self._head(), P(b), P(ax), P(pinv), P(self.V[0]), P(tol),
+                                             1 if first else 0, P(self.state), P(self.work),
+                                             _lib.stream_handle(self.device)), "edfmm_bgmres_start")
+
+    def arnoldi(self, j: int, av: Tensor, pinv: Optional[Tensor]):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_bgmres_arnoldi(*self._head(), j, P(self.V), P(av), P(pinv), P(self.w),
+                                               P(self.state), P(self.work), _lib.stream_handle(self.device)),
+                   "edfmm_bgmres_arnoldi")
+
+    def update(self, m: int, x: Tensor):
+        P = _lib.ptr
+        _lib.check(self.L.edfmm_bgmres_update(*self._head(), m, P(self.V), P(x), P(self.state), P(self.work),
+                                              _lib.stream_handle(self.device)), "edfmm_bgmres_update")
+
+
+@torch.no_grad()
+def gmres_batched(A: Callable[[Tensor], Tensor], b: Tensor, segments: List[int], *, restart: int = 40,
+                  tol: Union[float, Sequence[float], Tensor] = 1e-8, maxiter: int = 500,
+                  A_diag: Optional[Tensor] = None, x0: Optional[Tensor] = None, use_graph: bool = True,
+                  check_every: int = 8) -> Tuple[Tensor, Dict[str, Any]]:
+    """Restarted GMRES on K independent systems at once (not in the reference).
+
+    ``segments`` are the K+1 row offsets of the instances in ``b``; ``A`` must
+    be block diagonal over them (a batched plan's operator).  Every instance
+    runs the algorithm of ``gmres_restart`` with Jacobi preconditioning by
+    ``A_diag`` in its own Krylov space: its cycle ends at the step where its
+    residual estimate meets ``tol_k`` times its first preconditioned residual,
+    and it is done when its true residual at a cycle start is within
+    ``tol_k`` of its initial one.  One operator application per step serves
+    all instances still iterating; finished ones contribute zero rows.  A
+    negative ``tol_k`` leaves instance k untouched.  The host reads the active
+    flags every ``check_every`` steps (one captured graph per chunk).
+
+    Returns x and a dict with ``iters`` (operator applications), per-instance
+    ``instance_iters``, ``converged`` (bool per instance), ``rel_resid`` (true
+    residual at the last cycle start over the initial one) and ``code``
+    (0 all converged, 1 iteration limit, 5 non-finite values).
+    """
+    if restart <= 0 or restart > 256:
+        raise ValueError("restart must be in [1, 256]")
+    if maxiter <= 0:
+        raise ValueError("maxiter must be positive")
+    segments = [int(v) for v in segments]
+    if segments[0] != 0 or segments[-1] != b.numel() or any(segments[i + 1] < segments[i]
+                                                             for i in range(len(segments) - 1)):
+        raise ValueError("segments must be non-decreasing offsets from 0 to len(b)")
+    dev = b.device
+    if dev.type != "cuda":
+        raise RuntimeError("gmres_batched needs CUDA tensors")
+    dtype = b.dtype
+    if dtype not in (torch.float32, torch.float64):
+        raise ValueError("b must be float32 or float64")
+    K = len(segments) - 1
+    Kr = _BatchKrylov(segments, restart, dtype, dev)
+    tolv = torch.as_tensor(tol, dtype=torch.float64).reshape(-1).to(dev)
+    if tolv.numel() == 1:
+        tolv = tolv.expand(K).contiguous()
+    if tolv.numel() != K:
+        raise ValueError("tol must be a scalar or one value per instance")
+    pinv = None
+    if A_diag is not None:
+        pinv = setup_preconditioner("jacobi", A_diag=A_diag).pinv.to(dev, dtype).contiguous()
+    x = torch.zeros_like(b) if x0 is None else x0.to(dev, dtype).clone()
+    b = b.contiguous()
+    av = torch.empty_like(b)
+
+    def steps_eager(j0: int, count: int):
+        for j in range(j0, j0 + count):
+            av.copy_(A(Kr.V[j]))
+            Kr.arnoldi(j, av, pinv)
+
+    graphs: Dict[Tuple[int, int], Any] = {}
+
+    def run_steps(j0: int, count: int):
+        if not use_graph:
+            steps_eager(j0, count)
+            return
+        key = (j0, count)
+        if key not in graphs:
+            if not graphs:
+                # warm the operator's lazy state outside the capture; the
+                # output is discarded, so the Krylov state is untouched
+                torch.cuda.synchronize(dev)
+                s = torch.cuda.Stream(device=dev)
+                s.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.stream(s):
+                    A(Kr.V[j0])
+                torch.cuda.current_stream(dev).wait_stream(s)
+                torch.cuda.synchronize(dev)
+            g = torch.cuda.CUDAGraph()
+            l0 = _lib.launch_count()
+            with torch.cuda.graph(g):
+                steps_eager(j0, count)
+            n_k = _lib.launch_count() - l0
+            _lib.note_graph_replay(-n_k)  # captured, not executed
+            graphs[key] = (g, n_k)
+        g, n_k = graphs[key]
+        g.replay()
+        _lib.note_graph_replay(n_k)
+
+    chunk = max(1, int(check_every))
+    total = 0
+    r0 = None
+    code = 1
+    max_cycles = max(1, (maxiter + restart - 1) // restart)
+    for cycle in range(max_cycles + 1):
+        Kr.start(b, A(x), pinv, tolv, cycle == 0)
+        st = Kr.state[:, :10].cpu()
+        if cycle == 0:
+            r0 = st[:, Kr.RTRUE].clone()
+        if bool((st[:, Kr.NONFIN] != 0).any()):
+            code = 5
+            break
+        if not bool((st[:, Kr.ACTIVE] != 0).any()):
+            code = 0
+            break
+        if total >= maxiter:
+            code = 1
+            break
+        steps = min(restart, maxiter - total)
+        j0 = 0
+        while j0 < steps:
+            cnt = min(chunk, steps - j0)
+            run_steps(j0, cnt)
+            j0 += cnt
+            if not bool((Kr.state[:, Kr.ACTIVE] != 0).any()):
+                break
+        total += j0
+        Kr.update(j0, x)
+    st = Kr.state[:, :10].cpu()
+    r0s = torch.where(r0 > 0, r0, torch.ones_like(r0))
+    converged = (st[:, Kr.RTRUE] <= st[:, Kr.TOLABS])
+    return x, dict(iters=total, instance_iters=st[:, Kr.TOTAL].to(torch.int64).tolist(),
+                   converged=converged.tolist(), rel_resid=(st[:, Kr.RTRUE] / r0s).tolist(), code=code,
+                   success=code == 0)
+
+
+__all__ = ["DiagonalPreconditioner", "setup_preconditioner", "gmres_restart", "gmres_batched"]

@@ -23,7 +23,7 @@ namespace {
 constexpr int kRows = 256;  // targets per block (one per thread)
 constexpr int kTile = 256;  // sources staged per shared-memory tile
 
-__device__ __forceinline__ float inv_r(float r2) { return rsqrtf(fmaxf(r2, 1e-24f)); }
+__device__ __forceinline__ float inv_r(float r2) { return rsqrt_normal(fmaxf(r2, 1e-24f)); }
 __device__ __forceinline__ double inv_r(double r2) { return rsqrt(fmax(r2, 1e-24)); }
 
 template <typename T>

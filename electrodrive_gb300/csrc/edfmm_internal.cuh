@@ -110,6 +110,17 @@ template <> struct Vec4<double> {
     using type = double4;
 };
 
+#ifdef __CUDACC__
+// 1/sqrt(x) for a normal x > 0 (PTX rsqrt.approx.ftz.f32, relative error
+// below 2^-22.9).  Callers clamp the argument well above the subnormal range,
+// so flushing subnormals changes nothing and no range handling is needed.
+__device__ __forceinline__ float rsqrt_normal(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+#endif
+
 // Device-resident tree in DFS pre-order (the reference's node numbering).
 struct DevTree {
     int dtype = EDFMM_F32;

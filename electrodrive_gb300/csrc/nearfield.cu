@@ -33,6 +33,7 @@ template <> __device__ __forceinline__ double rdiv<double>(int n, int m) { retur
 
 __device__ __forceinline__ double inv_dist(double r2, double eps2) { return rsqrt(fmax(r2, eps2)); }
 
+
 // Re sum_{n,m} L_n^m R_n^m(x, y, z) over m in [-n, n]
 template <typename T>
 __device__ __forceinline__ T l2p_point(const Cplx<T> *L, int p, T x, T y, T z) {
@@ -139,7 +140,7 @@ __device__ __forceinline__ void accumulate_slot(const float *sx, const float *sy
         const float2 qw = *reinterpret_cast<const float2 *>(sw + 2 * j);
         const float2 dx = __fadd2_rn(qx, S.nx), dy = __fadd2_rn(qy, S.ny), dz = __fadd2_rn(qz, S.nz);
         const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-        float i0 = rsqrtf(fmaxf(r2.x, eps2)), i1 = rsqrtf(fmaxf(r2.y, eps2));
+        float i0 = rsqrt_normal(fmaxf(r2.x, eps2)), i1 = rsqrt_normal(fmaxf(r2.y, eps2));
         if (SELF) {
             if (sbase + 2 * j == S.ti) i0 = 0.0f;
             if (sbase + 2 * j + 1 == S.ti) i1 = 0.0f;

