@@ -616,7 +616,9 @@ def run_batch_workload(args, rank, world, local):
                "dtype": "f32+f64", "data": "synthetic",
                "config": {"workload": workload, "instances": K, "n_panels": n_total, "setup_s": t_setup,
                           "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
-                          "inner_operator": {k: tune[k] for k in ("leaf_size", "expansion_order", "ms")}},
+                          "inner_operator": {k: tune[k] for k in ("leaf_size", "expansion_order", "ms")},
+                          "inner_solver": "batched GMRES (one Krylov space per instance), restart 100",
+                          "start": "zero (first residual = b)"},
                "solve": {"code": info["code"], "outer_iters": info["outer"], "inner_iters": info["inner_iters"],
                          "instance_inner_iters": ({"mean": float(np.mean(info["instance_inner_iters"])),
                                                    "max": int(max(info["instance_inner_iters"]))}

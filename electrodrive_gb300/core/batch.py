@@ -113,9 +113,14 @@ class BatchSystem:
                          instance_offsets=self.offsets)
         return FmmOperator(plan, self.areas.to(dtype), self.self_corr.to(dtype))
 
-    def solve(self, x0: Optional[Tensor] = None, rtol: float = 1e-6, **kw) -> Tuple[Tensor, Dict[str, Any]]:
-        return solve_mixed(self.op64, self.op32, self.b, A_diag=self.diag, x0=self.x0_cold if x0 is None else x0,
-                           rtol=rtol, segments=self.offsets, **kw)
+    def solve(self, x0: Optional[Tensor] = None, rtol: float = 1e-6, inner_restart: int = 100,
+              **kw) -> Tuple[Tensor, Dict[str, Any]]:
+        """Mixed FP32/FP64 solve of all instances to ``rtol`` each.  Without
+        ``x0`` the solve starts from zero, whose residual is b itself (one FP64
+        operator application fewer than the cold start b / I_self, which the
+        Jacobi-preconditioned inner solve reaches in its first step anyway)."""
+        return solve_mixed(self.op64, self.op32, self.b, A_diag=self.diag, x0=x0, rtol=rtol,
+                           segments=self.offsets, inner_restart=inner_restart, **kw)
 
     def residuals(self, x: Tensor) -> Tensor:
         """Each instance's relative FP64 true residual."""

@@ -219,6 +219,7 @@ __device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, in
         // before the current chunk is computed, so the dependent global
         // loads overlap the arithmetic.
         float *sx = reinterpret_cast<float *>(sp), *sy = sx + 64, *sz = sx + 128, *sw = sx + 192;
+        const float eps2 = P.eps2;
         const int kbeg = P.off[t], kend = P.off[t + 1];
         int kb = kbeg, s_l = 0, sa_l = 0, se_l = 0;
         auto load_batch = [&](int base) {
@@ -266,9 +267,9 @@ __device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, in
                     qb = fetch(sb, se, lane + 32);
                 }
                 if (P.same && cs == t)
-                    accumulate_slots<true>(sx, sy, sz, sw, cnt, csb, lane, on, S, P.eps2);
+                    accumulate_slots<true>(sx, sy, sz, sw, cnt, csb, lane, on, S, eps2);
                 else
-                    accumulate_slots<false>(sx, sy, sz, sw, cnt, csb, lane, on, S, P.eps2);
+                    accumulate_slots<false>(sx, sy, sz, sw, cnt, csb, lane, on, S, eps2);
                 if (!more) break;
             }
         }
@@ -366,7 +367,7 @@ __device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb
     }
 }
 
-template <typename T> __global__ void __launch_bounds__(128) k_p2p_l2p(const NearParams<T> P) {
+template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 1) k_p2p_l2p(const NearParams<T> P) {
     using T4 = typename Vec4<T>::type;
     __shared__ T4 sp[4][64];  // FP32: a staged chunk of up to 64 sources; FP64: up to 32
     __shared__ Cplx<T> sL[4][ncoef(kPMax)];

@@ -1,0 +1,46 @@
+"""Mixed FP32/FP64 refinement (core.bem.solve_mixed) on a torus with the near
+correction: the solve stops only on an FP64 true residual <= rtol, whether
+the first residual of the start comes from the FP32 or the FP64 operator,
+and its density matches the plain FP64 GMRES solve of the same system.
+"""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torus_system(cuda_lib):
+    from electrodrive_gb300.core.bem import assemble_system
+    from electrodrive_gb300.core.bem_mesh import torus_mesh
+
+    spec = dict(conductors=[dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0)],
+                charges=[dict(type="point", q=1.0, pos=[1.6, 0.3, 0.2])])
+    mesh = torus_mesh(1.0, 0.35, 80, 32)
+    return assemble_system(mesh, spec, kind="fmm", dtypes=(torch.float64, torch.float32), near=True)
+
+
+@pytest.mark.parametrize("first", ["fp32", "fp64"])
+def test_mixed_solve_stops_on_fp64_residual(torus_system, first):
+    from electrodrive_gb300.core.bem import solve_mixed
+    from electrodrive_gb300.core.bem_solver import gmres_restart
+
+    S = torus_system
+    op64, op32 = S["ops"][torch.float64], S["ops"][torch.float32]
+    b = S["b"]
+    x, info = solve_mixed(op64, op32, b, A_diag=S["diag"], x0=S["x0"], rtol=1e-6, first_residual=first)
+    assert info["code"] == 0, info
+    rel = float(torch.linalg.norm(b - op64(x)) / torch.linalg.norm(b))
+    assert rel <= 1e-6 * (1 + 1e-9)
+    assert abs(rel - info["rel_resid"]) <= 1e-3 * rel  # the reported residual is the FP64 one
+    bn = float(torch.linalg.norm(b))
+    r0 = float(torch.linalg.norm(b - op64(S["x0"])))
+    xp, pinfo = gmres_restart(op64, b, restart=256, tol=1e-9 * bn / r0, maxiter=2000, precond="jacobi",
+                              A_diag=S["diag"], x0=S["x0"], early_exit=8)
+    assert pinfo["code"] == 0
+    assert float(torch.linalg.norm(x - xp) / torch.linalg.norm(xp)) < 1e-4
+    if first == "fp32":
+        # the start's residual came from the FP32 operator: one FP64 application per refinement step
+        assert info["matvec64"] == info["outer"]
+    else:
+        assert info["matvec64"] == info["outer"] + 1
