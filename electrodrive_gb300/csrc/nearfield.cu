@@ -2,13 +2,12 @@
 // matvec epilogue.
 //
 // One warp owns one target leaf.  Source leaves of the target's P2P row are
-// staged in shared memory (FP32: 64 points at a time, the next chunk loaded
-// while the current one is computed; FP64: 32) and read by broadcast.  FP32
-// splits the leaf's targets into slots that each fill the warp (32 targets
-// with one lane each, 16 with two, 8 with four, 4 with eight) and runs the
-// distances as packed FP32 pairs; FP64 gives each lane one or two targets
-// (or lets 2 / 4 lanes share one on small leaves).  The kernel
-// is the reference's kernels_cpu.py:83-153 contribution
+// staged in shared memory 64 points at a time (the next chunk loaded while
+// the current one is computed) and read by broadcast.  The leaf's targets
+// are split into slots that each fill the warp (32 targets with one lane
+// each, 16 with two, 8 with four, 4 with eight); FP32 runs the distances as
+// packed pairs.  The kernel is the reference's kernels_cpu.py:83-153
+// contribution
 //     q_s / max(|x_t - x_s|, eps)   (eps = machine epsilon of the dtype)
 // evaluated as q_s * rsqrt(max(r^2, eps^2)), with the diagonal dropped only
 // inside the self leaf pair.  The same warp then evaluates the leaf's local
@@ -94,42 +93,31 @@ template <typename T> struct NearParams {
     T *out;
 };
 
-template <typename T, int TPL, int G, bool SELF>
-__device__ __forceinline__ void accumulate_chunk(const typename Vec4<T>::type *sp, int cnt, int sbase, int part,
-                                                 const typename Vec4<T>::type (&x)[2], const int (&ti)[2], T eps2,
-                                                 T (&acc)[2]) {
-    // per-chunk partial sums, then one add: two-level summation
-    T psum[2] = {(T)0, (T)0};
-#pragma unroll 8
-    for (int j = part; j < cnt; j += G) {
-        const typename Vec4<T>::type q = sp[j];
-#pragma unroll
-        for (int u = 0; u < TPL; ++u) {
-            const T dx = x[u].x - q.x, dy = x[u].y - q.y, dz = x[u].z - q.z;
-            T inv = inv_dist(dx * dx + dy * dy + dz * dz, eps2);
-            if (SELF && sbase + j == ti[u]) inv = (T)0;
-            psum[u] += q.w * inv;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < TPL; ++u) acc[u] += psum[u];
-}
-
-// FP32 target slots.  A block of nt <= 64 targets of a leaf is split by the
+// Target slots.  A block of nt <= 64 targets of a leaf is split by the
 // binary digits of nt rounded up to a multiple of 4: up to two slots of 32
 // targets with one lane each, then 16 targets with 2 lanes each, 8 with 4
 // and 4 with 8.  Every slot fills the warp, so the lanes stay busy whatever
-// the leaf size; the lanes of a target take every G-th source pair of a
-// chunk and a fixed shuffle tree combines them.
-struct SlotF {
+// the leaf size; the lanes of a target take every G-th source (FP32: source
+// pair) of a chunk and a fixed shuffle tree combines them.
+template <typename T> struct Slot;
+template <> struct Slot<float> {
     float2 nx, ny, nz;  // -x of the lane's target, in both halves
     float2 ps;          // packed partial sums
-    int ti;             // target point index
+    int ti;             // target point index, -1 for a padding lane
+};
+template <> struct Slot<double> {
+    double x, y, z;
+    double ps;
+    int ti;
 };
 
+// FP32: sources two at a time as packed pairs (FADD2 / FMUL2 / FFMA2); only
+// the reciprocal square roots and the eps clamp are scalar.  An odd chunk is
+// padded with a zero-charge source.
 template <int G, bool SELF>
-__device__ __forceinline__ void accumulate_slot(const float *sx, const float *sy, const float *sz, const float *sw,
-                                                int cnt, int sbase, int part, SlotF &S, float eps2) {
+__device__ __forceinline__ void accumulate_slot(const float *sx, int cnt, int sbase, int part, Slot<float> &S,
+                                                float eps2) {
+    const float *sy = sx + 64, *sz = sx + 128, *sw = sx + 192;
     const int np = (cnt + 1) >> 1;
     float2 ps = S.ps;
 #pragma unroll 4
@@ -150,40 +138,74 @@ __device__ __forceinline__ void accumulate_slot(const float *sx, const float *sy
     S.ps = ps;
 }
 
-template <int G>
-__device__ __forceinline__ void slot_init(const NearParams<float> &P, int tb, int te, int base, int lane, SlotF &S) {
-    const int ti = tb + base + lane / G;
-    S.ti = ti < te ? ti : -1;
-    const float4 x = P.pts[ti < te ? ti : tb];
-    S.nx = make_float2(-x.x, -x.x);
-    S.ny = make_float2(-x.y, -x.y);
-    S.nz = make_float2(-x.z, -x.z);
-    S.ps = make_float2(0.0f, 0.0f);
+// FP64: one source per step from the staged (x, y, z, q) chunk
+template <int G, bool SELF>
+__device__ __forceinline__ void accumulate_slot(const double4 *sp, int cnt, int sbase, int part, Slot<double> &S,
+                                                double eps2) {
+    double ps = 0.0;
+#pragma unroll 4
+    for (int j = part; j < cnt; j += G) {
+        const double4 q = sp[j];
+        const double dx = S.x - q.x, dy = S.y - q.y, dz = S.z - q.z;
+        double inv = inv_dist(dx * dx + dy * dy + dz * dz, eps2);
+        if (SELF && sbase + j == S.ti) inv = 0.0;
+        ps += q.w * inv;
+    }
+    S.ps += ps;  // per-chunk partial, then one add: two-level summation
 }
 
-template <int G>
-__device__ __forceinline__ void slot_finish(SlotF &S, int lane, int tb, float *pot) {
-    float a = S.ps.x + S.ps.y;
+template <typename T, int G>
+__device__ __forceinline__ void slot_init(const NearParams<T> &P, int tb, int te, int base, int lane, Slot<T> &S) {
+    const int ti = tb + base + lane / G;
+    S.ti = ti < te ? ti : -1;
+    const typename Vec4<T>::type x = P.pts[ti < te ? ti : tb];
+    if constexpr (sizeof(T) == 4) {
+        S.nx = make_float2(-x.x, -x.x);
+        S.ny = make_float2(-x.y, -x.y);
+        S.nz = make_float2(-x.z, -x.z);
+        S.ps = make_float2(0.0f, 0.0f);
+    } else {
+        S.x = x.x;
+        S.y = x.y;
+        S.z = x.z;
+        S.ps = 0.0;
+    }
+}
+
+template <typename T, int G>
+__device__ __forceinline__ void slot_finish(Slot<T> &S, int lane, int tb, T *pot) {
+    T a;
+    if constexpr (sizeof(T) == 4)
+        a = S.ps.x + S.ps.y;
+    else
+        a = S.ps;
 #pragma unroll
     for (int o = 1; o < G; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
     if (lane % G == 0 && S.ti >= 0) pot[S.ti - tb] = a;
 }
 
-template <bool SELF>
-__device__ __forceinline__ void accumulate_slots(const float *sx, const float *sy, const float *sz, const float *sw,
-                                                 int cnt, int sb, int lane, const bool (&on)[5], SlotF (&S)[5],
-                                                 float eps2) {
-    if (on[0]) accumulate_slot<1, SELF>(sx, sy, sz, sw, cnt, sb, 0, S[0], eps2);
-    if (on[1]) accumulate_slot<1, SELF>(sx, sy, sz, sw, cnt, sb, 0, S[1], eps2);
-    if (on[2]) accumulate_slot<2, SELF>(sx, sy, sz, sw, cnt, sb, lane % 2, S[2], eps2);
-    if (on[3]) accumulate_slot<4, SELF>(sx, sy, sz, sw, cnt, sb, lane % 4, S[3], eps2);
-    if (on[4]) accumulate_slot<8, SELF>(sx, sy, sz, sw, cnt, sb, lane % 8, S[4], eps2);
+template <typename T, bool SELF, typename C>
+__device__ __forceinline__ void accumulate_slots(const C *chunk, int cnt, int sb, int lane, const bool (&on)[5],
+                                                 Slot<T> (&S)[5], T eps2) {
+    if (on[0]) accumulate_slot<1, SELF>(chunk, cnt, sb, 0, S[0], eps2);
+    if (on[1]) accumulate_slot<1, SELF>(chunk, cnt, sb, 0, S[1], eps2);
+    if (on[2]) accumulate_slot<2, SELF>(chunk, cnt, sb, lane % 2, S[2], eps2);
+    if (on[3]) accumulate_slot<4, SELF>(chunk, cnt, sb, lane % 4, S[3], eps2);
+    if (on[4]) accumulate_slot<8, SELF>(chunk, cnt, sb, lane % 8, S[4], eps2);
 }
 
 // Targets tb..te-1 (at most 64) of leaf t: near field by slots, then the
-// local expansion and the epilogue with one lane per target.
-__device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, int tb, int te, float4 *sp, float *pot,
-                                           const Cplx<float> *sL) {
+// local expansion and the epilogue with one lane per target.  Source chunks
+// of up to 64 points (one leaf, or a 64-point piece of a larger one) are
+// staged in shared memory (FP32 as x / y / z / q arrays, FP64 as points).
+// The leaf ids and ranges of the row are read 32 entries at a time (one per
+// lane) and broadcast by shuffles, and the next chunk's points are loaded
+// before the current chunk is computed, so the dependent global loads
+// overlap the arithmetic.
+template <typename T>
+__device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb, int te,
+                                           typename Vec4<T>::type *sp, T *pot, const Cplx<T> *sL) {
+    using T4 = typename Vec4<T>::type;
     const int lane = threadIdx.x & 31;
     const int nt = te - tb;
     bool on[5];
@@ -205,51 +227,48 @@ __device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, in
         on[4] = (rem & 4) != 0;
         base[4] = o;
     }
-    SlotF S[5];
-    slot_init<1>(P, tb, te, base[0], lane, S[0]);
-    slot_init<1>(P, tb, te, base[1], lane, S[1]);
-    slot_init<2>(P, tb, te, base[2], lane, S[2]);
-    slot_init<4>(P, tb, te, base[3], lane, S[3]);
-    slot_init<8>(P, tb, te, base[4], lane, S[4]);
+    Slot<T> S[5];
+    slot_init<T, 1>(P, tb, te, base[0], lane, S[0]);
+    slot_init<T, 1>(P, tb, te, base[1], lane, S[1]);
+    slot_init<T, 2>(P, tb, te, base[2], lane, S[2]);
+    slot_init<T, 4>(P, tb, te, base[3], lane, S[3]);
+    slot_init<T, 8>(P, tb, te, base[4], lane, S[4]);
     if (P.near) {
-        // Source chunks of up to 64 points (one leaf, or a 64-point piece of
-        // a larger one) staged as x / y / z / q arrays.  The leaf ids and
-        // ranges of the row are read 32 entries at a time (one per lane) and
-        // broadcast by shuffles, and the next chunk's points are loaded
-        // before the current chunk is computed, so the dependent global
-        // loads overlap the arithmetic.
-        float *sx = reinterpret_cast<float *>(sp), *sy = sx + 64, *sz = sx + 128, *sw = sx + 192;
-        const float eps2 = P.eps2;
+        const T eps2 = P.eps2;
         const int kbeg = P.off[t], kend = P.off[t + 1];
         int kb = kbeg, s_l = 0, sa_l = 0, se_l = 0;
-        auto load_batch = [&](int base) {
-            kb = base;
-            const int k = base + lane;
+        auto load_batch = [&](int b0) {
+            kb = b0;
+            const int k = b0 + lane;
             s_l = k < kend ? P.src[k] : 0;
             const int2 r = k < kend ? P.srange[s_l] : make_int2(0, 0);
             sa_l = r.x;
             se_l = r.y;
         };
-        auto fetch = [&](int sb, int se, int i) {
-            return i < se - sb ? P.spts[sb + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        };
+        auto fetch = [&](int sb, int se, int i) { return i < se - sb ? P.spts[sb + i] : T4{0, 0, 0, 0}; };
         if (kbeg < kend) {
             load_batch(kbeg);
             int k = kbeg;
             int s = __shfl_sync(0xffffffffu, s_l, 0), sb = __shfl_sync(0xffffffffu, sa_l, 0),
                 se = __shfl_sync(0xffffffffu, se_l, 0);
-            float4 qa = fetch(sb, se, lane), qb = fetch(sb, se, lane + 32);
+            T4 qa = fetch(sb, se, lane), qb = fetch(sb, se, lane + 32);
             while (true) {
                 const int cs = s, csb = sb, cnt = min(64, se - sb);
                 __syncwarp();
-                sx[lane] = qa.x;
-                sy[lane] = qa.y;
-                sz[lane] = qa.z;
-                sw[lane] = qa.w;
-                sx[lane + 32] = qb.x;
-                sy[lane + 32] = qb.y;
-                sz[lane + 32] = qb.z;
-                sw[lane + 32] = qb.w;
+                if constexpr (sizeof(T) == 4) {
+                    float *sx = reinterpret_cast<float *>(sp);
+                    sx[lane] = qa.x;
+                    sx[64 + lane] = qa.y;
+                    sx[128 + lane] = qa.z;
+                    sx[192 + lane] = qa.w;
+                    sx[lane + 32] = qb.x;
+                    sx[64 + lane + 32] = qb.y;
+                    sx[128 + lane + 32] = qb.z;
+                    sx[192 + lane + 32] = qb.w;
+                } else {
+                    sp[lane] = qa;
+                    sp[lane + 32] = qb;
+                }
                 __syncwarp();
                 bool more = true;
                 if (sb + 64 < se) {
@@ -266,36 +285,44 @@ __device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, in
                     qa = fetch(sb, se, lane);
                     qb = fetch(sb, se, lane + 32);
                 }
-                if (P.same && cs == t)
-                    accumulate_slots<true>(sx, sy, sz, sw, cnt, csb, lane, on, S, eps2);
-                else
-                    accumulate_slots<false>(sx, sy, sz, sw, cnt, csb, lane, on, S, eps2);
+                if constexpr (sizeof(T) == 4) {
+                    const float *sx = reinterpret_cast<const float *>(sp);
+                    if (P.same && cs == t)
+                        accumulate_slots<T, true>(sx, cnt, csb, lane, on, S, eps2);
+                    else
+                        accumulate_slots<T, false>(sx, cnt, csb, lane, on, S, eps2);
+                } else {
+                    if (P.same && cs == t)
+                        accumulate_slots<T, true>(sp, cnt, csb, lane, on, S, eps2);
+                    else
+                        accumulate_slots<T, false>(sp, cnt, csb, lane, on, S, eps2);
+                }
                 if (!more) break;
             }
         }
     }
-    slot_finish<1>(S[0], lane, tb, pot);
-    slot_finish<1>(S[1], lane, tb, pot);
-    slot_finish<2>(S[2], lane, tb, pot);
-    slot_finish<4>(S[3], lane, tb, pot);
-    slot_finish<8>(S[4], lane, tb, pot);
+    slot_finish<T, 1>(S[0], lane, tb, pot);
+    slot_finish<T, 1>(S[1], lane, tb, pot);
+    slot_finish<T, 2>(S[2], lane, tb, pot);
+    slot_finish<T, 4>(S[3], lane, tb, pot);
+    slot_finish<T, 8>(S[4], lane, tb, pot);
     __syncwarp();
-    float4 c;
-    float ia = 1.0f;
+    T4 c;
+    T ia = (T)1;
     if (P.far) {
         c = P.center[t];
-        ia = 1.0f / P.half[t].w;
+        ia = (T)1 / P.half[t].w;
     }
     for (int i = lane; i < nt; i += 32) {
         const int ti = tb + i;
-        const float4 x = P.pts[ti];
-        float v = P.near ? pot[i] : 0.0f;
-        if (P.far) v += l2p_point<float>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
+        const T4 x = P.pts[ti];
+        T v = P.near ? pot[i] : (T)0;
+        if (P.far) v += l2p_point<T>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
         if (P.scatter) {
             const int o = P.index_map[ti];
             v = v * P.k_e;
             if (P.self_int) v += P.self_int[o] * P.sigma[o] * P.areas[o];
-            if (!isfinite(v)) v = 0.0f;
+            if (!isfinite(v)) v = (T)0;
             P.out[o] = v;
         } else {
             P.out[ti] = v;
@@ -304,74 +331,11 @@ __device__ __forceinline__ void leaf_slots(const NearParams<float> &P, int t, in
     __syncwarp();
 }
 
-// FP64: one block of up to 32 * TPL / G targets of leaf t.  With G > 1 (small
-// leaves) G lanes share a target, each taking every G-th source of a chunk,
-// and their sums are combined with a fixed shuffle tree.
-template <typename T, int TPL, int G>
-__device__ __forceinline__ void leaf_block(const NearParams<T> &P, int t, int tb, int te, typename Vec4<T>::type *sp,
-                                           const Cplx<T> *sL) {
-    static_assert(G == 1 || TPL == 1, "lane groups are used for single-target lanes only");
+template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 4) k_p2p_l2p(const NearParams<T> P) {
     using T4 = typename Vec4<T>::type;
-    const int lane = threadIdx.x & 31;
-    const int part = lane % G;
-    T4 x[2];
-    int ti[2];
-    bool valid[2];
-    T acc[2] = {(T)0, (T)0};
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        ti[u] = tb + lane / G + 32 * u;
-        valid[u] = u < TPL && ti[u] < te;
-        x[u] = valid[u] ? P.pts[ti[u]] : P.pts[tb];
-    }
-    if (P.near) {
-        const int e = P.off[t + 1];
-        for (int k = P.off[t]; k < e; ++k) {
-            const int s = P.src[k];
-            const int2 sr = P.srange[s];
-            for (int sb = sr.x; sb < sr.y; sb += 32) {
-                const int cnt = min(32, sr.y - sb);
-                __syncwarp();
-                if (lane < cnt) sp[lane] = P.spts[sb + lane];
-                __syncwarp();
-                if (P.same && s == t)
-                    accumulate_chunk<T, TPL, G, true>(sp, cnt, sb, part, x, ti, P.eps2, acc);
-                else
-                    accumulate_chunk<T, TPL, G, false>(sp, cnt, sb, part, x, ti, P.eps2, acc);
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
-    if (part != 0) return;
-    T4 c;
-    T ia = (T)1;
-    if (P.far) {
-        c = P.center[t];
-        ia = (T)1 / P.half[t].w;
-    }
-#pragma unroll
-    for (int u = 0; u < TPL; ++u) {
-        if (!valid[u]) continue;
-        T v = acc[u];
-        if (P.far) v += l2p_point<T>(sL, P.p, (x[u].x - c.x) * ia, (x[u].y - c.y) * ia, (x[u].z - c.z) * ia);
-        if (P.scatter) {
-            const int o = P.index_map[ti[u]];
-            v = v * P.k_e;
-            if (P.self_int) v += P.self_int[o] * P.sigma[o] * P.areas[o];
-            if (!isfinite(v)) v = (T)0;
-            P.out[o] = v;
-        } else {
-            P.out[ti[u]] = v;
-        }
-    }
-}
-
-template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 1) k_p2p_l2p(const NearParams<T> P) {
-    using T4 = typename Vec4<T>::type;
-    __shared__ T4 sp[4][64];  // FP32: a staged chunk of up to 64 sources; FP64: up to 32
+    __shared__ T4 sp[4][64];  // a staged chunk of up to 64 sources
     __shared__ Cplx<T> sL[4][ncoef(kPMax)];
-    __shared__ float spot[4][64];  // FP32: the near-field sums of a block of targets
+    __shared__ T spot[4][64];  // the near-field sums of a block of targets
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t w = (int64_t)blockIdx.x * 4 + wl;
     if (w >= P.n_leaves) return;
@@ -382,19 +346,7 @@ template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 
         __syncwarp();
     }
     const int2 rg = P.range[t];
-    const int nt = rg.y - rg.x;
-    if constexpr (sizeof(T) == 4) {
-        for (int tb = rg.x; tb < rg.y; tb += 64)
-            leaf_slots(P, t, tb, min(rg.y, tb + 64), sp[wl], spot[wl], sL[wl]);
-    } else if (nt <= 8) {
-        leaf_block<T, 1, 4>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
-    } else if (nt <= 16) {
-        leaf_block<T, 1, 2>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
-    } else if (nt <= 32) {
-        leaf_block<T, 1, 1>(P, t, rg.x, rg.y, sp[wl], sL[wl]);
-    } else {
-        for (int tb = rg.x; tb < rg.y; tb += 64) leaf_block<T, 2, 1>(P, t, tb, min(rg.y, tb + 64), sp[wl], sL[wl]);
-    }
+    for (int tb = rg.x; tb < rg.y; tb += 64) leaf_slots<T>(P, t, tb, min(rg.y, tb + 64), sp[wl], spot[wl], sL[wl]);
 }
 
 }  // namespace
