@@ -567,8 +567,15 @@ def run_batch_workload(args, rank, world, local):
     t_setup = time.perf_counter() - t0
     tune = autotune_inner(system)
     result = {}
+    net = None
+    weights = os.path.join(ROOT, "electrodrive_gb300", "data", "pcn_weights.npz")
+    if os.path.exists(weights):
+        from electrodrive_gb300.core.warm_start import PointCloudNet
+
+        net = PointCloudNet.load(weights, device=dev)
 
     def step():
+        # zero start: the first residual is b itself (no operator application)
         result["x"], result["info"] = system.solve()
 
     warm = max(args.warmup, 3)
@@ -583,6 +590,12 @@ def run_batch_workload(args, rank, world, local):
     value = world * K * 1e3 / ms
     info = result["info"]
     per = system.residuals(result["x"]).cpu().numpy()
+    learned = {}
+
+    def learned_step():
+        # per-instance learned warm start (network + one FP32 application) inside the timing
+        learned["x"], learned["info"] = system.solve(x0=system.learned_start(net))
+    t_learned = _time_cuda(learned_step, dev, stream, flush, 1, 1)[0] if net is not None else None
     mv = {"float64": statistics.median(_time_cuda(lambda: system.op64(system.x0_cold), dev, stream, flush, 1, 3)),
           "float32": statistics.median(_time_cuda(lambda: system.op32(system.x0_cold.float()), dev, stream, flush,
                                                   1, 3))}
@@ -638,7 +651,12 @@ def run_batch_workload(args, rank, world, local):
                              "seconds_timed": sum(p["seconds"] for p in plain_ee),
                              "seconds_all_extrapolated_by_panels": t_plain_ee_all,
                              "solves_per_s": K / t_plain_ee_all},
-                         "speedup_vs_plain_fp64_early_exit": t_plain_ee_all / (ms * 1e-3)},
+                         "speedup_vs_plain_fp64_early_exit": t_plain_ee_all / (ms * 1e-3),
+                         "learned_start": None if t_learned is None else {
+                             "ms": t_learned, "solves_per_s": world * K * 1e3 / t_learned,
+                             "outer_iters": learned["info"]["outer"], "inner_iters": learned["info"]["inner_iters"],
+                             "fp64_matvecs": learned["info"]["matvec64"],
+                             "instance_inner_iters_mean": float(np.mean(learned["info"]["instance_inner_iters"]))}},
                "autotune_trials": tune["trials"], "matvec_ms": mv,
                "e2e": {"value": world * K * 1e3 / e2e_ms, "unit": "solves/s",
                        "h2d_bytes_per_step": int(n_total * 8 * (3 + 1 + 9)), "d2h_bytes_per_step": int(8 * n_total),

@@ -90,6 +90,8 @@ class BatchSystem:
         self.n = int(self.offsets[-1])
         C = np.concatenate([m.centroids for m, _ in self.cases])
         A = np.concatenate([m.areas for m, _ in self.cases])
+        self.normals = torch.as_tensor(np.concatenate([m.normals for m, _ in self.cases]), dtype=torch.float64,
+                                       device=dev)
         PV = np.concatenate([m.vertices[m.triangles] for m, _ in self.cases])
         self.C64 = torch.as_tensor(C, dtype=torch.float64, device=dev)
         self.areas = torch.as_tensor(A, dtype=torch.float64, device=dev)
@@ -121,6 +123,21 @@ class BatchSystem:
         Jacobi-preconditioned inner solve reaches in its first step anyway)."""
         return solve_mixed(self.op64, self.op32, self.b, A_diag=self.diag, x0=x0, rtol=rtol,
                            segments=self.offsets, inner_restart=inner_restart, **kw)
+
+    def learned_start(self, net) -> Tensor:
+        """Per-instance learned warm start x0 = s (1 + y) (core.warm_start):
+        s = b / A(1) from one FP32 application of the batched operator (block
+        diagonal, so every instance gets its own), y from the network run on
+        each instance's panels (its context is pooled over that instance)."""
+        from .warm_start import base_guess
+
+        s = base_guess(self.op32, self.b)
+        y = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        for k in range(len(self.cases)):
+            a, e = self.offsets[k], self.offsets[k + 1]
+            f = net.features(self.C64[a:e], self.normals[a:e], self.areas[a:e], self.b[a:e])
+            y[a:e] = net.forward(f).to(torch.float64)
+        return s * (1.0 + y)
 
     def residuals(self, x: Tensor) -> Tensor:
         """Each instance's relative FP64 true residual."""

@@ -103,3 +103,29 @@ def test_batched_dimer_solve_meets_the_tolerance_per_instance(cuda_lib):
         assert rd < 5e-6, (k, rd)
         err = float(torch.linalg.norm(xk - ref) / torch.linalg.norm(ref))
         assert err < 5e-4, (k, err)
+
+
+def test_batched_learned_start_equals_per_instance_warm_start(cuda_lib):
+    """BatchSystem.learned_start gives every instance the warm start that
+    core.warm_start.warm_start gives it alone (same network, same FP32
+    operator rows), and it starts much closer than the cold start."""
+    import os
+
+    from electrodrive_gb300.core.batch import BatchSystem, dimer_case
+    from electrodrive_gb300.core.bem import assemble_system, segment_norms
+    from electrodrive_gb300.core.warm_start import PointCloudNet, warm_start
+
+    weights = os.path.join(os.path.dirname(__file__), "..", "electrodrive_gb300", "data", "pcn_weights.npz")
+    net = PointCloudNet.load(weights, device="cuda")
+    cases = [dimer_case(200 + i, n) for i, n in enumerate([1200, 2000, 1600])]
+    system = BatchSystem(cases, leaf_size=64)
+    x0 = system.learned_start(net)
+    for k, (mesh, spec) in enumerate(cases):
+        sysd = assemble_system(mesh, spec, kind="fmm", dtypes=(torch.float32,))
+        xs = warm_start(net, mesh, sysd["b"], sysd["ops"][torch.float32])
+        a, b = system.offsets[k], system.offsets[k + 1]
+        assert float(torch.linalg.norm(x0[a:b] - xs) / torch.linalg.norm(xs)) < 1e-6, k
+    bn = segment_norms(system.b, system.offsets)
+    r_learned = segment_norms(system.b - system.op64(x0), system.offsets) / bn
+    r_cold = segment_norms(system.b - system.op64(system.x0_cold), system.offsets) / bn
+    assert bool((r_learned < r_cold).all()), (r_learned, r_cold)
