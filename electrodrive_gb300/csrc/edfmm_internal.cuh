@@ -211,6 +211,7 @@ struct NearArgs {
     bool scatter = false;             // write out[index_map[i]] with k_e, self term, clamp
     bool near = true;                 // include P2P
     bool far = true;                  // include L2P
+    const void *add_in = nullptr;     // tree-order sums added before the epilogue (nullable)
     // sources of the P2P when they are another tree's points (targets
     // evaluated against a source plan): no self exclusion then
     const struct DevTree *src_tree = nullptr;
@@ -229,4 +230,17 @@ struct edfmm_plan {
     int leaf_size = 64;
     int max_depth = 32;
     int device = 0;
+    // matvec: the near field runs on a second stream beside the far-field
+    // chain (fork / join events) into tree-order sums, created on first use
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    edfmm::DevBuf near_sum;
+    edfmm_plan() = default;
+    edfmm_plan(const edfmm_plan &) = delete;
+    edfmm_plan &operator=(const edfmm_plan &) = delete;
+    ~edfmm_plan() {
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
+    }
 };

@@ -83,6 +83,7 @@ template <typename T> struct NearParams {
     T eps2;
     int near;
     int far;
+    const T *add_in;  // tree-order near sums computed by an earlier pass (nullable)
     // epilogue
     int scatter;
     const int32_t *index_map;
@@ -317,6 +318,7 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
         const int ti = tb + i;
         const T4 x = P.pts[ti];
         T v = P.near ? pot[i] : (T)0;
+        if (P.add_in) v += P.add_in[ti];
         if (P.far) v += l2p_point<T>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
         if (P.scatter) {
             const int o = P.index_map[ti];
@@ -393,6 +395,7 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     P.eps2 = eps * eps;
     P.near = a.near ? 1 : 0;
     P.far = a.far ? 1 : 0;
+    P.add_in = static_cast<const T *>(a.add_in);
     P.scatter = a.scatter ? 1 : 0;
     P.index_map = dptr<int32_t>(tree.index_map);
     P.sigma = static_cast<const T *>(a.sigma);

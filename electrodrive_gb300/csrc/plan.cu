@@ -376,6 +376,43 @@ int edfmm_plan_matvec(edfmm_plan *p, const void *sigma, const void *areas, const
     int rc;
     if (swapped && (rc = lists_build_swapped(p->tree, p->lists, s))) return rc;
     if ((rc = set_charges(p->tree, sigma, areas, s))) return rc;
+    if (far && near) {
+        // The near field depends only on the charges: it runs on a second
+        // stream beside P2M -> M2M -> M2L -> L2L, into tree-order sums that
+        // the final pass (L2P + epilogue) adds.  Fork and join through
+        // events, so the pattern is also valid inside a stream capture.
+        if (!p->side) {
+            EDFMM_CUDA_TRY(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+            EDFMM_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+            EDFMM_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+        }
+        const size_t elt = p->tree.dtype == EDFMM_F64 ? sizeof(double) : sizeof(float);
+        if ((rc = p->near_sum.reserve(elt * (size_t)p->tree.n_points))) return rc;
+        EDFMM_CUDA_TRY(cudaEventRecord(p->ev_fork, s));
+        EDFMM_CUDA_TRY(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+        NearArgs an;
+        an.out = p->near_sum.p;
+        an.scatter = false;
+        an.near = true;
+        an.far = false;
+        if ((rc = run_p2p_l2p(p->tree, p->lists, p->fmm, an, p->side))) return rc;
+        EDFMM_CUDA_TRY(cudaEventRecord(p->ev_join, p->side));
+        if ((rc = run_p2m(p->tree, p->fmm, s)) || (rc = run_m2m(p->tree, p->fmm, s)) ||
+            (rc = run_m2l(p->tree, p->lists, p->fmm, swapped, s)) || (rc = run_l2l(p->tree, p->fmm, s)))
+            return rc;
+        EDFMM_CUDA_TRY(cudaStreamWaitEvent(s, p->ev_join, 0));
+        NearArgs a;
+        a.sigma = sigma;
+        a.areas = areas;
+        a.self_int = self_integrals;
+        a.k_e = k_e;
+        a.out = out;
+        a.scatter = true;
+        a.near = false;
+        a.far = true;
+        a.add_in = p->near_sum.p;
+        return run_p2p_l2p(p->tree, p->lists, p->fmm, a, s);
+    }
     if (far) {
         if ((rc = run_p2m(p->tree, p->fmm, s)) || (rc = run_m2m(p->tree, p->fmm, s)) ||
             (rc = run_m2l(p->tree, p->lists, p->fmm, swapped, s)) || (rc = run_l2l(p->tree, p->fmm, s)))
