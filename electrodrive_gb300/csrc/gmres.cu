@@ -1,15 +1,19 @@
 // Device-side Krylov arithmetic of restarted, left-preconditioned GMRES
 // (the reference's gmres_restart, electrodrive/core/bem_solver.py:125-920).
 //
-// Vectors are in the working dtype T (float or double); every inner product,
-// norm, Hessenberg entry, Givens rotation and the small triangular solve are
-// carried in FP64 on the device, so the host reads nothing until the end of
-// a restart cycle and a whole cycle can be replayed as one CUDA graph.
+// Vectors are in the working dtype T (float or double).  Elementwise work
+// (products, updates, the partial sums of a thread or lane) is done in T;
+// the reductions across lanes and blocks, every Hessenberg entry, Givens
+// rotation and the small triangular solve are carried in FP64 on the device
+// (FP64 arithmetic is scarce on this GPU, so it is kept off the per-element
+// path), so the host reads nothing until the end of a restart cycle and a
+// whole cycle can be replayed as one CUDA graph.
 // Orthogonalisation is classical Gram-Schmidt applied twice (CGS2): per
 // Arnoldi step two batched projections instead of the reference's j+1
 // sequential modified-Gram-Schmidt passes; in exact arithmetic the basis is
 // the same.  Reductions are deterministic: each block writes a partial sum
-// and the last block to finish adds the partials in block order.
+// and the partials are added in a fixed order (by a separate kernel, or by
+// the last block to finish).
 //
 // Layout: V is (restart + 1, n) row-major in T; H is (restart + 1, restart)
 // row-major FP64; g, cs, sn are FP64 vectors; `scal` (FP64) holds
@@ -78,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) k_start(int64_t n, const T *__restri
                                                     int restart, double *scal, void *work) {
     __shared__ double sm[32];
     Work W = work_view(work, restart);
-    double s_true = 0, s_pre = 0;
+    T s_true = 0, s_pre = 0;  // per-thread sums of kItems squares in T, then FP64
     const int64_t base = (int64_t)blockIdx.x * kChunkN;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
@@ -87,23 +91,25 @@ __global__ void __launch_bounds__(kThreads) k_start(int64_t n, const T *__restri
             const T rt = b[i] - ax[i];
             const T r = pinv ? pinv[i] * rt : rt;
             v0[i] = r;
-            s_true += (double)rt * (double)rt;
-            s_pre += (double)r * (double)r;
+            s_true += rt * rt;
+            s_pre += r * r;
         }
     }
-    double a = block_sum(s_true, sm);
-    double c = block_sum(s_pre, sm);
+    double a = block_sum((double)s_true, sm);
+    double c = block_sum((double)s_pre, sm);
     if (threadIdx.x == 0) {
         W.part[2 * blockIdx.x] = a;
         W.part[2 * blockIdx.x + 1] = c;
     }
     if (!last_block(W.counter)) return;
+    double ta = 0, tc = 0;
+    for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) {
+        ta += __ldcg(&W.part[2 * q]);
+        tc += __ldcg(&W.part[2 * q + 1]);
+    }
+    ta = block_sum(ta, sm);
+    tc = block_sum(tc, sm);
     if (threadIdx.x == 0) {
-        double ta = 0, tc = 0;
-        for (unsigned q = 0; q < gridDim.x; ++q) {
-            ta += __ldcg(&W.part[2 * q]);
-            tc += __ldcg(&W.part[2 * q + 1]);
-        }
         scal[0] = sqrt(ta);
         scal[1] = sqrt(tc);
         scal[2] = -1.0;
@@ -115,31 +121,39 @@ __global__ void __launch_bounds__(kThreads) k_start(int64_t n, const T *__restri
     }
 }
 
-// v <- v / scal[idx] (skipped when that value is 0 or not finite)
+// v <- v / scal[idx] (skipped when that value is 0 or not finite), as a
+// multiplication by the reciprocal taken once per block in FP64
 template <typename T>
 __global__ void k_scale_by(int64_t n, T *v, const T *src, const double *scal, int idx) {
+    __shared__ double inv;
+    if (threadIdx.x == 0) {
+        const double d = scal[idx];
+        inv = (d > 0.0 && isfinite(d)) ? 1.0 / d : 1.0;
+    }
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double d = scal[idx];
-    const T x = src[i];
-    v[i] = (d > 0.0 && isfinite(d)) ? (T)((double)x / d) : x;
+    v[i] = src[i] * (T)inv;
 }
 
-// h[i] = <V_i, w> for i <= j (w = pinv * av on the first pass, written back)
+// Partial h[r] = <V_r, w> over one chunk of kChunkN rows per block, r <= j
+// (w = pinv * av on the first pass, written back).  The chunk of w is staged
+// in shared memory and each warp takes whole rows r, so a block needs no
+// barrier per row; the partials are added by k_dots_fin.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_dots(int64_t n, int j, int restart, const T *__restrict__ V,
                                                    T *__restrict__ w, const T *__restrict__ av,
-                                                   const T *__restrict__ pinv, void *work, int pass) {
-    __shared__ double sm[32];
+                                                   const T *__restrict__ pinv, void *work) {
+    __shared__ T ws[kChunkN];
     Work W = work_view(work, restart);
-    double *h = pass == 1 ? W.h1 : W.h2;
     const int64_t base = (int64_t)blockIdx.x * kChunkN;
-    T wl[kItems];
+    const int cnt = (int)(n - base < kChunkN ? n - base : kChunkN);
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
+        const int q = k * kThreads + threadIdx.x;
+        const int64_t i = base + q;
         T x = 0;
-        if (i < n) {
+        if (q < cnt) {
             if (av) {
                 x = pinv ? pinv[i] * av[i] : av[i];
                 w[i] = x;
@@ -147,27 +161,35 @@ __global__ void __launch_bounds__(kThreads) k_dots(int64_t n, int j, int restart
                 x = w[i];
             }
         }
-        wl[k] = x;
-    }
-    for (int r = 0; r <= j; ++r) {
-        const T *vr = V + (int64_t)r * n;
-        double s = 0;
-#pragma unroll
-        for (int k = 0; k < kItems; ++k) {
-            const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
-            if (i < n) s += (double)vr[i] * (double)wl[k];
-        }
-        s = block_sum(s, sm);
-        if (threadIdx.x == 0) W.part[(int64_t)blockIdx.x * (restart + 1) + r] = s;
-    }
-    if (!last_block(W.counter)) return;
-    for (int r = threadIdx.x; r <= j; r += blockDim.x) {
-        double t = 0;
-        for (unsigned q = 0; q < gridDim.x; ++q) t += __ldcg(&W.part[(int64_t)q * (restart + 1) + r]);
-        h[r] = t;
+        ws[q] = x;
     }
     __syncthreads();
-    if (threadIdx.x == 0) *W.counter = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = wid; r <= j; r += kThreads / 32) {
+        const T *vr = V + (int64_t)r * n + base;
+        T sl = 0;  // a lane's 32 products in T, then FP64 across lanes and blocks
+#pragma unroll 8
+        for (int q = lane; q < cnt; q += 32) sl += vr[q] * ws[q];
+        double s = (double)sl;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) W.part[(int64_t)blockIdx.x * (restart + 1) + r] = s;
+    }
+}
+
+// h[r] = sum of the blocks' partials (fixed order: lane-strided sums, then a
+// fixed shuffle tree); one warp per row r, one block of 32 warps
+__global__ void __launch_bounds__(1024) k_dots_fin(int nb, int j, int restart, void *work, int pass) {
+    Work W = work_view(work, restart);
+    double *h = pass == 1 ? W.h1 : W.h2;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = wid; r <= j; r += 32) {
+        double t = 0;
+        for (int q = lane; q < nb; q += 32) t += W.part[(int64_t)q * (restart + 1) + r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) h[r] = t;
+    }
 }
 
 // w -= sum_i h[i] V_i; on the second pass also |w| -> H[j+1, j] via scal
@@ -175,31 +197,31 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_sub(int64_t n, int j, int restart, const T *__restrict__ V,
                                                   T *__restrict__ w, void *work, int pass, double *H) {
     __shared__ double sm[32];
-    __shared__ double hs[257];
+    __shared__ T hs[257];
     Work W = work_view(work, restart);
     const double *h = pass == 1 ? W.h1 : W.h2;
-    for (int r = threadIdx.x; r <= j; r += blockDim.x) hs[r] = h[r];
+    for (int r = threadIdx.x; r <= j; r += blockDim.x) hs[r] = (T)h[r];
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * kChunkN;
-    double s2 = 0;
+    T s2 = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
         if (i < n) {
-            double x = (double)w[i];
-            for (int r = 0; r <= j; ++r) x -= hs[r] * (double)V[(int64_t)r * n + i];
-            const T xt = (T)x;
-            w[i] = xt;
-            s2 += (double)xt * (double)xt;
+            T x = w[i];
+            for (int r = 0; r <= j; ++r) x -= hs[r] * V[(int64_t)r * n + i];
+            w[i] = x;
+            s2 += x * x;
         }
     }
     if (pass == 1) return;
-    s2 = block_sum(s2, sm);
-    if (threadIdx.x == 0) W.part[blockIdx.x] = s2;
+    double s2d = block_sum((double)s2, sm);
+    if (threadIdx.x == 0) W.part[blockIdx.x] = s2d;
     if (!last_block(W.counter)) return;
+    double t = 0;
+    for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) t += __ldcg(&W.part[q]);
+    t = block_sum(t, sm);
     if (threadIdx.x == 0) {
-        double t = 0;
-        for (unsigned q = 0; q < gridDim.x; ++q) t += __ldcg(&W.part[q]);
         H[(int64_t)(j + 1) * restart + j] = sqrt(t);
         *W.counter = 0;
     }
@@ -207,38 +229,48 @@ __global__ void __launch_bounds__(kThreads) k_sub(int64_t n, int j, int restart,
 
 // Hessenberg column j = h1 + h2, Givens rotations, g update, residual estimate.
 // Mirrors bem_solver.py:590-616 (rotation with denom < 1e-14 -> identity).
+// The column is gathered into shared memory by the warp, rotated by one
+// thread there (a dependent chain through shared memory, not global), and
+// written back by the warp.
 __global__ void k_givens(int j, int restart, double *H, double *g, double *cs, double *sn, double *scal, void *work) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    __shared__ double col[258];
+    if (blockIdx.x != 0) return;
     Work W = work_view(work, restart);
-    for (int i = 0; i <= j; ++i) H[(int64_t)i * restart + j] = W.h1[i] + W.h2[i];
-    const double hn = H[(int64_t)(j + 1) * restart + j];
-    if (!(isfinite(hn) && hn > 0.0)) {
-        if (scal[2] < 0) scal[2] = (double)j;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) col[i] = W.h1[i] + W.h2[i];
+    if (threadIdx.x == 0) col[j + 1] = H[(int64_t)(j + 1) * restart + j];
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        const double hn = col[j + 1];
+        if (!(isfinite(hn) && hn > 0.0)) {
+            if (scal[2] < 0) scal[2] = (double)j;
+        }
+        for (int i = 0; i < j; ++i) {
+            const double a = col[i], b = col[i + 1];
+            col[i] = cs[i] * a + sn[i] * b;
+            col[i + 1] = -sn[i] * a + cs[i] * b;
+        }
+        const double a = col[j], b = col[j + 1];
+        const double den = sqrt(a * a + b * b);
+        double c = 1.0, s = 0.0;
+        if (den >= 1e-14 && isfinite(den)) {
+            c = a / den;
+            s = b / den;
+        }
+        cs[j] = c;
+        sn[j] = s;
+        col[j] = c * a + s * b;
+        col[j + 1] = 0.0;
+        const double gj = g[j];
+        g[j] = c * gj;
+        g[j + 1] = -s * gj;
+        const double rn = fabs(g[j + 1]);
+        scal[4 + j] = rn;
+        if (!isfinite(rn)) scal[3] = 1.0;
+        // keep the unrotated subdiagonal for the basis scaling
+        scal[4 + restart] = hn;
     }
-    for (int i = 0; i < j; ++i) {
-        const double a = H[(int64_t)i * restart + j], b = H[(int64_t)(i + 1) * restart + j];
-        H[(int64_t)i * restart + j] = cs[i] * a + sn[i] * b;
-        H[(int64_t)(i + 1) * restart + j] = -sn[i] * a + cs[i] * b;
-    }
-    const double a = H[(int64_t)j * restart + j], b = H[(int64_t)(j + 1) * restart + j];
-    const double den = sqrt(a * a + b * b);
-    double c = 1.0, s = 0.0;
-    if (den >= 1e-14 && isfinite(den)) {
-        c = a / den;
-        s = b / den;
-    }
-    cs[j] = c;
-    sn[j] = s;
-    H[(int64_t)j * restart + j] = c * a + s * b;
-    H[(int64_t)(j + 1) * restart + j] = 0.0;
-    const double gj = g[j];
-    g[j] = c * gj;
-    g[j + 1] = -s * gj;
-    const double rn = fabs(g[j + 1]);
-    scal[4 + j] = rn;
-    if (!isfinite(rn)) scal[3] = 1.0;
-    // keep the unrotated subdiagonal for the basis scaling
-    scal[4 + restart] = hn;
+    __syncwarp();
+    for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) H[(int64_t)i * restart + j] = col[i];
 }
 
 // y = R^{-1} g[0:m] (upper triangular, FP64)
@@ -256,15 +288,15 @@ __global__ void k_trsv(int m, int restart, const double *H, const double *g, voi
 // x += V[0:m]^T y
 template <typename T>
 __global__ void k_update(int64_t n, int m, int restart, const T *__restrict__ V, T *__restrict__ x, void *work) {
-    __shared__ double ys[256];
+    __shared__ T ys[256];
     Work W = work_view(work, restart);
-    for (int r = threadIdx.x; r < m; r += blockDim.x) ys[r] = W.y[r];
+    for (int r = threadIdx.x; r < m; r += blockDim.x) ys[r] = (T)W.y[r];
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double acc = (double)x[i];
-    for (int r = 0; r < m; ++r) acc += ys[r] * (double)V[(int64_t)r * n + i];
-    x[i] = (T)acc;
+    T acc = x[i];
+    for (int r = 0; r < m; ++r) acc += ys[r] * V[(int64_t)r * n + i];
+    x[i] = acc;
 }
 
 }  // namespace
@@ -289,12 +321,16 @@ int gmres_arnoldi(int64_t n, int j, int restart, void *V, const void *av, const 
                   void *sn, void *scal, void *w, void *work, cudaStream_t s) {
     const unsigned nb = nblocks(n);
     T *Vt = (T *)V;
-    k_dots<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, (const T *)av, (const T *)pinv, work, 1);
+    k_dots<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, (const T *)av, (const T *)pinv, work);
     EDFMM_LAUNCH_CHECK("k_dots");
+    k_dots_fin<<<1, 1024, 0, s>>>((int)nb, j, restart, work, 1);
+    EDFMM_LAUNCH_CHECK("k_dots_fin");
     k_sub<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, work, 1, (double *)H);
     EDFMM_LAUNCH_CHECK("k_sub");
-    k_dots<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, nullptr, nullptr, work, 2);
+    k_dots<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, nullptr, nullptr, work);
     EDFMM_LAUNCH_CHECK("k_dots");
+    k_dots_fin<<<1, 1024, 0, s>>>((int)nb, j, restart, work, 2);
+    EDFMM_LAUNCH_CHECK("k_dots_fin");
     k_sub<T><<<nb, kThreads, 0, s>>>(n, j, restart, Vt, (T *)w, work, 2, (double *)H);
     EDFMM_LAUNCH_CHECK("k_sub");
     k_givens<<<1, 32, 0, s>>>(j, restart, (double *)H, (double *)g, (double *)cs, (double *)sn, (double *)scal, work);

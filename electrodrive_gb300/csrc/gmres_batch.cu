@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kThreads) k_bstart(BatchView W, const T *__res
     const int k = blockIdx.y, bb = blockIdx.x;
     int64_t lo, hi;
     chunk_of(W, k, bb, lo, hi);
-    double s_true = 0, s_pre = 0;
+    T s_true = 0, s_pre = 0;  // per-thread sums in T, FP64 across threads and blocks
 #pragma unroll
     for (int q = 0; q < kItems; ++q) {
         const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
@@ -86,12 +86,12 @@ __global__ void __launch_bounds__(kThreads) k_bstart(BatchView W, const T *__res
             const T rt = b[i] - ax[i];
             const T r = pinv ? pinv[i] * rt : rt;
             v0[i] = r;
-            s_true += (double)rt * (double)rt;
-            s_pre += (double)r * (double)r;
+            s_true += rt * rt;
+            s_pre += r * r;
         }
     }
-    const double a = block_sum(s_true, sm);
-    const double c = block_sum(s_pre, sm);
+    const double a = block_sum((double)s_true, sm);
+    const double c = block_sum((double)s_pre, sm);
     if (threadIdx.x == 0) {
         double *p = W.part + ((int64_t)k * W.B + bb) * (W.R + 1);
         p[0] = a;
@@ -141,33 +141,40 @@ __global__ void __launch_bounds__(kThreads) k_bscale(BatchView W, T *__restrict_
     const int k = blockIdx.y, bb = blockIdx.x;
     int64_t lo, hi;
     chunk_of(W, k, bb, lo, hi);
-    const double *S = W.row(k);
-    const bool on = S[S_ACTIVE] != 0.0;
-    const double d = S[col];
-    const bool ok = on && d > 0.0 && isfinite(d);
+    __shared__ double inv;  // the reciprocal once per block in FP64
+    if (threadIdx.x == 0) {
+        const double *S = W.row(k);
+        const double d = S[col];
+        inv = (S[S_ACTIVE] != 0.0 && d > 0.0 && isfinite(d)) ? 1.0 / d : 0.0;
+    }
+    __syncthreads();
+    const T f = (T)inv;
 #pragma unroll
     for (int q = 0; q < kItems; ++q) {
         const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
-        if (i < hi) v[i] = ok ? (T)((double)src[i] / d) : (T)0;
+        if (i < hi) v[i] = src[i] * f;
     }
 }
 
-// partial <V_r, w> for r <= j (w = pinv * av on the first pass, written back)
+// partial <V_r, w> for r <= j over the block's chunk (w = pinv * av on the
+// first pass, written back); the chunk of w is staged in shared memory and
+// each warp takes whole rows r (no barrier per row)
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bdots(BatchView W, int j, int64_t n, const T *__restrict__ V,
                                                     T *__restrict__ w, const T *__restrict__ av,
                                                     const T *__restrict__ pinv) {
-    __shared__ double sm[32];
+    __shared__ T ws[kChunk];
     const int k = blockIdx.y, bb = blockIdx.x;
     if (W.row(k)[S_ACTIVE] == 0.0) return;  // uniform over the block
     int64_t lo, hi;
     chunk_of(W, k, bb, lo, hi);
-    T wl[kItems];
+    const int cnt = hi > lo ? (int)(hi - lo) : 0;
 #pragma unroll
     for (int q = 0; q < kItems; ++q) {
-        const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
+        const int o = q * kThreads + threadIdx.x;
+        const int64_t i = lo + o;
         T x = 0;
-        if (i < hi) {
+        if (o < cnt) {
             if (av) {
                 x = pinv ? pinv[i] * av[i] : av[i];
                 w[i] = x;
@@ -175,19 +182,20 @@ __global__ void __launch_bounds__(kThreads) k_bdots(BatchView W, int j, int64_t 
                 x = w[i];
             }
         }
-        wl[q] = x;
+        ws[o] = x;
     }
+    __syncthreads();
     double *p = W.part + ((int64_t)k * W.B + bb) * (W.R + 1);
-    for (int r = 0; r <= j; ++r) {
-        const T *vr = V + (int64_t)r * n;
-        double s = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = wid; r <= j; r += kThreads / 32) {
+        const T *vr = V + (int64_t)r * n + lo;
+        T sl = 0;  // a lane's products in T, then FP64 across lanes and blocks
+#pragma unroll 8
+        for (int q = lane; q < cnt; q += 32) sl += vr[q] * ws[q];
+        double s = (double)sl;
 #pragma unroll
-        for (int q = 0; q < kItems; ++q) {
-            const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
-            if (i < hi) s += (double)vr[i] * (double)wl[q];
-        }
-        s = block_sum(s, sm);
-        if (threadIdx.x == 0) p[r] = s;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) p[r] = s;
     }
 }
 
@@ -208,29 +216,28 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bsub(BatchView W, int j, int64_t n, const T *__restrict__ V,
                                                    T *__restrict__ w, int pass) {
     __shared__ double sm[32];
-    __shared__ double hs[257];
+    __shared__ T hs[257];
     const int k = blockIdx.y, bb = blockIdx.x;
     if (W.row(k)[S_ACTIVE] == 0.0) return;
     const double *h = W.h + ((int64_t)(pass - 1) * W.K + k) * (W.R + 1);
-    for (int r = threadIdx.x; r <= j; r += blockDim.x) hs[r] = h[r];
+    for (int r = threadIdx.x; r <= j; r += blockDim.x) hs[r] = (T)h[r];
     __syncthreads();
     int64_t lo, hi;
     chunk_of(W, k, bb, lo, hi);
-    double s2 = 0;
+    T s2 = 0;
 #pragma unroll
     for (int q = 0; q < kItems; ++q) {
         const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
         if (i < hi) {
-            double x = (double)w[i];
-            for (int r = 0; r <= j; ++r) x -= hs[r] * (double)V[(int64_t)r * n + i];
-            const T xt = (T)x;
-            w[i] = xt;
-            s2 += (double)xt * (double)xt;
+            T x = w[i];
+            for (int r = 0; r <= j; ++r) x -= hs[r] * V[(int64_t)r * n + i];
+            w[i] = x;
+            s2 += x * x;
         }
     }
     if (pass == 1) return;
-    s2 = block_sum(s2, sm);
-    if (threadIdx.x == 0) W.part[((int64_t)k * W.B + bb) * (W.R + 1)] = s2;
+    const double s2d = block_sum((double)s2, sm);
+    if (threadIdx.x == 0) W.part[((int64_t)k * W.B + bb) * (W.R + 1)] = s2d;
 }
 
 // Hessenberg column j, Givens rotations, estimate, and the instance's exit
@@ -314,10 +321,10 @@ __global__ void k_btrsv(BatchView W) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bupdate(BatchView W, int m, int64_t n, const T *__restrict__ V,
                                                       T *__restrict__ x) {
-    __shared__ double ys[256];
+    __shared__ T ys[256];
     const int k = blockIdx.y, bb = blockIdx.x;
     const double *y = W.y + (int64_t)k * W.R;
-    for (int r = threadIdx.x; r < m; r += blockDim.x) ys[r] = y[r];
+    for (int r = threadIdx.x; r < m; r += blockDim.x) ys[r] = (T)y[r];
     __syncthreads();
     int64_t lo, hi;
     chunk_of(W, k, bb, lo, hi);
@@ -325,9 +332,9 @@ __global__ void __launch_bounds__(kThreads) k_bupdate(BatchView W, int m, int64_
     for (int q = 0; q < kItems; ++q) {
         const int64_t i = lo + (int64_t)q * kThreads + threadIdx.x;
         if (i < hi) {
-            double acc = (double)x[i];
-            for (int r = 0; r < m; ++r) acc += ys[r] * (double)V[(int64_t)r * n + i];
-            x[i] = (T)acc;
+            T acc = x[i];
+            for (int r = 0; r < m; ++r) acc += ys[r] * V[(int64_t)r * n + i];
+            x[i] = acc;
         }
     }
 }
