@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import math
 import time
+import weakref
 from typing import Any, Callable, Dict, List, Optional, Sequence, Tuple, Union
 
 import torch
@@ -114,6 +115,24 @@ class _Krylov:
                                              P(self.work), _lib.stream_handle(self.device)), "edfmm_gmres_update")
 
 
+# Krylov buffers and captured step graphs kept with the operator object:
+# repeated solves with the same operator replay the graphs instead of
+# capturing them again (a graph bakes in the buffer addresses it was captured
+# with, so the buffers live as long as the graphs).
+_GRAPH_CACHE: "weakref.WeakKeyDictionary[Any, Dict[tuple, Dict[str, Any]]]" = weakref.WeakKeyDictionary()
+
+
+def _graph_workspace(A: Any, key: tuple, make: Callable[[], Dict[str, Any]]) -> Dict[str, Any]:
+    try:
+        per = _GRAPH_CACHE.setdefault(A, {})
+    except TypeError:  # the operator cannot be weakly referenced: no reuse
+        return make()
+    ws = per.get(key)
+    if ws is None:
+        ws = per[key] = make()
+    return ws
+
+
 @torch.no_grad()
 def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable[[Tensor], Tensor]] = None,
                   restart: int = 80, tol: float = 1e-8, maxiter: int = 500, logger: Optional[Any] = None,
@@ -193,13 +212,22 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                              _retry_without_precond=True)
 
     can_retry = used_pc and not _retry_without_precond and N <= 512
-    K = _Krylov(N, restart, work_dtype, dev)
     x = torch.zeros(N, dtype=work_dtype, device=dev) if x0 is None else x0.to(dev, work_dtype).clone()
     b_work = b.to(dev, work_dtype).contiguous()
-    av = torch.empty(N, dtype=work_dtype, device=dev)
     want_graph = (use_graph is True) or (use_graph == "auto" and bool(getattr(A, "capturable", False))
                                           and M_python is None and work_dtype == orig_dtype
                                           and orig_device.type == "cuda")
+    if want_graph and M_python is None:
+        ws = _graph_workspace(A, ("gmres", N, restart, work_dtype, dev, pinv is not None), lambda: dict(
+            K=_Krylov(N, restart, work_dtype, dev), av=torch.empty(N, dtype=work_dtype, device=dev),
+            pinv=None if pinv is None else torch.empty_like(pinv), graphs={}, warmed=[False]))
+        if pinv is not None:
+            ws["pinv"].copy_(pinv)
+            pinv = ws["pinv"]
+    else:
+        ws = dict(K=_Krylov(N, restart, work_dtype, dev), av=torch.empty(N, dtype=work_dtype, device=dev),
+                  graphs={}, warmed=[False])
+    K, av = ws["K"], ws["av"]
 
     def start_cycle():
         ax = A_apply(x)
@@ -218,8 +246,8 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
             av.copy_(y)
             K.arnoldi(j, av, pinv if M_python is None else None)
 
-    graphs: Dict[Tuple[int, int], Any] = {}
-    warmed = [False]
+    graphs: Dict[Tuple[int, int], Any] = ws["graphs"]
+    warmed = ws["warmed"]
 
     def run_steps(j0: int, count: int):
         """Arnoldi steps j0 .. j0+count-1, as a captured graph when allowed."""
@@ -428,7 +456,6 @@ def gmres_batched(A: Callable[[Tensor], Tensor], b: Tensor, segments: List[int],
     if dtype not in (torch.float32, torch.float64):
         raise ValueError("b must be float32 or float64")
     K = len(segments) - 1
-    Kr = _BatchKrylov(segments, restart, dtype, dev)
     tolv = torch.as_tensor(tol, dtype=torch.float64).reshape(-1).to(dev)
     if tolv.numel() == 1:
         tolv = tolv.expand(K).contiguous()
@@ -437,16 +464,25 @@ def gmres_batched(A: Callable[[Tensor], Tensor], b: Tensor, segments: List[int],
     pinv = None
     if A_diag is not None:
         pinv = setup_preconditioner("jacobi", A_diag=A_diag).pinv.to(dev, dtype).contiguous()
+    if use_graph:
+        ws = _graph_workspace(A, ("batched", tuple(segments), restart, dtype, dev, pinv is not None), lambda: dict(
+            Kr=_BatchKrylov(segments, restart, dtype, dev), av=torch.empty_like(b),
+            pinv=None if pinv is None else torch.empty_like(pinv), graphs={}))
+        if pinv is not None:
+            ws["pinv"].copy_(pinv)
+            pinv = ws["pinv"]
+    else:
+        ws = dict(Kr=_BatchKrylov(segments, restart, dtype, dev), av=torch.empty_like(b), graphs={})
+    Kr, av = ws["Kr"], ws["av"]
     x = torch.zeros_like(b) if x0 is None else x0.to(dev, dtype).clone()
     b = b.contiguous()
-    av = torch.empty_like(b)
 
     def steps_eager(j0: int, count: int):
         for j in range(j0, j0 + count):
             av.copy_(A(Kr.V[j]))
             Kr.arnoldi(j, av, pinv)
 
-    graphs: Dict[Tuple[int, int], Any] = {}
+    graphs: Dict[Tuple[int, int], Any] = ws["graphs"]
 
     def run_steps(j0: int, count: int):
         if not use_graph:
