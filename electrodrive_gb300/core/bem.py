@@ -331,7 +331,7 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
             tol_k = inner_tol if inner_tol is not None else min(0.1, max(inner_tol_floor, 0.3 * rtol / rel))
             d, info = gmres_restart(op32, r32, restart=inner_restart, tol=tol_k, maxiter=inner_maxiter,
                                     precond="jacobi" if d32 is not None else None, A_diag=d32, use_graph=use_graph,
-                                    early_exit=inner_early_exit)
+                                    early_exit=inner_early_exit, final_check=False)
         inner_total += info["iters"]
         x = x + d.to(torch.float64)
         r = b64 - op64(x)

@@ -142,7 +142,7 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                   callback_context: Optional[Dict[str, Any]] = None,
                   precond: Optional[Union[str, Callable[[Tensor], Tensor]]] = None, areas: Optional[Tensor] = None,
                   A_diag: Optional[Tensor] = None, validate_operators: bool = False, use_graph: Union[bool, str] = "auto",
-                  early_exit: Optional[int] = None,
+                  early_exit: Optional[int] = None, final_check: bool = True,
                   _retry_without_precond: bool = False) -> Tuple[Tensor, Dict[str, Any]]:
     """Restarted GMRES with the reference's semantics (see the module docstring).
 
@@ -150,6 +150,12 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
     steps: every ``c`` steps the device's inner residual estimate is read, and
     the cycle ends once it is below ``tol`` times the first cycle's
     preconditioned residual norm; the true-residual test then decides as usual.
+    With ``final_check=False`` (also not in the reference) a cycle that ends
+    on that estimate returns at once (code 0, ``converged_on="estimate"``)
+    instead of applying the operator once more for the true residual: for
+    callers that compute the residual themselves (iterative refinement);
+    such a solve from x0 = None also takes the zero start's residual as b
+    without applying the operator.
     """
     if restart <= 0:
         raise ValueError("restart must be positive")
@@ -229,8 +235,13 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                   graphs={}, warmed=[False])
     K, av = ws["K"], ws["av"]
 
+    # refinement callers (final_check=False) skip A(0) at a zero start; the
+    # default keeps the reference's r = b - A(0), which also screens the
+    # operator for non-finite output
+    x_is_zero = [x0 is None and not final_check]
+
     def start_cycle():
-        ax = A_apply(x)
+        ax = torch.zeros_like(b_work) if x_is_zero[0] else A_apply(x)
         if M_python is None:
             K.start(b_work, ax, pinv)
         else:  # generic preconditioner: precondition on the host side of the call
@@ -324,6 +335,7 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                 return x.to(orig_dtype).to(orig_device), _info(total_iters, float("nan"), False, 2, r_true_norm,
                                                                tol_abs, used_pc)
         steps = min(restart, maxiter - total_iters)
+        met_estimate = False
         if early_exit:
             chunk = max(1, int(early_exit))
             j0 = 0
@@ -334,6 +346,7 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                 tail = K.scal[2:5 + restart].cpu()
                 est = float(tail[2 + j0 - 1])
                 if tail[0] >= 0 or tail[1] != 0 or not math.isfinite(est) or est <= tol * beta_first:
+                    met_estimate = tail[0] < 0 and tail[1] == 0 and math.isfinite(est) and est <= tol * beta_first
                     break
             steps = j0
         elif want_graph and steps == restart:
@@ -368,6 +381,10 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
                 return retry()
             return x.to(orig_dtype).to(orig_device), _info(total_iters, r_norm, False, 2, r_true_norm, tol_abs, used_pc)
         K.update(m_use, x)
+        x_is_zero[0] = False
+        if met_estimate and not final_check:
+            return x.to(orig_dtype).to(orig_device), _info(total_iters, est, True, 0, r_true_norm, tol_abs, used_pc,
+                                                           converged_on="estimate")
     if can_retry:
         return retry()
     return x.to(orig_dtype).to(orig_device), _info(total_iters, r_norm, False, 1, r_true_norm, tol_abs, used_pc)

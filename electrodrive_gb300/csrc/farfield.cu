@@ -159,23 +159,65 @@ __global__ void __launch_bounds__(128) k_m2m(const int32_t *__restrict__ nodes, 
 }
 
 // ---------------------------------------------------------------------------
-// packed FP32 pair helpers (FFMA2: the re and im halves in one instruction)
+// pair helpers: (sr, si) += (xr, xi) * (c0, c1) on coefficients held in
+// separate re / im arrays; FP32 as one packed FMA (FFMA2), FP64 as two
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-// (sr, si) += (xr, xi) * c as one packed FMA on coefficients held in separate
-// re / im register arrays.
+template <typename T> struct Pair {};
+template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<double> { using type = double2; };
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ void fma2_into(float &sr, float &si, float xr, float xi, float2 c) {
     const float2 r = __ffma2_rn(f2(xr, xi), c, f2(sr, si));
     sr = r.x;
     si = r.y;
 }
+__device__ __forceinline__ void fma2_into(double &sr, double &si, double xr, double xi, double2 c) {
+    sr = fma(xr, c.x, sr);
+    si = fma(xi, c.y, si);
+}
+
+// FP64 coefficient arrays in the thread's shared-memory slots (element i at
+// b[i * STRIDE]: one word per thread per coefficient, conflict-free): the
+// 180 doubles of a translation do not fit in registers.  Elements are read
+// and written with volatile shared-memory accesses, which the compiler keeps
+// in program order and may neither hoist into registers nor merge, so the
+// arrays stay in shared memory (FP64 FMAs are the cost here, not the loads).
+__device__ __forceinline__ double lds_vol(const double *p) {
+    double v;
+    asm volatile("ld.volatile.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ void sts_vol(double *p, double v) {
+    asm volatile("st.volatile.shared.f64 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "d"(v));
+}
+struct DRef {
+    double *p;
+    __device__ __forceinline__ operator double() const { return lds_vol(p); }
+    __device__ __forceinline__ DRef &operator=(double v) {
+        sts_vol(p, v);
+        return *this;
+    }
+    __device__ __forceinline__ DRef &operator=(const DRef &o) { return *this = (double)o; }
+    __device__ __forceinline__ DRef &operator+=(double v) { return *this = lds_vol(p) + v; }
+};
+template <int STRIDE> struct DArr {
+    double *b;
+    __device__ __forceinline__ DRef operator[](int i) const { return DRef{b + i * STRIDE}; }
+};
+__device__ __forceinline__ void fma2_into(DRef sr, DRef si, double xr, double xi, double2 c) {
+    sr = fma(xr, c.x, (double)sr);
+    si = fma(xi, c.y, (double)si);
+}
 
 // ---------------------------------------------------------------------------
-// M2M / L2L fast paths (FP32, compile-time order): one thread per node of a
-// level, everything in registers, packed FMAs.  Both translations factor the
-// azimuth out like the M2L.  With d = (c_C - c_P) / a_P = (s cos phi,
-// s sin phi, z) and the real regular harmonics rho_k^l := R_k^l(s, 0, z)
-// (R_k^l(d) = e^{i l phi} rho_k^l, rho_k^{-l} = (-1)^l rho_k^l):
+// M2M / L2L fast paths (compile-time order): one thread per node of a level,
+// FP32 in registers with packed FMAs, FP64 in shared-memory slots.  Both
+// translations factor the azimuth out like the M2L.  With
+// d = (c_C - c_P) / a_P = (s cos phi, s sin phi, z) and the real regular
+// harmonics rho_k^l := R_k^l(s, 0, z) (R_k^l(d) = e^{i l phi} rho_k^l,
+// rho_k^{-l} = (-1)^l rho_k^l):
 //   M2M  Mhat_P,n^m = sum_C e^{-i m phi} sum_{k,l} rho_k^l Mt_{n-k}^{m-l},
 //        Mt_j^u = e^{i u phi} (a_C/a_P)^j Mhat_C,j^u
 //   L2L  Lhat_C,j^u += (a_C/a_P)^j e^{-i u phi} sum_{k,l} rho_k^l Lt_{j+k}^{u+l},
@@ -185,19 +227,21 @@ __device__ __forceinline__ void fma2_into(float &sr, float &si, float xr, float 
 // multipoles (fixed order: deterministic), stores its own multipole, then
 // writes its translation to the parent's centre for the next level up.
 // ---------------------------------------------------------------------------
-template <int P, int MU, int K>
-__device__ __forceinline__ void m2m_degree(const float (&mr)[ncoef(P)], const float (&mi)[ncoef(P)], float z, float r2,
-                                           float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
-                                           float (&Si)[ncoef(P)]) {
-    float c;
+template <typename T, int MU, int K>
+__device__ __forceinline__ T rho_coef(T z, T r2, T diag, T cm1, T cm2) {
     if constexpr (K == MU) {
-        c = diag;
+        return diag;
     } else if constexpr (K == MU + 1) {
-        c = ((float)(2 * K - 1) / (float)((K + MU) * (K - MU))) * z * cm1;
+        return ((T)(2 * K - 1) / (T)((K + MU) * (K - MU))) * z * cm1;
     } else {
-        c = ((float)(2 * K - 1) * z * cm1 - r2 * cm2) * (1.0f / (float)((K + MU) * (K - MU)));
+        return ((T)(2 * K - 1) * z * cm1 - r2 * cm2) * ((T)1 / (T)((K + MU) * (K - MU)));
     }
-    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
+}
+
+template <typename T, int P, int MU, int K, typename AR>
+__device__ __forceinline__ void m2m_degree(AR &mr, AR &mi, T z, T r2, T diag, T cm1, T cm2, AR &Sr, AR &Si) {
+    const T c = rho_coef<T, MU, K>(z, r2, diag, cm1, cm2);
+    const auto cpp = mk2(c, c), cnn = mk2(-c, -c), cpn = mk2(c, -c), cnp = mk2(-c, c);
 #pragma unroll
     for (int n = 0; n <= P; ++n) {
         if (n < K) continue;
@@ -220,22 +264,13 @@ __device__ __forceinline__ void m2m_degree(const float (&mr)[ncoef(P)], const fl
             }
         }
     }
-    if constexpr (K < P) m2m_degree<P, MU, K + 1>(mr, mi, z, r2, diag, c, cm1, Sr, Si);
+    if constexpr (K < P) m2m_degree<T, P, MU, K + 1>(mr, mi, z, r2, diag, c, cm1, Sr, Si);
 }
 
-template <int P, int MU, int K>
-__device__ __forceinline__ void l2l_degree(const float (&lr)[ncoef(P)], const float (&li)[ncoef(P)], float z, float r2,
-                                           float diag, float cm1, float cm2, float (&Sr)[ncoef(P)],
-                                           float (&Si)[ncoef(P)]) {
-    float c;
-    if constexpr (K == MU) {
-        c = diag;
-    } else if constexpr (K == MU + 1) {
-        c = ((float)(2 * K - 1) / (float)((K + MU) * (K - MU))) * z * cm1;
-    } else {
-        c = ((float)(2 * K - 1) * z * cm1 - r2 * cm2) * (1.0f / (float)((K + MU) * (K - MU)));
-    }
-    const float2 cpp = f2(c, c), cnn = f2(-c, -c), cpn = f2(c, -c), cnp = f2(-c, c);
+template <typename T, int P, int MU, int K, typename AR>
+__device__ __forceinline__ void l2l_degree(AR &lr, AR &li, T z, T r2, T diag, T cm1, T cm2, AR &Sr, AR &Si) {
+    const T c = rho_coef<T, MU, K>(z, r2, diag, cm1, cm2);
+    const auto cpp = mk2(c, c), cnn = mk2(-c, -c), cpn = mk2(c, -c), cnp = mk2(-c, c);
 #pragma unroll
     for (int j = 0; j <= P; ++j) {
         if (j + K > P) continue;
@@ -260,24 +295,23 @@ __device__ __forceinline__ void l2l_degree(const float (&lr)[ncoef(P)], const fl
             }
         }
     }
-    if constexpr (K < P) l2l_degree<P, MU, K + 1>(lr, li, z, r2, diag, c, cm1, Sr, Si);
+    if constexpr (K < P) l2l_degree<T, P, MU, K + 1>(lr, li, z, r2, diag, c, cm1, Sr, Si);
 }
 
 // columns mu = 0..P of rho; diag carries rho_mu^mu = -s / (2 mu) rho_{mu-1}^{mu-1}
-template <int P, bool L2L, int MU>
-__device__ __forceinline__ void shift_column(const float (&xr)[ncoef(P)], const float (&xi)[ncoef(P)], float s, float z,
-                                             float r2, float &diag, float (&Sr)[ncoef(P)], float (&Si)[ncoef(P)]) {
-    if constexpr (MU > 0) diag *= -s * (1.0f / (float)(2 * MU));
+template <typename T, int P, bool L2L, int MU, typename AR>
+__device__ __forceinline__ void shift_column(AR &xr, AR &xi, T s, T z, T r2, T &diag, AR &Sr, AR &Si) {
+    if constexpr (MU > 0) diag *= -s * ((T)1 / (T)(2 * MU));
     if constexpr (L2L)
-        l2l_degree<P, MU, MU>(xr, xi, z, r2, diag, 0.0f, 0.0f, Sr, Si);
+        l2l_degree<T, P, MU, MU>(xr, xi, z, r2, diag, (T)0, (T)0, Sr, Si);
     else
-        m2m_degree<P, MU, MU>(xr, xi, z, r2, diag, 0.0f, 0.0f, Sr, Si);
-    if constexpr (MU < P) shift_column<P, L2L, MU + 1>(xr, xi, s, z, r2, diag, Sr, Si);
+        m2m_degree<T, P, MU, MU>(xr, xi, z, r2, diag, (T)0, (T)0, Sr, Si);
+    if constexpr (MU < P) shift_column<T, P, L2L, MU + 1>(xr, xi, s, z, r2, diag, Sr, Si);
 }
 
-// Load a coefficient row (16-byte aligned float2 x nc_pad) into re / im arrays.
-template <int P>
-__device__ __forceinline__ void load_row(const float2 *row, float (&xr)[ncoef(P)], float (&xi)[ncoef(P)]) {
+// Load a coefficient row (16-byte aligned, nc_pad complex) into re / im arrays.
+template <int P, typename AR>
+__device__ __forceinline__ void load_row(const float2 *row, AR &xr, AR &xi) {
     constexpr int NC = ncoef(P);
     const float4 *r4 = reinterpret_cast<const float4 *>(row);
 #pragma unroll
@@ -291,134 +325,201 @@ __device__ __forceinline__ void load_row(const float2 *row, float (&xr)[ncoef(P)
         }
     }
 }
+template <int P, typename AR>
+__device__ __forceinline__ void load_row(const double2 *row, AR &xr, AR &xi) {
+#pragma unroll
+    for (int q = 0; q < ncoef(P); ++q) {
+        const double2 v = row[q];
+        xr[q] = v.x;
+        xi[q] = v.y;
+    }
+}
+template <int P, typename AR>
+__device__ __forceinline__ void store_row(float2 *row, AR &xr, AR &xi) {
+    constexpr int NC = ncoef(P);
+    float4 *o4 = reinterpret_cast<float4 *>(row);
+#pragma unroll
+    for (int q = 0; q < (NC + 1) / 2; ++q)
+        o4[q] = make_float4(xr[2 * q], xi[2 * q], 2 * q + 1 < NC ? xr[2 * q + 1] : 0.0f,
+                            2 * q + 1 < NC ? xi[2 * q + 1] : 0.0f);
+}
+template <int P, typename AR>
+__device__ __forceinline__ void store_row(double2 *row, AR &xr, AR &xi) {
+#pragma unroll
+    for (int q = 0; q < ncoef(P); ++q) row[q] = make_double2(xr[q], xi[q]);
+}
 
 // x_n^m <- e^{i m phi} f^n x_n^m  (f = 1 for the L2L)
-template <int P>
-__device__ __forceinline__ void rotate_scale(float (&xr)[ncoef(P)], float (&xi)[ncoef(P)], float ec, float es, float f) {
-    float wr = 1.0f, wi = 0.0f;
+template <typename T, int P, typename AR>
+__device__ __forceinline__ void rotate_scale(AR &xr, AR &xi, T ec, T es, T f) {
+    T wr = 1, wi = 0;
 #pragma unroll
     for (int m = 0; m <= P; ++m) {
         if (m > 0) {
-            const float nr = wr * ec - wi * es, ni = wr * es + wi * ec;
+            const T nr = wr * ec - wi * es, ni = wr * es + wi * ec;
             wr = nr;
             wi = ni;
         }
-        float fk = 1.0f;
+        T fk = 1;
 #pragma unroll
         for (int n = 0; n <= P; ++n) {
             if (n >= m) {
-                const float fr = wr * fk, fi = wi * fk;
-                const float2 x = f2(xr[tri(n, m)], xi[tri(n, m)]);
-                const float2 y = __ffma2_rn(f2(x.y, x.x), f2(-fi, fi), __fmul2_rn(x, f2(fr, fr)));
-                xr[tri(n, m)] = y.x;
-                xi[tri(n, m)] = y.y;
+                const T fr = wr * fk, fi = wi * fk;
+                if constexpr (sizeof(T) == 4) {
+                    const float2 x = f2(xr[tri(n, m)], xi[tri(n, m)]);
+                    const float2 y = __ffma2_rn(f2(x.y, x.x), f2(-fi, fi), __fmul2_rn(x, f2(fr, fr)));
+                    xr[tri(n, m)] = y.x;
+                    xi[tri(n, m)] = y.y;
+                } else {
+                    const T a = xr[tri(n, m)], b = xi[tri(n, m)];
+                    xr[tri(n, m)] = a * fr - b * fi;
+                    xi[tri(n, m)] = a * fi + b * fr;
+                }
             }
             fk *= f;
         }
     }
 }
 
-template <int P>
-__global__ void __launch_bounds__(128) k_m2m_fast(const int32_t *__restrict__ nodes, int count,
-                                                  const uint8_t *__restrict__ is_leaf,
-                                                  const int32_t *__restrict__ children, const int32_t *__restrict__ parent,
-                                                  const float4 *__restrict__ center, const float4 *__restrict__ half,
-                                                  float2 *__restrict__ Mexp, float2 *__restrict__ moved, int nc_pad) {
+// frame of the translation child -> parent: d = (c_C - c_P) / a_P
+template <typename T> struct Shift {
+    T ratio, s, z, r2, ec, es;
+};
+template <typename T>
+__device__ __forceinline__ Shift<T> shift_of(typename Vec4<T>::type cc, typename Vec4<T>::type cp, T a_child,
+                                             T a_par) {
+    Shift<T> f;
+    const T iaP = (T)1 / a_par;
+    f.ratio = a_child * iaP;
+    const T dx = (cc.x - cp.x) * iaP, dy = (cc.y - cp.y) * iaP;
+    f.z = (cc.z - cp.z) * iaP;
+    const T s2 = dx * dx + dy * dy;
+    f.s = sqrt(s2);
+    f.r2 = s2 + f.z * f.z;
+    f.ec = 1;
+    f.es = 0;
+    if (s2 > (T)0) {
+        const T is = (T)1 / f.s;
+        f.ec = dx * is;
+        f.es = dy * is;
+    }
+    return f;
+}
+
+template <typename T, int P, typename AR>
+__device__ __forceinline__ void m2m_node(int node, const uint8_t *__restrict__ is_leaf,
+                                         const int32_t *__restrict__ children, const int32_t *__restrict__ parent,
+                                         const typename Vec4<T>::type *__restrict__ center,
+                                         const typename Vec4<T>::type *__restrict__ half,
+                                         typename Pair<T>::type *__restrict__ Mexp,
+                                         typename Pair<T>::type *__restrict__ moved, int nc_pad, AR &xr, AR &xi,
+                                         AR &Sr, AR &Si) {
     constexpr int NC = ncoef(P);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const int node = nodes[i];
-    float xr[NC], xi[NC];
     if (is_leaf[node]) {
         load_row<P>(Mexp + (int64_t)node * nc_pad, xr, xi);
     } else {
 #pragma unroll
-        for (int q = 0; q < NC; ++q) xr[q] = xi[q] = 0.0f;
+        for (int q = 0; q < NC; ++q) xr[q] = xi[q] = (T)0;
         for (int o = 0; o < 8; ++o) {
             const int ch = children[8 * node + o];
             if (ch < 0) continue;
-            float yr[NC], yi[NC];
-            load_row<P>(moved + (int64_t)ch * nc_pad, yr, yi);
+            load_row<P>(moved + (int64_t)ch * nc_pad, Sr, Si);
 #pragma unroll
             for (int q = 0; q < NC; ++q) {
-                xr[q] += yr[q];
-                xi[q] += yi[q];
+                xr[q] += Sr[q];
+                xi[q] += Si[q];
             }
         }
-        float4 *o4 = reinterpret_cast<float4 *>(Mexp + (int64_t)node * nc_pad);
-#pragma unroll
-        for (int q = 0; q < (NC + 1) / 2; ++q)
-            o4[q] = make_float4(xr[2 * q], xi[2 * q], 2 * q + 1 < NC ? xr[2 * q + 1] : 0.0f,
-                                2 * q + 1 < NC ? xi[2 * q + 1] : 0.0f);
+        store_row<P>(Mexp + (int64_t)node * nc_pad, xr, xi);
     }
     const int par = parent[node];
     if (par < 0) return;
-    const float4 cc = center[node], cp = center[par];
-    const float iaP = 1.0f / half[par].w;
-    const float ratio = half[node].w * iaP;
-    const float dx = (cc.x - cp.x) * iaP, dy = (cc.y - cp.y) * iaP, z = (cc.z - cp.z) * iaP;
-    const float s2 = dx * dx + dy * dy;
-    const float s = sqrtf(s2);
-    float ec = 1.0f, es = 0.0f;
-    if (s2 > 0.0f) {
-        const float is = 1.0f / s;
-        ec = dx * is;
-        es = dy * is;
-    }
-    rotate_scale<P>(xr, xi, ec, es, ratio);
-    float Sr[NC], Si[NC];
+    const Shift<T> f = shift_of<T>(center[node], center[par], half[node].w, half[par].w);
+    rotate_scale<T, P>(xr, xi, f.ec, f.es, f.ratio);
 #pragma unroll
-    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
-    float diag = 1.0f;
-    shift_column<P, false, 0>(xr, xi, s, z, s2 + z * z, diag, Sr, Si);
-    rotate_scale<P>(Sr, Si, ec, -es, 1.0f);  // e^{-i m phi}
-    float4 *o4 = reinterpret_cast<float4 *>(moved + (int64_t)node * nc_pad);
-#pragma unroll
-    for (int q = 0; q < (NC + 1) / 2; ++q)
-        o4[q] = make_float4(Sr[2 * q], Si[2 * q], 2 * q + 1 < NC ? Sr[2 * q + 1] : 0.0f,
-                            2 * q + 1 < NC ? Si[2 * q + 1] : 0.0f);
+    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = (T)0;
+    T diag = 1;
+    shift_column<T, P, false, 0>(xr, xi, f.s, f.z, f.r2, diag, Sr, Si);
+    rotate_scale<T, P>(Sr, Si, f.ec, -f.es, (T)1);  // e^{-i m phi}
+    store_row<P>(moved + (int64_t)node * nc_pad, Sr, Si);
 }
 
-template <int P>
-__global__ void __launch_bounds__(128) k_l2l_fast(const int32_t *__restrict__ nodes, int count,
-                                                  const int32_t *__restrict__ parent, const float4 *__restrict__ center,
-                                                  const float4 *__restrict__ half, float2 *__restrict__ Lexp,
-                                                  int nc_pad) {
+template <typename T, int P, typename AR>
+__device__ __forceinline__ void l2l_node(int node, const int32_t *__restrict__ parent,
+                                         const typename Vec4<T>::type *__restrict__ center,
+                                         const typename Vec4<T>::type *__restrict__ half,
+                                         typename Pair<T>::type *__restrict__ Lexp, int nc_pad, AR &xr, AR &xi,
+                                         AR &Sr, AR &Si) {
+    constexpr int NC = ncoef(P);
+    const int par = parent[node];
+    if (par < 0) return;
+    const Shift<T> f = shift_of<T>(center[node], center[par], half[node].w, half[par].w);
+    load_row<P>(Lexp + (int64_t)par * nc_pad, xr, xi);
+    rotate_scale<T, P>(xr, xi, f.ec, f.es, (T)1);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = (T)0;
+    T diag = 1;
+    shift_column<T, P, true, 0>(xr, xi, f.s, f.z, f.r2, diag, Sr, Si);
+    rotate_scale<T, P>(Sr, Si, f.ec, -f.es, f.ratio);  // (a_C/a_P)^j e^{-i u phi}
+    load_row<P>(Lexp + (int64_t)node * nc_pad, xr, xi);
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+        xr[q] += Sr[q];
+        xi[q] += Si[q];
+    }
+    store_row<P>(Lexp + (int64_t)node * nc_pad, xr, xi);
+}
+
+constexpr int kFastThreads32 = 128, kFastThreads64 = 64;
+
+template <typename T> constexpr int fast_threads() { return sizeof(T) == 4 ? kFastThreads32 : kFastThreads64; }
+template <typename T, int P> constexpr size_t fast_smem() {
+    return sizeof(T) == 4 ? 0 : (size_t)4 * ncoef(P) * kFastThreads64 * sizeof(double);
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(fast_threads<T>()) k_m2m_fast(
+    const int32_t *__restrict__ nodes, int count, const uint8_t *__restrict__ is_leaf,
+    const int32_t *__restrict__ children, const int32_t *__restrict__ parent,
+    const typename Vec4<T>::type *__restrict__ center, const typename Vec4<T>::type *__restrict__ half,
+    typename Pair<T>::type *__restrict__ Mexp, typename Pair<T>::type *__restrict__ moved, int nc_pad) {
     constexpr int NC = ncoef(P);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const int node = nodes[i];
-    const int par = parent[node];
-    if (par < 0) return;
-    const float4 cc = center[node], cp = center[par];
-    const float iaP = 1.0f / half[par].w;
-    const float ratio = half[node].w * iaP;
-    const float dx = (cc.x - cp.x) * iaP, dy = (cc.y - cp.y) * iaP, z = (cc.z - cp.z) * iaP;
-    const float s2 = dx * dx + dy * dy;
-    const float s = sqrtf(s2);
-    float ec = 1.0f, es = 0.0f;
-    if (s2 > 0.0f) {
-        const float is = 1.0f / s;
-        ec = dx * is;
-        es = dy * is;
+    if constexpr (sizeof(T) == 4) {
+        float xr[NC], xi[NC], Sr[NC], Si[NC];
+        m2m_node<T, P>(node, is_leaf, children, parent, center, half, Mexp, moved, nc_pad, xr, xi, Sr, Si);
+    } else {
+        extern __shared__ double fast_dsm[];
+        constexpr int S = kFastThreads64;
+        DArr<S> xr{fast_dsm + threadIdx.x}, xi{fast_dsm + NC * S + threadIdx.x}, Sr{fast_dsm + 2 * NC * S + threadIdx.x},
+            Si{fast_dsm + 3 * NC * S + threadIdx.x};
+        m2m_node<T, P>(node, is_leaf, children, parent, center, half, Mexp, moved, nc_pad, xr, xi, Sr, Si);
     }
-    float xr[NC], xi[NC];
-    load_row<P>(Lexp + (int64_t)par * nc_pad, xr, xi);
-    rotate_scale<P>(xr, xi, ec, es, 1.0f);
-    float Sr[NC], Si[NC];
-#pragma unroll
-    for (int q = 0; q < NC; ++q) Sr[q] = Si[q] = 0.0f;
-    float diag = 1.0f;
-    shift_column<P, true, 0>(xr, xi, s, z, s2 + z * z, diag, Sr, Si);
-    rotate_scale<P>(Sr, Si, ec, -es, ratio);  // (a_C/a_P)^j e^{-i u phi}
-    float cr[NC], ci[NC];
-    load_row<P>(Lexp + (int64_t)node * nc_pad, cr, ci);
-    float4 *o4 = reinterpret_cast<float4 *>(Lexp + (int64_t)node * nc_pad);
-#pragma unroll
-    for (int q = 0; q < (NC + 1) / 2; ++q)
-        o4[q] = make_float4(cr[2 * q] + Sr[2 * q], ci[2 * q] + Si[2 * q],
-                            2 * q + 1 < NC ? cr[2 * q + 1] + Sr[2 * q + 1] : 0.0f,
-                            2 * q + 1 < NC ? ci[2 * q + 1] + Si[2 * q + 1] : 0.0f);
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(fast_threads<T>()) k_l2l_fast(const int32_t *__restrict__ nodes, int count,
+                                                                 const int32_t *__restrict__ parent,
+                                                                 const typename Vec4<T>::type *__restrict__ center,
+                                                                 const typename Vec4<T>::type *__restrict__ half,
+                                                                 typename Pair<T>::type *__restrict__ Lexp,
+                                                                 int nc_pad) {
+    constexpr int NC = ncoef(P);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int node = nodes[i];
+    if constexpr (sizeof(T) == 4) {
+        float xr[NC], xi[NC], Sr[NC], Si[NC];
+        l2l_node<T, P>(node, parent, center, half, Lexp, nc_pad, xr, xi, Sr, Si);
+    } else {
+        extern __shared__ double fast_dsm[];
+        constexpr int S = kFastThreads64;
+        DArr<S> xr{fast_dsm + threadIdx.x}, xi{fast_dsm + NC * S + threadIdx.x}, Sr{fast_dsm + 2 * NC * S + threadIdx.x},
+            Si{fast_dsm + 3 * NC * S + threadIdx.x};
+        l2l_node<T, P>(node, parent, center, half, Lexp, nc_pad, xr, xi, Sr, Si);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -633,42 +734,63 @@ template <typename T> int p2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
     return EDFMM_OK;
 }
 
-template <int P> void launch_m2m_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+template <typename T, int P> int fast_smem_attr(const void *fn) {
+    if (fast_smem<T, P>() <= 48 * 1024) return EDFMM_OK;
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast_smem<T, P>());
+    return e == cudaSuccess ? EDFMM_OK : fail(EDFMM_ERR_CUDA, std::string("fast M2M/L2L shared memory: ") +
+                                                                   cudaGetErrorString(e));
+}
+
+template <typename T, int P> int launch_m2m_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    using T2 = typename Pair<T>::type;
+    static const int attr = fast_smem_attr<T, P>((const void *)k_m2m_fast<T, P>);
+    if (attr) return attr;
+    constexpr int NT = fast_threads<T>();
     for (int lev = tree.max_level; lev >= 0; --lev) {
         const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
         if (hi <= lo) continue;
-        k_m2m_fast<P><<<nblk(hi - lo, 128), 128, 0, s>>>(
+        k_m2m_fast<T, P><<<nblk(hi - lo, NT), NT, fast_smem<T, P>(), s>>>(
             dptr<int32_t>(tree.level_nodes) + lo, hi - lo, dptr<uint8_t>(tree.is_leaf), dptr<int32_t>(tree.children),
-            dptr<int32_t>(tree.parent), dptr<float4>(tree.center), dptr<float4>(tree.half), dptr<float2>(buf.multipoles),
-            dptr<float2>(buf.translated), buf.nc_pad);
+            dptr<int32_t>(tree.parent), dptr<T4>(tree.center), dptr<T4>(tree.half), dptr<T2>(buf.multipoles),
+            dptr<T2>(buf.translated), buf.nc_pad);
         if (lev > 0) count_launch();
     }
+    return EDFMM_OK;
 }
 
-template <int P> void launch_l2l_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+template <typename T, int P> int launch_l2l_fast(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    using T2 = typename Pair<T>::type;
+    static const int attr = fast_smem_attr<T, P>((const void *)k_l2l_fast<T, P>);
+    if (attr) return attr;
+    constexpr int NT = fast_threads<T>();
     for (int lev = 1; lev <= tree.max_level; ++lev) {
         const int lo = tree.level_offsets[lev], hi = tree.level_offsets[lev + 1];
         if (hi <= lo) continue;
-        k_l2l_fast<P><<<nblk(hi - lo, 128), 128, 0, s>>>(dptr<int32_t>(tree.level_nodes) + lo, hi - lo,
-                                                          dptr<int32_t>(tree.parent), dptr<float4>(tree.center),
-                                                          dptr<float4>(tree.half), dptr<float2>(buf.locals), buf.nc_pad);
+        k_l2l_fast<T, P><<<nblk(hi - lo, NT), NT, fast_smem<T, P>(), s>>>(
+            dptr<int32_t>(tree.level_nodes) + lo, hi - lo, dptr<int32_t>(tree.parent), dptr<T4>(tree.center),
+            dptr<T4>(tree.half), dptr<T2>(buf.locals), buf.nc_pad);
         if (lev < tree.max_level) count_launch();
     }
+    return EDFMM_OK;
 }
 
 template <typename T> int m2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
-    if (sizeof(T) == 4 && buf.p <= 8 && tree.n_nodes > 0) {
+    if (buf.p <= 8 && tree.n_nodes > 0) {
+        int rc;
         switch (buf.p) {
-            case 1: launch_m2m_fast<1>(tree, buf, s); break;
-            case 2: launch_m2m_fast<2>(tree, buf, s); break;
-            case 3: launch_m2m_fast<3>(tree, buf, s); break;
-            case 4: launch_m2m_fast<4>(tree, buf, s); break;
-            case 5: launch_m2m_fast<5>(tree, buf, s); break;
-            case 6: launch_m2m_fast<6>(tree, buf, s); break;
-            case 7: launch_m2m_fast<7>(tree, buf, s); break;
-            default: launch_m2m_fast<8>(tree, buf, s); break;
+            case 1: rc = launch_m2m_fast<T, 1>(tree, buf, s); break;
+            case 2: rc = launch_m2m_fast<T, 2>(tree, buf, s); break;
+            case 3: rc = launch_m2m_fast<T, 3>(tree, buf, s); break;
+            case 4: rc = launch_m2m_fast<T, 4>(tree, buf, s); break;
+            case 5: rc = launch_m2m_fast<T, 5>(tree, buf, s); break;
+            case 6: rc = launch_m2m_fast<T, 6>(tree, buf, s); break;
+            case 7: rc = launch_m2m_fast<T, 7>(tree, buf, s); break;
+            default: rc = launch_m2m_fast<T, 8>(tree, buf, s); break;
         }
+        if (rc) return rc;
         EDFMM_LAUNCH_CHECK("k_m2m_fast");
         return EDFMM_OK;
     }
@@ -685,18 +807,20 @@ template <typename T> int m2m_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
 
 template <typename T> int l2l_impl(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
-    if (sizeof(T) == 4 && buf.p <= 8) {
+    if (buf.p <= 8) {
         if (tree.max_level < 1) return EDFMM_OK;
+        int rc;
         switch (buf.p) {
-            case 1: launch_l2l_fast<1>(tree, buf, s); break;
-            case 2: launch_l2l_fast<2>(tree, buf, s); break;
-            case 3: launch_l2l_fast<3>(tree, buf, s); break;
-            case 4: launch_l2l_fast<4>(tree, buf, s); break;
-            case 5: launch_l2l_fast<5>(tree, buf, s); break;
-            case 6: launch_l2l_fast<6>(tree, buf, s); break;
-            case 7: launch_l2l_fast<7>(tree, buf, s); break;
-            default: launch_l2l_fast<8>(tree, buf, s); break;
+            case 1: rc = launch_l2l_fast<T, 1>(tree, buf, s); break;
+            case 2: rc = launch_l2l_fast<T, 2>(tree, buf, s); break;
+            case 3: rc = launch_l2l_fast<T, 3>(tree, buf, s); break;
+            case 4: rc = launch_l2l_fast<T, 4>(tree, buf, s); break;
+            case 5: rc = launch_l2l_fast<T, 5>(tree, buf, s); break;
+            case 6: rc = launch_l2l_fast<T, 6>(tree, buf, s); break;
+            case 7: rc = launch_l2l_fast<T, 7>(tree, buf, s); break;
+            default: rc = launch_l2l_fast<T, 8>(tree, buf, s); break;
         }
+        if (rc) return rc;
         EDFMM_LAUNCH_CHECK("k_l2l_fast");
         return EDFMM_OK;
     }
