@@ -103,6 +103,7 @@ def _declare(L):
         "edfmm_dense_workspace_bytes": (C.c_size_t, [i64, i32]),
         "edfmm_dense_matvec_ws": (i32, [_vp, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp, C.c_size_t, _vp]),
         "edfmm_dense_potential_targets": (i32, [_vp, i64, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
+        "edfmm_dense_field_targets": (i32, [_vp, i64, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_self_integrals": (i32, [_vp, _vp, i64, i32, i32, dbl, _vp, _vp]),
         "edfmm_near_create": (i32, [_vp, _vp, _vp, i64, dbl, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_near_destroy": (i32, [_vp]),

@@ -28,7 +28,8 @@ from torch import Tensor
 from .. import _lib
 from ..utils.config import K_E, BEMConfig
 from .bem_mesh import TriMesh, generate_mesh
-from .bem_near import NearCorrection, point_charge_potential, potential_at_targets, self_integrals
+from .bem_near import (NearCorrection, field_at_targets, point_charge_field, point_charge_potential,
+                       potential_at_targets, self_integrals)
 from .bem_solver import gmres_batched, gmres_restart
 from .operators import DenseOperator, FmmOperator
 
@@ -120,6 +121,17 @@ class BEMSolution:
         if self.charges:
             v = v + point_charge_potential(pts, self.charges)
         return v
+
+    def eval_V_E_batched(self, points: Tensor) -> Tuple[Tensor, Tensor]:
+        """Total potential (N,) and field (N, 3) at points: free-space point
+        charges plus the panels' induced part (bem.py:1533-1542 with
+        bem_E_field_targets, bem_kernel.py:914, for the field)."""
+        pts = torch.as_tensor(points).to(self.sigma.device, self.sigma.dtype).reshape(-1, 3).contiguous()
+        v = self.eval(pts)
+        e = field_at_targets(pts, self.centroids, self.sigma, self.areas)
+        if self.charges:
+            e = e + point_charge_field(pts, self.charges)
+        return v, e
 
 
 def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,

@@ -107,4 +107,27 @@ def bem_potential_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor,
     return tg.potential(sigma.to(dev, dt), areas.to(dev, dt), k_e=K_E)
 
 
-__all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu", "bem_potential_targets"]
+def bem_E_field_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor, sigma: Tensor, tile_size: int = 1024,
+                        *, logger: Optional[Any] = None, use_keops: bool = False, kernel: Optional[Any] = None,
+                        backend: str = "auto") -> Tensor:
+    """Induced field at targets, (M, 3) (electrodrive/core/bem_kernel.py:914):
+    K_E sum_j sigma_j A_j (x - r_j) / max(|x - r_j|^2, 1e-24)^(3/2), the
+    reference's Laplace fast path, evaluated on the GPU.  ``backend`` accepts
+    the reference's names ("auto", "torch_tiled", "keops"); all run the same
+    kernel.  Only the Laplace kernel is supported."""
+    from .bem_near import field_at_targets
+
+    if backend not in {"auto", "torch_tiled", "keops"}:
+        raise ValueError(f"Unknown backend for bem_E_field_targets: {backend!r}")
+    if kernel is not None and not isinstance(kernel, LaplaceSingleLayerKernel):
+        raise ValueError("only the Laplace single-layer kernel is supported")
+    _ensure_tile_size(tile_size)
+    if targets.ndim != 2 or targets.shape[-1] != 3:
+        raise ValueError("targets must have shape (M, 3)")
+    if int(sigma.shape[0]) == 0 or int(targets.shape[0]) == 0:
+        return torch.zeros(int(targets.shape[0]), 3, dtype=sigma.dtype, device=sigma.device)
+    return field_at_targets(targets, src_centroids, sigma, areas)
+
+
+__all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu", "bem_potential_targets",
+           "bem_E_field_targets"]

@@ -152,5 +152,34 @@ def potential_at_targets(targets: Tensor, centroids: Tensor, sigma: Tensor, area
     return out
 
 
+def field_at_targets(targets: Tensor, centroids: Tensor, sigma: Tensor, areas: Tensor, *,
+                     k_e: float = K_E) -> Tensor:
+    """Induced field of panel charges at targets, (M, 3) (bem_E_field_targets,
+    bem_kernel.py:280-335: K_E sum_j sigma_j A_j (x - r_j) / max(r^2, 1e-24)^(3/2))."""
+    L = _lib.load_library()
+    dev, dt = sigma.device, sigma.dtype
+    T = lambda x: x.to(dev, dt).contiguous()
+    t = T(targets).reshape(-1, 3)
+    out = torch.empty(t.shape[0], 3, dtype=dt, device=dev)
+    with torch.cuda.device(dev):
+        _lib.check(L.edfmm_dense_field_targets(_lib.ptr(t), t.shape[0], _lib.ptr(T(centroids)), _lib.ptr(T(sigma)),
+                                               _lib.ptr(T(areas)), sigma.shape[0], _lib.dtype_code(dt), float(k_e),
+                                               _lib.ptr(out), _lib.stream_handle(dev)),
+                   "edfmm_dense_field_targets")
+    return out
+
+
+def point_charge_field(points: Tensor, charges) -> Tensor:
+    """Free-space field of point charges, sum_k K_E q_k (x - r_k) / max(|x - r_k|, 1e-12)^3
+    (_free_space_E_field_at_points, bem.py:340-370), (M, 3) in the points' dtype."""
+    P = points.reshape(-1, 3)
+    E = torch.zeros_like(P)
+    for q, pos in charges:
+        R = P - torch.as_tensor(pos, dtype=P.dtype, device=P.device)[None, :]
+        r = torch.linalg.norm(R, dim=1, keepdim=True).clamp_min(1e-12)
+        E = E + (K_E * float(q)) * R / (r ** 3)
+    return E
+
+
 __all__ = ["self_integrals", "NearCorrection", "apply_near_quadrature_matvec_cuda", "point_charge_potential",
-           "potential_at_targets"]
+           "potential_at_targets", "field_at_targets", "point_charge_field"]

@@ -135,6 +135,89 @@ __global__ void __launch_bounds__(kRows) k_targets_partial(const T *__restrict__
         partial[(int64_t)blockIdx.y * m + i] = acc;
 }
 
+// induced field at separate targets: E_i = sum_j (K_E / max(|x_i - r_j|^2,
+// 1e-24)^(3/2)) (sigma_j A_j) (x_i - r_j)  (bem_kernel.py:280-335, Laplace
+// fast path).  The weight is formed in the working dtype in the reference's
+// order (K_E times 1/r^3, times sigma A), so a near-coincident pair overflows
+// where the reference's does, and non-finite components become zero at the
+// end (bem_kernel.py:990-997).
+template <typename T>
+__global__ void __launch_bounds__(kRows) k_field_partial(const T *__restrict__ tgt, int64_t m,
+                                                         const T *__restrict__ c, const T *__restrict__ sigma,
+                                                         const T *__restrict__ areas, int64_t n, int64_t chunk,
+                                                         T *__restrict__ partial, int finish_rows, T k_e,
+                                                         T *__restrict__ out) {
+    using T4 = typename Vec4<T>::type;
+    __shared__ T4 src[kTile];
+    const int64_t i = (int64_t)blockIdx.x * kRows + threadIdx.x;
+    const int64_t j0 = (int64_t)blockIdx.y * chunk;
+    const int64_t j1 = min(n, j0 + chunk);
+    T xi = 0, yi = 0, zi = 0;
+    if (i < m) {
+        xi = tgt[3 * i];
+        yi = tgt[3 * i + 1];
+        zi = tgt[3 * i + 2];
+    }
+    T ex = 0, ey = 0, ez = 0;
+    for (int64_t jb = j0; jb < j1; jb += kTile) {
+        const int64_t j = jb + threadIdx.x;
+        T4 s;
+        if (j < j1) {
+            s.x = c[3 * j];
+            s.y = c[3 * j + 1];
+            s.z = c[3 * j + 2];
+            s.w = sigma[j] * areas[j];
+        } else {
+            s.x = s.y = s.z = s.w = 0;
+        }
+        __syncthreads();
+        src[threadIdx.x] = s;
+        __syncthreads();
+        const int cnt = (int)((j1 - jb) < (int64_t)kTile ? (j1 - jb) : (int64_t)kTile);
+        T tx = 0, ty = 0, tz = 0;
+#pragma unroll 8
+        for (int k = 0; k < cnt; ++k) {
+            const T4 q = src[k];
+            const T dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+            const T ir = inv_r(dx * dx + dy * dy + dz * dz);
+            const T w = (k_e * (ir * ir * ir)) * q.w;
+            tx += w * dx;
+            ty += w * dy;
+            tz += w * dz;
+        }
+        ex += tx;
+        ey += ty;
+        ez += tz;
+    }
+    if (i >= m) return;
+    if (finish_rows) {
+        out[3 * i] = isfinite(ex) ? ex : (T)0;
+        out[3 * i + 1] = isfinite(ey) ? ey : (T)0;
+        out[3 * i + 2] = isfinite(ez) ? ez : (T)0;
+    } else {
+        T *p = partial + ((int64_t)blockIdx.y * m + i) * 3;
+        p[0] = ex;
+        p[1] = ey;
+        p[2] = ez;
+    }
+}
+
+template <typename T>
+__global__ void k_field_reduce(const T *__restrict__ partial, int chunks, int64_t m, T *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    T ex = 0, ey = 0, ez = 0;
+    for (int c = 0; c < chunks; ++c) {
+        const T *p = partial + ((int64_t)c * m + i) * 3;
+        ex += p[0];
+        ey += p[1];
+        ez += p[2];
+    }
+    out[3 * i] = isfinite(ex) ? ex : (T)0;
+    out[3 * i + 1] = isfinite(ey) ? ey : (T)0;
+    out[3 * i + 2] = isfinite(ez) ? ez : (T)0;
+}
+
 template <typename T>
 __global__ void k_targets_reduce(const T *__restrict__ partial, int chunks, int64_t m, T k_e, T *__restrict__ out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -323,7 +406,57 @@ int targets_run(const T *tgt, int64_t m, const T *c, const T *sigma, const T *ar
     if (partial) cudaFreeAsync(partial, s);
     return rc;
 }
+template <typename T>
+int field_run(const T *tgt, int64_t m, const T *c, const T *sigma, const T *areas, int64_t n, T k_e, T *out,
+              cudaStream_t s) {
+    const int64_t rows = (m + kRows - 1) / kRows;
+    const int64_t want = 8LL * sm_count();
+    int64_t nch = rows >= want ? 1 : (want + rows - 1) / rows;
+    nch = std::min<int64_t>(std::max<int64_t>(nch, 1), 64);
+    int64_t chunk = ((n + nch - 1) / nch + kTile - 1) / kTile * kTile;
+    if (chunk <= 0) chunk = kTile;
+    int chunks = (int)((n + chunk - 1) / chunk);
+    if (chunks < 1) chunks = 1;
+    T *partial = nullptr;
+    if (chunks > 1)
+        EDFMM_CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(T) * 3 * (size_t)chunks * (size_t)m, s));
+    dim3 grid((unsigned)((m + kRows - 1) / kRows), (unsigned)chunks);
+    k_field_partial<T><<<grid, kRows, 0, s>>>(tgt, m, c, sigma, areas, n, chunk, partial, chunks == 1, k_e, out);
+    int rc = EDFMM_OK;
+    {
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("k_field_partial: ") + cudaGetErrorString(e));
+    }
+    if (!rc && chunks > 1) {
+        k_field_reduce<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(partial, chunks, m, out);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("k_field_reduce: ") + cudaGetErrorString(e));
+    }
+    if (partial) cudaFreeAsync(partial, s);
+    return rc;
+}
 }  // namespace
+
+extern "C" EDFMM_API int edfmm_dense_field_targets(const void *targets, int64_t m, const void *centroids,
+                                                   const void *sigma, const void *areas, int64_t n, int dtype,
+                                                   double k_e, void *out, void *stream) {
+    if (m < 0 || n < 0) return fail(EDFMM_ERR_ARG, "sizes must be >= 0");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "bad dtype");
+    if (m == 0) return EDFMM_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        EDFMM_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)m * 3 * (dtype == EDFMM_F64 ? 8 : 4), s));
+        return EDFMM_OK;
+    }
+    if (!targets || !centroids || !sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "NULL argument");
+    if (dtype == EDFMM_F64)
+        return field_run<double>((const double *)targets, m, (const double *)centroids, (const double *)sigma,
+                                 (const double *)areas, n, k_e, (double *)out, s);
+    return field_run<float>((const float *)targets, m, (const float *)centroids, (const float *)sigma,
+                            (const float *)areas, n, (float)k_e, (float *)out, s);
+}
 
 extern "C" EDFMM_API int edfmm_dense_potential_targets(const void *targets, int64_t m, const void *centroids,
                                                        const void *sigma, const void *areas, int64_t n, int dtype,

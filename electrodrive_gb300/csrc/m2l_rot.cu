@@ -91,10 +91,18 @@ __device__ __forceinline__ double lds_keep(const double *p) {
     asm volatile("ld.volatile.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
     return v;
 }
+// The matching stores are volatile too: volatile accesses keep their program
+// order, which a plain store next to an asm load would not be guaranteed.
+__device__ __forceinline__ void sts_keep(float *p, float v) {
+    asm volatile("st.volatile.shared.f32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v));
+}
+__device__ __forceinline__ void sts_keep(double *p, double v) {
+    asm volatile("st.volatile.shared.f64 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "d"(v));
+}
 template <typename T, int STRIDE> struct SmemV {
     T *base;  // this lane's slot 0; slot i at base[i * STRIDE]
     __device__ __forceinline__ T get(int i) const { return lds_keep(base + i * STRIDE); }
-    __device__ __forceinline__ void set(int i, T x) { base[i * STRIDE] = x; }
+    __device__ __forceinline__ void set(int i, T x) { sts_keep(base + i * STRIDE, x); }
 };
 
 template <typename T> struct Vec2 {};
@@ -115,6 +123,14 @@ __device__ __forceinline__ double2 lds_keep(const double2 *p) {
                  : "r"((unsigned)__cvta_generic_to_shared(p)));
     return v;
 }
+__device__ __forceinline__ void sts_keep(float2 *p, float2 v) {
+    asm volatile("st.volatile.shared.v2.f32 [%0], {%1, %2};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v.x),
+                 "f"(v.y));
+}
+__device__ __forceinline__ void sts_keep(double2 *p, double2 v) {
+    asm volatile("st.volatile.shared.v2.f64 [%0], {%1, %2};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "d"(v.x),
+                 "d"(v.y));
+}
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
@@ -125,7 +141,12 @@ template <typename T, int STRIDE> struct AccC {
     using T2 = typename Vec2<T>::type;
     T2 *base;
     __device__ __forceinline__ T2 get(int q) const { return lds_keep(base + q * STRIDE); }
-    __device__ __forceinline__ void set(int q, T2 x) { base[q * STRIDE] = x; }
+    __device__ __forceinline__ void set(int q, T2 x) {
+        if constexpr (sizeof(T) == 8)
+            sts_keep(base + q * STRIDE, x);
+        else
+            base[q * STRIDE] = x;
+    }
 };
 
 // forward rotation of degree n: scale by f^n, R_z(+phi), Q_p, R_z(+theta), Q_m

@@ -216,6 +216,14 @@ EDFMM_API int edfmm_dense_matvec_noalloc(const void *centroids_dev, const void *
 EDFMM_API int edfmm_dense_potential_targets(const void *targets_dev, int64_t m, const void *centroids_dev,
                                             const void *sigma_dev, const void *areas_dev, int64_t n, int dtype,
                                             double k_e, void *out_dev, void *stream);
+/* Induced field at m separate targets (bem_E_field_targets, the Laplace fast
+ * path of electrodrive/core/bem_kernel.py:280-335):
+ *   E_i = sum_j (k_e / max(|x_i - r_j|^2, 1e-24)^(3/2)) (sigma_j A_j) (x_i - r_j),
+ * non-finite components set to zero as the reference does; targets (m, 3) and
+ * centroids (n, 3) row-major, out (m, 3). */
+EDFMM_API int edfmm_dense_field_targets(const void *targets_dev, int64_t m, const void *centroids_dev,
+                                        const void *sigma_dev, const void *areas_dev, int64_t n, int dtype,
+                                        double k_e, void *out_dev, void *stream);
 
 /*
  * Dense operator with a caller-provided workspace of

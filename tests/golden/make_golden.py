@@ -12,6 +12,9 @@ it (paths inside the reference project):
   and ``electrodrive/fmm3d/interaction_lists.py:531`` ``build_interaction_lists``
   pairs, plus ``electrodrive/fmm3d/kernels_cpu.py:183`` ``apply_p2p_cpu_tiled``
   potentials for seeded charges.
+* ``efield_cases.npz`` -- ``electrodrive/core/bem_kernel.py:914``
+  ``bem_E_field_targets`` and ``electrodrive/core/bem.py:340``
+  ``_free_space_E_field_at_points``.
 * ``fmm_*.npz``    -- ``electrodrive/fmm3d/bem_fmm.py:888``
   ``make_laplace_fmm_backend(...).matvec`` (CPU) next to
   ``electrodrive/core/bem_kernel.py:558`` ``bem_matvec_gpu(backend="torch_tiled")``.
@@ -21,6 +24,8 @@ from __future__ import annotations
 import os
 import sys
 import time
+
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -312,8 +317,37 @@ def save_targets_cases():
     np.savez_compressed(os.path.join(HERE, "targets_cases.npz"), **out)
 
 
+def save_efield_cases():
+    """electrodrive/core/bem_kernel.py:914 bem_E_field_targets (dense induced
+    field at targets) and electrodrive/core/bem.py:340
+    _free_space_E_field_at_points, on seeded panels, densities and targets
+    (inside, on and around the source cloud, and one target on a centroid)."""
+    from electrodrive.core.bem import _free_space_E_field_at_points
+    from electrodrive.core.bem_kernel import bem_E_field_targets
+
+    out = {}
+    for name, (n, m, seed, dtype) in {"cloud_f64": (1500, 400, 31, torch.float64),
+                                      "cloud_f32": (1200, 300, 32, torch.float32)}.items():
+        g = torch.Generator().manual_seed(seed)
+        c = torch.rand(n, 3, generator=g, dtype=torch.float64).to(dtype)
+        a = (torch.rand(n, generator=g, dtype=torch.float64) * 0.5 + 0.5).to(dtype) / n
+        sig = (torch.rand(n, generator=g, dtype=torch.float64) * 2 - 1).to(dtype)
+        t = (torch.rand(m, 3, generator=g, dtype=torch.float64) * 2.0 - 0.5).to(dtype)
+        t[0] = c[7]  # a target on a source centroid: the 1e-24 clamp of r^2
+        E = bem_E_field_targets(t, c, a, sig, tile_size=256, backend="torch_tiled")
+        spec = SimpleNamespace(charges=[{"type": "point", "q": 1.5, "pos": [0.2, 0.3, 1.4]},
+                                        {"type": "point", "q": -0.5, "pos": [0.9, -0.4, 0.1]}])
+        Ef = _free_space_E_field_at_points(spec, t, dtype, torch.device("cpu"))
+        for k, v in dict(centroids=c, areas=a, sigma=sig, targets=t, E=E, E_free=Ef).items():
+            out[f"{name}__{k}"] = v.numpy()
+        print(f"efield {name}: |E| {float(E.norm()):.4g}")
+    np.savez_compressed(os.path.join(HERE, "efield_cases.npz"), **out)
+
+
 def main():
-    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets", "efield"]
+    if "efield" in which:
+        save_efield_cases()
     if "targets" in which:
         save_targets_cases()
     if "near" in which:
