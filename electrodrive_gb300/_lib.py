@@ -105,6 +105,7 @@ def _declare(L):
         "edfmm_dense_potential_targets": (i32, [_vp, i64, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_dense_field_targets": (i32, [_vp, i64, _vp, _vp, _vp, i64, i32, dbl, _vp, _vp]),
         "edfmm_self_integrals": (i32, [_vp, _vp, i64, i32, i32, dbl, _vp, _vp]),
+        "edfmm_near_targets_correct": (i32, [_vp, i64, _vp, _vp, _vp, _vp, i64, dbl, i32, i32, dbl, _vp, _vp]),
         "edfmm_near_create": (i32, [_vp, _vp, _vp, i64, dbl, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_near_destroy": (i32, [_vp]),
         "edfmm_near_num_pairs": (i64, [_vp]),

@@ -28,8 +28,8 @@ from torch import Tensor
 from .. import _lib
 from ..utils.config import K_E, BEMConfig
 from .bem_mesh import TriMesh, generate_mesh
-from .bem_near import (NearCorrection, field_at_targets, point_charge_field, point_charge_potential,
-                       potential_at_targets, self_integrals)
+from .bem_near import (NearCorrection, field_at_targets, near_potential_correction, point_charge_field,
+                       point_charge_potential, potential_at_targets, self_integrals)
 from .bem_solver import gmres_batched, gmres_restart
 from .operators import DenseOperator, FmmOperator
 
@@ -113,11 +113,23 @@ class BEMSolution:
     areas: Tensor
     sigma: Tensor
     charges: List[Tuple[float, Tuple[float, float, float]]] = field(default_factory=list)
+    # target-side near quadrature of the induced potential (bem.py:1404-1417)
+    panel_vertices: Optional[Tensor] = None
+    near_quadrature: bool = False
+    near_quad_order: int = 2
+    near_quad_dist_factor: float = 1.5
+    near_quad_max_depth: Optional[int] = None
 
     def eval(self, points: Tensor) -> Tensor:
-        """Total potential V_free + V_induced at points (N, 3) (dense induced part)."""
+        """Total potential V_free + V_induced at points (N, 3): the dense induced
+        part, corrected near the surface by the panels' quadrature when
+        ``near_quadrature`` is on and panel vertices are known (bem.py:1461-1499)."""
         pts = torch.as_tensor(points).to(self.sigma.device, self.sigma.dtype).reshape(-1, 3).contiguous()
         v = potential_at_targets(pts, self.centroids, self.sigma, self.areas)
+        if self.near_quadrature and self.panel_vertices is not None and self.panel_vertices.numel() > 0:
+            v = near_potential_correction(v, pts, self.centroids, self.areas, self.sigma, self.panel_vertices,
+                                          distance_factor=self.near_quad_dist_factor,
+                                          quad_order=self.near_quad_order, max_depth=self.near_quad_max_depth)
         if self.charges:
             v = v + point_charge_potential(pts, self.charges)
         return v
@@ -213,7 +225,19 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     bc_resid = float(torch.max(torch.abs(V_tot - bc)))
     torch.cuda.synchronize(dev)
     t_total = time.perf_counter() - t0
-    sol = BEMSolution(centroids=C_dev, areas=A_dev.to(dtype), sigma=sigma, charges=charges)
+    # evaluation near quadrature as bem.py:2560-2600 configures it
+    eval_factor = float(getattr(cfg, "near_quadrature_distance_factor", 1.5))
+    ctypes_ = {_cget(c, "type") for c in (_cget(spec, "conductors", []) or [])}
+    if "sphere" in ctypes_:
+        eval_factor = max(eval_factor, 6.0)
+    elif "plane" in ctypes_:
+        eval_factor = max(eval_factor, 3.0)
+    use_near_eval = bool(getattr(cfg, "use_near_quadrature", False)) and N > 0
+    sol = BEMSolution(centroids=C_dev, areas=A_dev.to(dtype), sigma=sigma, charges=charges,
+                      panel_vertices=torch.as_tensor(PV, dtype=torch.float64, device=dev) if use_near_eval else None,
+                      near_quadrature=use_near_eval,
+                      near_quad_order=int(getattr(cfg, "near_quadrature_order", 2)),
+                      near_quad_dist_factor=eval_factor, near_quad_max_depth=quad_depths(spec)[0])
     mesh_stats = dict(n_panels=N, total_area=float(mesh.areas.sum()), bc_residual_linf=bc_resid, h_final=h,
                       operator="fmm" if isinstance(op.base, FmmOperator) else "dense",
                       near_pairs=0 if near is None else near.n_pairs)

@@ -169,6 +169,30 @@ def field_at_targets(targets: Tensor, centroids: Tensor, sigma: Tensor, areas: T
     return out
 
 
+def near_potential_correction(V: Tensor, targets: Tensor, centroids: Tensor, areas: Tensor, sigma: Tensor,
+                              panel_vertices: Tensor, *, distance_factor: float, quad_order: int = 2,
+                              max_depth: Optional[int] = None, k_e: float = K_E) -> Tensor:
+    """Target-side near-field quadrature (_apply_near_quadrature_potentials,
+    bem.py:940-1046): returns V plus, for every panel j whose centroid is within
+    distance_factor * sqrt(A_j / pi) of a target x, sigma_j (I_near(x) -
+    K_E A_j / max(|C_j - x|, 1e-12)), with I_near the adaptive rule of panel j
+    about x (depth ``max_depth``, 4 when None as for the reference's "telles").
+    Computed in FP64 on the GPU; the result has V's dtype and device."""
+    L = _lib.load_library()
+    dev = V.device if V.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    D = lambda x: torch.as_tensor(x).to(dev, torch.float64).contiguous()
+    t = D(targets).reshape(-1, 3)
+    out = D(V).clone()
+    depth = 4 if max_depth is None else int(max_depth)
+    with torch.cuda.device(dev):
+        _lib.check(L.edfmm_near_targets_correct(_lib.ptr(t), t.shape[0], _lib.ptr(D(centroids)), _lib.ptr(D(areas)),
+                                                _lib.ptr(D(sigma)), _lib.ptr(D(panel_vertices)), int(areas.shape[0]),
+                                                float(distance_factor), int(quad_order), depth, float(k_e),
+                                                _lib.ptr(out), _lib.stream_handle(dev)),
+                   "edfmm_near_targets_correct")
+    return out.to(V.dtype).to(V.device)
+
+
 def point_charge_field(points: Tensor, charges) -> Tensor:
     """Free-space field of point charges, sum_k K_E q_k (x - r_k) / max(|x - r_k|, 1e-12)^3
     (_free_space_E_field_at_points, bem.py:340-370), (M, 3) in the points' dtype."""
@@ -182,4 +206,4 @@ def point_charge_field(points: Tensor, charges) -> Tensor:
 
 
 __all__ = ["self_integrals", "NearCorrection", "apply_near_quadrature_matvec_cuda", "point_charge_potential",
-           "potential_at_targets", "field_at_targets", "point_charge_field"]
+           "potential_at_targets", "field_at_targets", "point_charge_field", "near_potential_correction"]

@@ -128,10 +128,49 @@ __global__ void k_self_integrals(const double *__restrict__ verts, const double 
                           order, depth, ke);
 }
 
+__device__ __forceinline__ double disk_radius(double a) { return __dsqrt_rn(__ddiv_rn(a > 0.0 ? a : 0.0, M_PI)); }
+
+// Near-field correction of potentials at arbitrary targets
+// (_apply_near_quadrature_potentials, electrodrive/core/bem.py:940-1046): for
+// target x and every panel j with |C_j - x| <= f R_j, R_j = sqrt(A_j / pi),
+// and A_j > 0, sigma_j != 0:
+//   V(x) += sigma_j (I_near - K_E A_j / max(|C_j - x|, 1e-12)),
+// I_near the adaptive rule of panel j about x (the rule of the self integrals).
+// One warp per target; the lanes stride over the panels with a squared-
+// distance bound before the exact test (the numpy-order distance against
+// f R_j), and a fixed shuffle tree adds the lanes' sums into V(x).
+__global__ void k_near_targets(const double *__restrict__ tgt, int64_t m, const double *__restrict__ cent,
+                               const double *__restrict__ areas, const double *__restrict__ sigma,
+                               const double *__restrict__ verts, int64_t n, double factor, int order, int depth,
+                               double ke, double *__restrict__ V) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= m) return;  // uniform over the warp
+    const V3 x = ld3(tgt + 3 * w);
+    const double f2pi = factor * factor / M_PI * (1.0 + 1e-9);  // bound on (f R)^2, slightly widened
+    double acc = 0.0;
+    for (int64_t j = lane; j < n; j += 32) {
+        const double a = areas[j];
+        const double dx = cent[3 * j] - x.x, dy = cent[3 * j + 1] - x.y, dz = cent[3 * j + 2] - x.z;
+        if (dx * dx + dy * dy + dz * dz > f2pi * (a > 0.0 ? a : 0.0)) continue;
+        const V3 c = ld3(cent + 3 * j);
+        const double d = dist_np(c, x);
+        if (!(d <= factor * disk_radius(a))) continue;
+        const double sj = sigma[j];
+        if (!(a > 0.0) || sj == 0.0) continue;
+        const double I_near = adaptive_sum(ld3(verts + 9 * j), ld3(verts + 9 * j + 3), ld3(verts + 9 * j + 6), x,
+                                           order, depth, ke);
+        const double I_far = ke * a / (d < 1e-12 ? 1e-12 : d);
+        acc += sj * (I_near - I_far);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) V[w] += acc;
+}
+
 // ---------------------------------------------------------------------------
 // near pairs by uniform grid
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double disk_radius(double a) { return __dsqrt_rn(__ddiv_rn(a > 0.0 ? a : 0.0, M_PI)); }
 
 __global__ void k_radii_bounds(const double *cent, const double *areas, int64_t n, double *radii,
                                unsigned long long *rmax, long long *lo, long long *hi) {
@@ -361,6 +400,24 @@ EDFMM_API int edfmm_self_integrals(const void *panel_vertices_dev, const void *c
         static_cast<const double *>(panel_vertices_dev), static_cast<const double *>(centroids_dev), n, quad_order,
         depth, k_e, static_cast<double *>(out_dev));
     EDFMM_LAUNCH_CHECK("k_self_integrals");
+    return EDFMM_OK;
+}
+
+EDFMM_API int edfmm_near_targets_correct(const void *targets_dev, int64_t m, const void *centroids_dev,
+                                         const void *areas_dev, const void *sigma_dev,
+                                         const void *panel_vertices_dev, int64_t n, double distance_factor,
+                                         int quad_order, int depth, double k_e, void *V_dev, void *stream) {
+    if (m < 0 || n < 0 || depth < 0 || depth > kMaxAdaptiveDepth)
+        return fail(EDFMM_ERR_ARG, "bad m, n or depth (0..8)");
+    if (m == 0 || n == 0) return EDFMM_OK;
+    if (!targets_dev || !centroids_dev || !areas_dev || !sigma_dev || !panel_vertices_dev || !V_dev)
+        return fail(EDFMM_ERR_ARG, "NULL argument");
+    k_near_targets<<<nb(m * 32, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const double *>(targets_dev), m, static_cast<const double *>(centroids_dev),
+        static_cast<const double *>(areas_dev), static_cast<const double *>(sigma_dev),
+        static_cast<const double *>(panel_vertices_dev), n, distance_factor, quad_order, depth, k_e,
+        static_cast<double *>(V_dev));
+    EDFMM_LAUNCH_CHECK("k_near_targets");
     return EDFMM_OK;
 }
 

@@ -302,6 +302,17 @@ EDFMM_API int edfmm_bgmres_update(int64_t n, int dtype, int K, const int64_t *so
  */
 EDFMM_API int edfmm_self_integrals(const void *panel_vertices_dev, const void *centroids_dev, int64_t n,
                                    int quad_order, int depth, double k_e, void *out_dev, void *stream);
+/* Near-field correction of potentials at m arbitrary targets
+ * (_apply_near_quadrature_potentials, electrodrive/core/bem.py:940-1046), in
+ * place on V (m, FP64): for every panel j with |C_j - x| <= distance_factor *
+ * sqrt(A_j / pi), A_j > 0 and sigma_j != 0,
+ *   V(x) += sigma_j (I_near - k_e A_j / max(|C_j - x|, 1e-12)),
+ * I_near the adaptive rule of edfmm_self_integrals about x.  All arrays FP64:
+ * targets (m, 3), centroids (n, 3), areas, sigma (n), panel_vertices (n, 3, 3). */
+EDFMM_API int edfmm_near_targets_correct(const void *targets_dev, int64_t m, const void *centroids_dev,
+                                         const void *areas_dev, const void *sigma_dev,
+                                         const void *panel_vertices_dev, int64_t n, double distance_factor,
+                                         int quad_order, int depth, double k_e, void *V_dev, void *stream);
 
 /*
  * Near-pair correction set (core/bem.py:475-734): pairs 0 < |C_i - C_j| <=

@@ -12,6 +12,8 @@ it (paths inside the reference project):
   and ``electrodrive/fmm3d/interaction_lists.py:531`` ``build_interaction_lists``
   pairs, plus ``electrodrive/fmm3d/kernels_cpu.py:183`` ``apply_p2p_cpu_tiled``
   potentials for seeded charges.
+* ``nearpot_cases.npz`` -- ``electrodrive/core/bem.py:940``
+  ``_apply_near_quadrature_potentials``.
 * ``efield_cases.npz`` -- ``electrodrive/core/bem_kernel.py:914``
   ``bem_E_field_targets`` and ``electrodrive/core/bem.py:340``
   ``_free_space_E_field_at_points``.
@@ -317,6 +319,41 @@ def save_targets_cases():
     np.savez_compressed(os.path.join(HERE, "targets_cases.npz"), **out)
 
 
+def save_nearpot_cases():
+    """electrodrive/core/bem.py:940 _apply_near_quadrature_potentials: the
+    target-side near correction on a sphere and a torus mesh, at targets
+    close to the surface, on centroids (the r < 1e-12 branch) and far away."""
+    from electrodrive.core.bem import _apply_near_quadrature_potentials
+    from electrodrive.core.bem_mesh import generate_mesh
+
+    cases = {
+        "sphere": (dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=0.0), 0.4, 6.0, 3),
+        "torus": (dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0), 0.45, 1.5, 4),
+    }
+    out = {}
+    g = torch.Generator().manual_seed(91)
+    for name, (cond, h, factor, depth) in cases.items():
+        mesh = generate_mesh(_spec([cond], [dict(type="point", q=1.0, pos=[0.2, 0.1, 1.7])]), h)
+        C = torch.as_tensor(mesh.centroids, dtype=torch.float64)
+        A = torch.as_tensor(mesh.areas, dtype=torch.float64)
+        PV = torch.as_tensor(np.asarray(mesh.vertices)[np.asarray(mesh.triangles)], dtype=torch.float64)
+        n = C.shape[0]
+        sig = torch.randn(n, generator=g, dtype=torch.float64)
+        pick = torch.randperm(n, generator=g)[:40]
+        near = C[pick] * (1.0 + 0.05 * torch.randn(40, 1, generator=g, dtype=torch.float64))
+        far = torch.randn(10, 3, generator=g, dtype=torch.float64) * 3.0
+        T = torch.cat([near, C[pick[:5]], far])
+        v0 = torch.randn(T.shape[0], generator=g, dtype=torch.float64)
+        # the reference edits the numpy view of its input in place: pass a copy
+        v = _apply_near_quadrature_potentials(v0.clone(), T, C, A, sig, PV, distance_factor=factor, quad_order=2,
+                                              max_depth=depth)
+        for k, val in dict(centroids=C, areas=A, panel_vertices=PV, sigma=sig, targets=T, v_in=v0, v_out=v).items():
+            out[f"{name}__{k}"] = val.numpy()
+        out[f"{name}__meta"] = np.array([factor, 2, depth])
+        print(f"nearpot {name}: N={n} M={T.shape[0]} |dv|={float((v - v0).norm()):.3g}")
+    np.savez_compressed(os.path.join(HERE, "nearpot_cases.npz"), **out)
+
+
 def save_efield_cases():
     """electrodrive/core/bem_kernel.py:914 bem_E_field_targets (dense induced
     field at targets) and electrodrive/core/bem.py:340
@@ -345,7 +382,9 @@ def save_efield_cases():
 
 
 def main():
-    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets", "efield"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets", "efield", "nearpot"]
+    if "nearpot" in which:
+        save_nearpot_cases()
     if "efield" in which:
         save_efield_cases()
     if "targets" in which:
