@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=256, help="instances of the batch_solve workload")
     ap.add_argument("--torus-grid", default="500x200", help="torus_solve mesh grid n_u x n_v (2 n_u n_v panels)")
     ap.add_argument("--no-plain", action="store_true", help="torus_solve: skip the plain FP64 GMRES comparison")
+    ap.add_argument("--inner-tol-floor", type=float, default=1e-5,
+                    help="batch_solve: floor of the per-instance inner GMRES tolerance")
     return ap.parse_args()
 
 
@@ -593,7 +595,7 @@ def run_batch_workload(args, rank, world, local):
 
     def step():
         # zero start: the first residual is b itself (no operator application)
-        result["x"], result["info"] = system.solve()
+        result["x"], result["info"] = system.solve(inner_tol_floor=args.inner_tol_floor)
 
     warm = max(args.warmup, 3)
     for _ in range(warm):
@@ -611,7 +613,7 @@ def run_batch_workload(args, rank, world, local):
 
     def learned_step():
         # per-instance learned warm start (network + one FP32 application) inside the timing
-        learned["x"], learned["info"] = system.solve(x0=system.learned_start(net))
+        learned["x"], learned["info"] = system.solve(x0=system.learned_start(net), inner_tol_floor=args.inner_tol_floor)
     t_learned = _time_cuda(learned_step, dev, stream, flush, 1, 1)[0] if net is not None else None
     mv = {"float64": statistics.median(_time_cuda(lambda: system.op64(system.x0_cold), dev, stream, flush, 1, 3)),
           "float32": statistics.median(_time_cuda(lambda: system.op32(system.x0_cold.float()), dev, stream, flush,
@@ -633,7 +635,7 @@ def run_batch_workload(args, rank, world, local):
     t0 = time.perf_counter()
     sys2 = BatchSystem(cases, device=dev, inner_leaf_size=tune["leaf_size"],
                        inner_expansion_order=tune["expansion_order"])
-    x2, _ = sys2.solve()
+    x2, _ = sys2.solve(inner_tol_floor=args.inner_tol_floor)
     x2.cpu()
     e2e_ms = 1e3 * (time.perf_counter() - t0)
     del sys2
@@ -648,6 +650,7 @@ def run_batch_workload(args, rank, world, local):
                           "l2": "flushed by a 256 MiB write between steps", "parallelism": f"replicas x{world}",
                           "inner_operator": {k: tune[k] for k in ("leaf_size", "expansion_order", "ms")},
                           "inner_solver": "batched GMRES (one Krylov space per instance), restart 100",
+                          "inner_tol_floor": args.inner_tol_floor,
                           "start": "zero (first residual = b)"},
                "solve": {"code": info["code"], "outer_iters": info["outer"], "inner_iters": info["inner_iters"],
                          "instance_inner_iters": ({"mean": float(np.mean(info["instance_inner_iters"])),
