@@ -85,7 +85,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=256, help="instances of the batch_solve workload")
     ap.add_argument("--torus-grid", default="500x200", help="torus_solve mesh grid n_u x n_v (2 n_u n_v panels)")
     ap.add_argument("--no-plain", action="store_true", help="torus_solve: skip the plain FP64 GMRES comparison")
-    ap.add_argument("--inner-tol-floor", type=float, default=1e-5,
+    ap.add_argument("--inner-tol-floor", type=float, default=3e-7,
                     help="batch_solve: floor of the per-instance inner GMRES tolerance")
     return ap.parse_args()
 
