@@ -97,3 +97,63 @@ def test_fmm_config_validation_matches_reference():
                 dict(p2p_batch_size=0)):
         with pytest.raises(ValueError):
             FmmConfig(**bad)
+
+
+def test_new_entry_points_reject_bad_arguments_before_touching_the_gpu(edlib):
+    """Field, evaluation-side near quadrature and batched GMRES check their
+    arguments on the host and return EDFMM_ERR_ARG without a CUDA call."""
+    from electrodrive_gb300 import _lib
+
+    E = _lib.EDFMM_ERR_ARG
+    # field at targets: negative sizes, bad dtype, NULL arrays
+    assert edlib.edfmm_dense_field_targets(None, -1, None, None, None, 4, 0, 1.0, None, None) == E
+    assert edlib.edfmm_dense_field_targets(None, 4, None, None, None, 4, 9, 1.0, None, None) == E
+    assert edlib.edfmm_dense_field_targets(None, 4, None, None, None, 4, 0, 1.0, None, None) == E
+    # m = 0 is a no-op
+    assert edlib.edfmm_dense_field_targets(None, 0, None, None, None, 4, 0, 1.0, None, None) == _lib.EDFMM_OK
+    # evaluation-side near quadrature: depth beyond the rule's limit, NULL arrays
+    assert edlib.edfmm_near_targets_correct(None, 3, None, None, None, None, 3, 1.5, 2, 9, 1.0, None, None) == E
+    assert edlib.edfmm_near_targets_correct(None, 3, None, None, None, None, 3, 1.5, 2, 3, 1.0, None, None) == E
+    assert edlib.edfmm_near_targets_correct(None, 0, None, None, None, None, 3, 1.5, 2, 3, 1.0, None, None) == \
+        _lib.EDFMM_OK
+    # batched GMRES: restart out of range, max_seg beyond n, NULL arrays, bad step index
+    assert edlib.edfmm_bgmres_start(10, 0, 2, None, 5, 0, None, None, None, None, None, 1, None, None, None) == E
+    assert edlib.edfmm_bgmres_start(10, 0, 2, None, 11, 8, None, None, None, None, None, 1, None, None, None) == E
+    assert edlib.edfmm_bgmres_start(10, 0, 2, None, 5, 8, None, None, None, None, None, 1, None, None, None) == E
+    assert edlib.edfmm_bgmres_arnoldi(10, 0, 2, None, 5, 8, 8, None, None, None, None, None, None, None) == E
+    assert edlib.edfmm_bgmres_update(10, 0, 2, None, 5, 8, 9, None, None, None, None, None) == E
+    assert int(edlib.edfmm_bgmres_state_cols(40)) == 50
+    assert int(edlib.edfmm_bgmres_work_bytes(3, 2000, 40)) > 0
+
+
+def test_gmres_batched_validates_segments():
+    import torch
+
+    from electrodrive_gb300.core.bem_solver import gmres_batched
+
+    b = torch.ones(6, dtype=torch.float64)
+    with pytest.raises(ValueError):
+        gmres_batched(lambda v: v, b, [0, 3, 5])  # does not end at len(b)
+    with pytest.raises(ValueError):
+        gmres_batched(lambda v: v, b, [0, 4, 3, 6])  # decreasing
+    with pytest.raises(ValueError):
+        gmres_batched(lambda v: v, b, [0, 6], restart=0)
+    with pytest.raises(RuntimeError):
+        gmres_batched(lambda v: v, b, [0, 2, 6])  # CPU tensors: the solver runs on CUDA only
+
+
+def test_bem_E_field_targets_validates_like_the_reference():
+    import torch
+
+    from electrodrive_gb300.core.bem_kernel import bem_E_field_targets
+
+    t = torch.zeros(3, 3, dtype=torch.float64)
+    c = torch.zeros(4, 3, dtype=torch.float64)
+    a = torch.ones(4, dtype=torch.float64)
+    with pytest.raises(ValueError):
+        bem_E_field_targets(t, c, a, a, backend="bogus")
+    with pytest.raises(ValueError):
+        bem_E_field_targets(t[:, :2], c, a, a)
+    # no panels: a zero field without touching the GPU
+    z = bem_E_field_targets(t, c[:0], a[:0], a[:0])
+    assert z.shape == (3, 3) and not z.any()
