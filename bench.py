@@ -335,7 +335,12 @@ def run_solve_workload(args, rank, world, local):
             result["x"], result["info"] = gmres_restart(op64, b, restart=50, tol=1e-8, maxiter=2000, precond="jacobi",
                                                         areas=sysd["areas"], A_diag=diag, x0=x0, use_graph=True)
     else:
-        op32 = sysd["ops"][torch.float32]
+        # the FP32 inner operator: the fastest expansion order within 3e-7 of the FP64 operator
+        from electrodrive_gb300.core.bem import autotune_inner_operator
+
+        op32, inner_trials = autotune_inner_operator(op64, sysd["centroids"], sysd["areas"], sysd["self_corr"],
+                                                     near=sysd["ops"][torch.float32].near, device=dev)
+        sysd["ops"][torch.float32] = op32
         net = geom = None
         weights = os.path.join(ROOT, "electrodrive_gb300", "data", "pcn_weights.npz")
         if os.path.exists(weights):
@@ -454,11 +459,13 @@ def run_solve_workload(args, rank, world, local):
         fp32_peak = _lib.measure_fp32_peak()
         p32.set_charges(sig.float() * sysd["areas"].float())
         m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 2, 5))
-        achieved = p32.info.n_m2l_pairs * M2L_FLOPS_PER_PAIR / (m2l_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_m2l_rot<float, 8> (M2L of the FP32 inner operator)", "bound": "fp32", "achieved": achieved,
+        order32 = int(p32.info.expansion_order)
+        achieved = p32.info.n_m2l_pairs * m2l_flops_per_pair(order32) / (m2l_ms * 1e-3) / 1e12
+        roof = {"kernel": f"k_m2l_rot<float, {order32}> (M2L of the FP32 inner operator)", "bound": "fp32",
+                "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
-                "traffic": M2L_DRAM_BYTES_PER_PAIR * p32.info.n_m2l_pairs,
-                "traffic_note": "scaled from an ncu capture of the same kernel at N=262,144 (uniform cube)",
+                "traffic": M2L_DRAM_BYTES_PER_PAIR * p32.info.n_m2l_pairs if order32 == 8 else None,
+                "traffic_note": "scaled from an ncu capture of the p = 8 kernel at N=262,144 (uniform cube)",
                 "peak_source": "FP32 FMA probe measured in this run (edfmm_measure_fp32_peak)"}
         extra = {"plain_fp64_gmres": {"solves_per_s": 1e3 / t_plain if t_plain else None, "ms": t_plain,
                                       "iters": pinfo["iters"], "code": pinfo["code"], "true_rel_resid": plain_rel,
@@ -474,7 +481,9 @@ def run_solve_workload(args, rank, world, local):
                  "outer_iters": info["outer"], "inner_iters": info["inner_iters"], "fp64_matvecs": info["matvec64"],
                  "n_nodes_fp32": p32.info.n_nodes, "n_m2l_pairs_fp32": p32.info.n_m2l_pairs,
                  "n_p2p_pairs_fp32": p32.info.n_p2p_pairs, "p2p_interactions_fp32": p32.info.p2p_interactions,
-                 "n_m2l_pairs_fp64": p64.info.n_m2l_pairs, "m2l_fp32_ms": m2l_ms}
+                 "n_m2l_pairs_fp64": p64.info.n_m2l_pairs, "m2l_fp32_ms": m2l_ms,
+                 "inner_operator": {"expansion_order": order32, "leaf_size": int(p32.info.leaf_size),
+                                    "trials": inner_trials}}
         plain_matvecs = max(1, pinfo["iters"] + pinfo["iters"] // 256 + 2)
         # the same mixed solver from the cold start (x0 = b / I_self)
         cold = {}
@@ -492,7 +501,7 @@ def run_solve_workload(args, rank, world, local):
                                         "cold": relative_error(x0, plain["x"], sysd["areas"])}
         cfg = BEMConfig(use_near_quadrature_matvec=True)
         e2e_call = lambda: bem_solve(spec, cfg, mesh=mesh, operator="fmm", self_integral="quadrature", mixed=True,
-                                     mixed_rtol=1e-6, inner_restart=40)
+                                     mixed_rtol=1e-6, inner_restart=40, inner_expansion_order=order32)
         h2d = n * 8 * (3 + 1 + 9 + 3 + 1) * 2
 
     # end to end through the public API: host mesh -> solve -> host sigma

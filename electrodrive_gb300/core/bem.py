@@ -149,7 +149,7 @@ class BEMSolution:
 def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,
               *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
               use_graph: bool = True, self_integral: str = "auto", mixed: bool = False, mixed_rtol: float = 1e-6,
-              inner_restart: int = 40) -> Dict[str, Any]:
+              inner_restart: int = 40, inner_expansion_order: Optional[int] = None) -> Dict[str, Any]:
     """One solve pass.  ``self_integral``: "auto" follows the reference
     (quadrature self terms only when a near-quadrature option is on, else the
     equal-area disk value 2 pi K_E sqrt(A / pi), bem.py:1747-1816), or force
@@ -199,7 +199,8 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     op32 = None
     if mixed:
         op32 = build_operator(C64, A64, self_corr.to(torch.float32), dtype=torch.float32, kind=operator,
-                              fmm_threshold=fmm_threshold, near=make_near(torch.float32), device=dev)
+                              fmm_threshold=fmm_threshold, near=make_near(torch.float32), device=dev,
+                              expansion_order=inner_expansion_order or 8)
     charges = point_charges(spec)
     C_dev = C64.to(dev, dtype)
     V_free = point_charge_potential(C_dev, charges) if charges else torch.zeros(N, dtype=dtype, device=dev)
@@ -277,7 +278,48 @@ def assemble_system(mesh: TriMesh, spec: Any, *, kind: str = "dense", dtypes=(to
     b = torch.as_tensor(bc_vector(spec, mesh), dtype=torch.float64, device=dev) - V_free
     diag = I_self.clamp_min(1e-18)
     return dict(ops=ops, b=b, diag=diag, x0=b / diag, areas=A_dev, centroids=C64, n=mesh.n_panels,
-                near_pairs=0 if not near else next(iter(ops.values())).near.n_pairs, charges=charges)
+                near_pairs=0 if not near else next(iter(ops.values())).near.n_pairs, charges=charges,
+                self_corr=self_corr)
+
+
+def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: Tensor, near=None, *,
+                            orders=(8, 7, 6), leaf_sizes=(64,), max_rel_error: float = 3e-7, reps: int = 5,
+                            device=None) -> Tuple[Any, List[Dict[str, Any]]]:
+    """The FP32 FMM operator for the inner solves of iterative refinement:
+    among expansion orders and leaf sizes, the fastest whose output on a
+    fixed random density is within ``max_rel_error`` of ``op64``'s (the FP32
+    operator at p = 8 is about 2e-7 away; looser operators make the first
+    refinement step fall short of 1e-6).  ``near`` is the FP32 near
+    correction the operator adds.  Returns (operator, trials)."""
+    dev = torch.device(device) if device is not None else op64.device if hasattr(op64, "device") else \
+        torch.device("cuda", torch.cuda.current_device())
+    g = torch.Generator(device="cpu").manual_seed(0)
+    probe = torch.rand(int(areas.shape[0]), generator=g, dtype=torch.float64).to(dev)
+    ref = op64(probe).to(torch.float64).clone()
+    stream = torch.cuda.current_stream(dev)
+    trials, best = [], None
+    for leaf in leaf_sizes:
+        for p in orders:
+            op = build_operator(centroids, areas, self_corr.to(torch.float32), dtype=torch.float32, kind="fmm",
+                                near=near, leaf_size=leaf, expansion_order=p, device=dev)
+            x = probe.float()
+            op(x)
+            times = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                y = op(x)
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                times.append(e0.elapsed_time(e1))
+            err = float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
+            t = sorted(times)[len(times) // 2]
+            trials.append(dict(leaf_size=leaf, expansion_order=p, ms=t, rel_error=err))
+            if err <= max_rel_error and (best is None or t < best[0]):
+                best = (t, op)
+    if best is None:
+        raise RuntimeError("no inner operator met the accuracy bound")
+    return best[1], trials
 
 
 def segment_norms(v: Tensor, offsets: Optional[List[int]]) -> Tensor:
@@ -377,5 +419,6 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
                    matvec64=matvec64, instance_inner_iters=inst_iters)
 
 
-__all__ = ["BEMOperator", "BEMSolution", "assemble_system", "bem_solve", "build_operator", "bc_vector", "point_charges",
+__all__ = ["BEMOperator", "BEMSolution", "assemble_system", "autotune_inner_operator", "bem_solve", "build_operator",
+           "bc_vector", "point_charges",
            "quad_depths", "segment_norms", "solve_mixed"]

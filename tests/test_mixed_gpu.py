@@ -44,3 +44,20 @@ def test_mixed_solve_stops_on_fp64_residual(torus_system, first):
         assert info["matvec64"] == info["outer"]
     else:
         assert info["matvec64"] == info["outer"] + 1
+
+
+def test_autotuned_inner_operator_meets_its_bound_and_the_solve_converges(torus_system):
+    from electrodrive_gb300.core.bem import autotune_inner_operator, solve_mixed
+
+    S = torus_system
+    op64 = S["ops"][torch.float64]
+    op32, trials = autotune_inner_operator(op64, S["centroids"], S["areas"], S["self_corr"],
+                                           near=S["ops"][torch.float32].near, orders=(8, 6), max_rel_error=3e-7)
+    assert {t["expansion_order"] for t in trials} == {8, 6}
+    chosen = [t for t in trials if t["expansion_order"] == op32.base.plan.info.expansion_order][0]
+    assert chosen["rel_error"] <= 3e-7
+    assert chosen["ms"] == min(t["ms"] for t in trials if t["rel_error"] <= 3e-7)
+    b = S["b"]
+    x, info = solve_mixed(op64, op32, b, A_diag=S["diag"], x0=S["x0"], rtol=1e-6)
+    assert info["code"] == 0
+    assert float(torch.linalg.norm(b - op64(x)) / torch.linalg.norm(b)) <= 1e-6 * (1 + 1e-9)
