@@ -75,6 +75,7 @@ def _declare(L):
         "edfmm_targets_info": (i32, [_vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
         "edfmm_targets_export_lists": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_targets_potential": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
+        "edfmm_targets_field": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
         "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
@@ -438,4 +439,15 @@ class Targets:
         with torch.cuda.device(self.device):
             check(self._lib.edfmm_targets_potential(self._h, ptr(s), ptr(a), float(k_e), ptr(o), int(flags),
                                                     stream_handle(self.device)), "edfmm_targets_potential")
+        return o
+
+    def field(self, sigma: torch.Tensor, areas: torch.Tensor, *, k_e: float = 1.0, out=None, flags: int = 0):
+        """Field k_e sum_j sigma_j A_j (x - c_j) / |x - c_j|^3 at the targets, (m, 3), by FMM."""
+        dt = self.plan.dtype
+        s = sigma.to(self.device, dt).contiguous()
+        a = areas.to(self.device, dt).contiguous()
+        o = torch.empty(self.n, 3, dtype=dt, device=self.device) if out is None else out
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_targets_field(self._h, ptr(s), ptr(a), float(k_e), ptr(o), int(flags),
+                                                stream_handle(self.device)), "edfmm_targets_field")
         return o

@@ -109,16 +109,23 @@ def bem_potential_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor,
 
 def bem_E_field_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor, sigma: Tensor, tile_size: int = 1024,
                         *, logger: Optional[Any] = None, use_keops: bool = False, kernel: Optional[Any] = None,
-                        backend: str = "auto") -> Tensor:
+                        backend: str = "auto", method: str = "dense", leaf_size: int = 64, expansion_order: int = 8,
+                        mac_theta: float = 0.5) -> Tensor:
     """Induced field at targets, (M, 3) (electrodrive/core/bem_kernel.py:914):
     K_E sum_j sigma_j A_j (x - r_j) / max(|x - r_j|^2, 1e-24)^(3/2), the
     reference's Laplace fast path, evaluated on the GPU.  ``backend`` accepts
     the reference's names ("auto", "torch_tiled", "keops"); all run the same
-    kernel.  Only the Laplace kernel is supported."""
+    dense kernel.  ``method="fmm"`` (not in the reference) evaluates the field
+    by FMM instead: a plan of the panels, a target tree, near sums over the
+    P2P lists and minus the gradient of the local expansions (distances within
+    the dtype's epsilon contribute nothing).  Only the Laplace kernel is
+    supported."""
     from .bem_near import field_at_targets
 
     if backend not in {"auto", "torch_tiled", "keops"}:
         raise ValueError(f"Unknown backend for bem_E_field_targets: {backend!r}")
+    if method not in ("dense", "fmm"):
+        raise ValueError(f"unknown method {method!r}")
     if kernel is not None and not isinstance(kernel, LaplaceSingleLayerKernel):
         raise ValueError("only the Laplace single-layer kernel is supported")
     _ensure_tile_size(tile_size)
@@ -126,7 +133,14 @@ def bem_E_field_targets(targets: Tensor, src_centroids: Tensor, areas: Tensor, s
         raise ValueError("targets must have shape (M, 3)")
     if int(sigma.shape[0]) == 0 or int(targets.shape[0]) == 0:
         return torch.zeros(int(targets.shape[0]), 3, dtype=sigma.dtype, device=sigma.device)
-    return field_at_targets(targets, src_centroids, sigma, areas)
+    if method == "dense":
+        return field_at_targets(targets, src_centroids, sigma, areas)
+    dev = sigma.device if sigma.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    dt = sigma.dtype
+    plan = _lib.Plan(src_centroids.to(dev, dt).contiguous(), leaf_size=leaf_size, mac_theta=mac_theta,
+                     expansion_order=expansion_order)
+    tg = plan.targets(targets.to(dev, dt))
+    return tg.field(sigma.to(dev, dt), areas.to(dev, dt), k_e=K_E)
 
 
 __all__ = ["LaplaceSingleLayerKernel", "DEFAULT_SINGLE_LAYER_KERNEL", "bem_matvec_gpu", "bem_potential_targets",

@@ -216,6 +216,9 @@ struct NearArgs {
     // evaluated against a source plan): no self exclusion then
     const struct DevTree *src_tree = nullptr;
 };
+// field at the points of a target tree (evaluation from a source plan)
+int run_targets_field(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf, const DevTree &stree,
+                      double k_e, bool near, bool far, void *out, cudaStream_t s);
 int run_p2p_l2p(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
                 const NearArgs &args, cudaStream_t s);
 int upload_tables();

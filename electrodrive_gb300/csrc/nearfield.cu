@@ -416,4 +416,132 @@ int run_p2p_l2p(const DevTree &tree, const DevLists &lists, const FmmBuffers &bu
                                    : near_impl<float>(tree, lists, buf, args, s);
 }
 
+namespace {
+
+// Gradient of the local expansion sum_{n,m} w_m Re(L_n^m R_n^m(x, y, z))
+// (w_0 = 1, w_m = 2) in the node's scaled frame, from
+//   d/dz R_n^m = R_{n-1}^m,  (d/dx + i d/dy) R_n^m = R_{n-1}^{m+1},
+//   (d/dx - i d/dy) R_n^m = -R_{n-1}^{m-1}
+// (negative orders through R^{-m} = (-1)^m conj(R^m)).
+template <typename T>
+__device__ void l2p_gradient(const Cplx<T> *L, int p, T x, T y, T z, T &gx, T &gy, T &gz) {
+    Cplx<T> R[ncoef(kPMax - 1)];
+    gx = gy = gz = (T)0;
+    if (p < 1) return;
+    regular_harmonics_rt<T>(x, y, z, p - 1, R);
+    for (int n = 1; n <= p; ++n) {
+        for (int m = 0; m <= n; ++m) {
+            const Cplx<T> l = L[tri(n, m)];
+            const Cplx<T> zero{(T)0, (T)0};
+            const Cplx<T> dp = m + 1 <= n - 1 ? R[tri(n - 1, m + 1)] : zero;
+            Cplx<T> dm = zero;
+            if (m - 1 >= -(n - 1) && m - 1 <= n - 1) {
+                const Cplx<T> h = harm_at<T>(R, n - 1, m - 1);
+                dm = Cplx<T>{-h.re, -h.im};
+            }
+            const Cplx<T> dz = m <= n - 1 ? R[tri(n - 1, m)] : zero;
+            const T w = m == 0 ? (T)1 : (T)2;
+            const Cplx<T> sp = cmul(l, Cplx<T>{dp.re + dm.re, dp.im + dm.im});
+            const Cplx<T> sm = cmul(l, Cplx<T>{dp.re - dm.re, dp.im - dm.im});
+            gx += w * (T)0.5 * sp.re;
+            gy += w * (T)0.5 * sm.im;
+            gz += w * cmul(l, dz).re;
+        }
+    }
+}
+
+// Field at the points of a target tree from a source plan: one warp per
+// target leaf, one lane per target.  Near part: sum_j q_j (x - y_j) / r^3
+// over the leaf's P2P row (the gradient of the potential kernel
+// q / max(r, eps), zero where r <= eps); far part: minus the gradient of the
+// leaf's local expansion.  out[3 * index_map[i] + c] = k_e * E_c.
+template <typename T>
+__global__ void __launch_bounds__(128) k_targets_field(
+    const int32_t *__restrict__ leaves, int64_t n_leaves, const int32_t *__restrict__ off,
+    const int32_t *__restrict__ src, const typename Vec4<T>::type *__restrict__ pts, const int2 *__restrict__ range,
+    const typename Vec4<T>::type *__restrict__ spts, const int2 *__restrict__ srange,
+    const typename Vec4<T>::type *__restrict__ center, const typename Vec4<T>::type *__restrict__ half,
+    const Cplx<T> *__restrict__ Lexp, int p, int nc_pad, T eps2, int near, int far,
+    const int32_t *__restrict__ index_map, T k_e, T *__restrict__ out) {
+    using T4 = typename Vec4<T>::type;
+    __shared__ T4 sp[4][32];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * 4 + wl;
+    if (w >= n_leaves) return;
+    const int t = leaves[w];
+    const int2 rg = range[t];
+    T4 c{};
+    T ia = (T)1;
+    if (far) {
+        c = center[t];
+        ia = (T)1 / half[t].w;
+    }
+    for (int tb = rg.x; tb < rg.y; tb += 32) {
+        const int ti = tb + lane;
+        const bool valid = ti < rg.y;
+        const T4 x = pts[valid ? ti : rg.x];
+        T ex = 0, ey = 0, ez = 0;
+        if (near) {
+            for (int k = off[t]; k < off[t + 1]; ++k) {
+                const int2 sr = srange[src[k]];
+                for (int sb = sr.x; sb < sr.y; sb += 32) {
+                    const int cnt = min(32, sr.y - sb);
+                    __syncwarp();
+                    if (lane < cnt) sp[wl][lane] = spts[sb + lane];
+                    __syncwarp();
+                    for (int j = 0; j < cnt; ++j) {
+                        const T4 q = sp[wl][j];
+                        const T dx = x.x - q.x, dy = x.y - q.y, dz = x.z - q.z;
+                        const T r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 > eps2) {
+                            const T ir = (T)1 / sqrt(r2);
+                            const T wq = q.w * ir * ir * ir;
+                            ex += wq * dx;
+                            ey += wq * dy;
+                            ez += wq * dz;
+                        }
+                    }
+                }
+            }
+        }
+        if (far && valid) {
+            T gx, gy, gz;
+            l2p_gradient<T>(Lexp + (int64_t)t * nc_pad, p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia, gx, gy,
+                            gz);
+            ex -= gx * ia;
+            ey -= gy * ia;
+            ez -= gz * ia;
+        }
+        if (valid) {
+            const int o = index_map[ti];
+            out[3 * o] = k_e * ex;
+            out[3 * o + 1] = k_e * ey;
+            out[3 * o + 2] = k_e * ez;
+        }
+    }
+}
+
+template <typename T>
+int field_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf, const DevTree &stree, double k_e,
+               bool near, bool far, void *out, cudaStream_t s) {
+    using T4 = typename Vec4<T>::type;
+    if (tree.n_leaves == 0) return EDFMM_OK;
+    const T eps = sizeof(T) == 8 ? (T)DBL_EPSILON : (T)FLT_EPSILON;
+    k_targets_field<T><<<(unsigned)((tree.n_leaves + 3) / 4), 128, 0, s>>>(
+        dptr<int32_t>(tree.leaves), tree.n_leaves, dptr<int32_t>(lists.p2p_off), dptr<int32_t>(lists.p2p_src),
+        dptr<T4>(tree.pts), dptr<int2>(tree.range), dptr<T4>(stree.pts), dptr<int2>(stree.range),
+        dptr<T4>(tree.center), dptr<T4>(tree.half), dptr<Cplx<T>>(buf.locals), buf.p, buf.nc_pad, eps * eps,
+        near ? 1 : 0, far ? 1 : 0, dptr<int32_t>(tree.index_map), (T)k_e, static_cast<T *>(out));
+    EDFMM_LAUNCH_CHECK("k_targets_field");
+    return EDFMM_OK;
+}
+
+}  // namespace
+
+int run_targets_field(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf, const DevTree &stree,
+                      double k_e, bool near, bool far, void *out, cudaStream_t s) {
+    return tree.dtype == EDFMM_F64 ? field_impl<double>(tree, lists, buf, stree, k_e, near, far, out, s)
+                                   : field_impl<float>(tree, lists, buf, stree, k_e, near, far, out, s);
+}
+
 }  // namespace edfmm

@@ -528,4 +528,24 @@ int edfmm_targets_potential(edfmm_targets *t, const void *sigma, const void *are
     return run_p2p_l2p(t->tree, t->lists, t->buf, a, s);
 }
 
+int edfmm_targets_field(edfmm_targets *t, const void *sigma, const void *areas, double k_e, void *out, int flags,
+                        void *stream) {
+    if (!t) return fail(EDFMM_ERR_ARG, "targets is NULL");
+    edfmm_plan *p = t->plan;
+    if (int rc = check_plan(p)) return rc;
+    if (t->tree.n_points == 0) return EDFMM_OK;
+    if (!sigma || !areas || !out) return fail(EDFMM_ERR_ARG, "sigma, areas and out must be non-NULL");
+    cudaStream_t s = S(stream);
+    const bool far = (flags & EDFMM_NO_FARFIELD) == 0;
+    const bool near = (flags & EDFMM_NO_NEARFIELD) == 0;
+    int rc;
+    if ((rc = set_charges(p->tree, sigma, areas, s))) return rc;
+    if (far) {
+        if ((rc = run_p2m(p->tree, p->fmm, s)) || (rc = run_m2m(p->tree, p->fmm, s)) ||
+            (rc = run_m2l_two(t->tree, p->tree, t->lists, p->fmm, t->buf, s)) || (rc = run_l2l(t->tree, t->buf, s)))
+            return rc;
+    }
+    return run_targets_field(t->tree, t->lists, t->buf, p->tree, k_e, near, far, out, s);
+}
+
 }  // extern "C"

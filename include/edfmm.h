@@ -378,8 +378,12 @@ EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_ou
  * (electrodrive/fmm3d/interaction_lists.py:374-577).
  * edfmm_targets_potential writes out[i] = k_e * sum_j sigma_j A_j / |x_i - c_j|
  * (FMM, p of the plan; distances clamped at the dtype's epsilon) in the
- * targets' original order.  The targets object keeps a pointer to the plan,
- * which must outlive it.  The electric field is not provided.
+ * targets' original order.  edfmm_targets_field writes the field
+ * out[3 i + c] = k_e * E_c(x_i), E = sum_j sigma_j A_j (x_i - c_j) / |x_i - c_j|^3
+ * (zero for distances within the dtype's epsilon; far part as minus the
+ * gradient of the local expansions), the FMM counterpart of the dense
+ * bem_E_field_targets (electrodrive/core/bem_kernel.py:914).  The targets
+ * object keeps a pointer to the plan, which must outlive it.
  */
 typedef struct edfmm_targets edfmm_targets;
 EDFMM_API int edfmm_targets_create(edfmm_plan *plan, const void *targets_dev, int64_t m, void *stream,
@@ -392,6 +396,8 @@ EDFMM_API int edfmm_targets_export_lists(const edfmm_targets *targets, int64_t *
                                          void *stream);
 EDFMM_API int edfmm_targets_potential(edfmm_targets *targets, const void *sigma_dev, const void *areas_dev, double k_e,
                                       void *out_dev, int flags, void *stream);
+EDFMM_API int edfmm_targets_field(edfmm_targets *targets, const void *sigma_dev, const void *areas_dev, double k_e,
+                                  void *out_dev, int flags, void *stream);
 
 /*
  * Point-cloud warm-start network (no counterpart in the reference: it maps

@@ -67,3 +67,23 @@ def test_solution_field_is_minus_potential_gradient(cuda_lib):
     g = torch.stack([(sol.eval(p + h * d) - sol.eval(p - h * d)) / (2 * h)
                      for d in torch.eye(3, dtype=torch.float64, device="cuda")], dim=1)
     assert float(torch.linalg.norm(e + g) / torch.linalg.norm(e)) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_fmm_field_matches_dense_field(cuda_lib, dtype):
+    """The FMM field at targets (near sums over the P2P lists, minus the
+    gradient of the local expansions) agrees with the dense field to the
+    FMM's accuracy at p = 8, for targets inside, around and outside the cloud."""
+    from electrodrive_gb300.core.bem_kernel import bem_E_field_targets
+
+    rng = np.random.default_rng(11)
+    T = lambda x: torch.as_tensor(x, dtype=dtype, device="cuda")
+    c = T(rng.random((20000, 3)))
+    a = T(rng.uniform(0.5, 1.5, 20000) / 20000)
+    s = T(rng.uniform(-1, 1, 20000))
+    x = T(rng.random((3000, 3)) * 1.6 - 0.3)
+    ed = bem_E_field_targets(x, c, a, s).double()
+    ef = bem_E_field_targets(x, c, a, s, method="fmm").double()
+    assert ef.shape == (3000, 3)
+    assert float(torch.linalg.norm(ef - ed) / torch.linalg.norm(ed)) < 3e-5
