@@ -7,6 +7,7 @@ to a CPU implementation.
 from __future__ import annotations
 
 import ctypes as C
+from typing import Optional
 import os
 import re
 import threading
@@ -78,6 +79,7 @@ def _declare(L):
         "edfmm_targets_field": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
+        "edfmm_plan_set_instance_mask": (i32, [_vp, _vp, i32]),
         "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
         "edfmm_plan_export_tree": (i32, [_vp] * 11),
         "edfmm_plan_export_lists": (i32, [_vp, _vp, _vp, _vp]),
@@ -374,6 +376,17 @@ class Plan:
         with torch.cuda.device(self.device):
             check(self._lib.edfmm_plan_set_charges(self._h, ptr(charges), stream_handle(self.device)),
                   "edfmm_plan_set_charges")
+
+    @property
+    def n_instances(self) -> int:
+        return 1 if self.instance_offsets is None else len(self.instance_offsets) - 1
+
+    def set_instance_mask(self, flags: Optional[torch.Tensor], stride: int = 1):
+        """Batched plans: skip the M2L rows and near-field leaves of instances
+        whose flags[k * stride] is 0 (an FP64 device tensor kept alive by the
+        caller); None removes the mask."""
+        check(self._lib.edfmm_plan_set_instance_mask(self._h, None if flags is None else ptr(flags), int(stride)),
+              "edfmm_plan_set_instance_mask")
 
     def stage(self, name: str, *args):
         fn = getattr(self._lib, f"edfmm_plan_{name}")

@@ -87,6 +87,11 @@ class BEMOperator:
             self.near.apply(sigma, v, v)
         return v
 
+    def set_active_mask(self, flags: Optional[Tensor], stride: int = 1) -> bool:
+        """Forwarded to the FMM base operator (batched plans only)."""
+        fn = getattr(self.base, "set_active_mask", None)
+        return bool(fn(flags, stride)) if fn is not None else False
+
 
 def build_operator(centroids, areas, self_corr: Tensor, *, dtype: torch.dtype, kind: str = "auto",
                    fmm_threshold: int = 20000, near: Optional[NearCorrection] = None, leaf_size: int = 64,

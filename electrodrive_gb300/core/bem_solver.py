@@ -528,35 +528,51 @@ def gmres_batched(A: Callable[[Tensor], Tensor], b: Tensor, segments: List[int],
         g.replay()
         _lib.note_graph_replay(n_k)
 
+    # Operators of batched plans skip the rows of instances that have left
+    # their cycle (the active column of the state) during the Arnoldi steps;
+    # the cycle starts apply the whole operator.
+    set_mask = getattr(A, "set_active_mask", None)
+    active_col = Kr.state[:, Kr.ACTIVE]  # a strided view: flags[k * cols]
+
+    def mask(on: bool):
+        if set_mask is not None:
+            set_mask(active_col if on else None, Kr.state.shape[1])
+
     chunk = max(1, int(check_every))
     total = 0
     r0 = None
     code = 1
     max_cycles = max(1, (maxiter + restart - 1) // restart)
-    for cycle in range(max_cycles + 1):
-        Kr.start(b, A(x), pinv, tolv, cycle == 0)
-        st = Kr.state[:, :10].cpu()
-        if cycle == 0:
-            r0 = st[:, Kr.RTRUE].clone()
-        if bool((st[:, Kr.NONFIN] != 0).any()):
-            code = 5
-            break
-        if not bool((st[:, Kr.ACTIVE] != 0).any()):
-            code = 0
-            break
-        if total >= maxiter:
-            code = 1
-            break
-        steps = min(restart, maxiter - total)
-        j0 = 0
-        while j0 < steps:
-            cnt = min(chunk, steps - j0)
-            run_steps(j0, cnt)
-            j0 += cnt
-            if not bool((Kr.state[:, Kr.ACTIVE] != 0).any()):
+    try:
+        for cycle in range(max_cycles + 1):
+            mask(False)
+            Kr.start(b, A(x), pinv, tolv, cycle == 0)
+            st = Kr.state[:, :10].cpu()
+            if cycle == 0:
+                r0 = st[:, Kr.RTRUE].clone()
+            if bool((st[:, Kr.NONFIN] != 0).any()):
+                code = 5
                 break
-        total += j0
-        Kr.update(j0, x)
+            if not bool((st[:, Kr.ACTIVE] != 0).any()):
+                code = 0
+                break
+            if total >= maxiter:
+                code = 1
+                break
+            steps = min(restart, maxiter - total)
+            j0 = 0
+            mask(True)
+            while j0 < steps:
+                cnt = min(chunk, steps - j0)
+                run_steps(j0, cnt)
+                j0 += cnt
+                if not bool((Kr.state[:, Kr.ACTIVE] != 0).any()):
+                    break
+            mask(False)
+            total += j0
+            Kr.update(j0, x)
+    finally:
+        mask(False)
     st = Kr.state[:, :10].cpu()
     r0s = torch.where(r0 > 0, r0, torch.ones_like(r0))
     converged = (st[:, Kr.RTRUE] <= st[:, Kr.TOLABS])

@@ -69,5 +69,15 @@ class FmmOperator:
         s = sigma if sigma.is_contiguous() else sigma.contiguous()
         return self.plan.matvec(s, self.a, self.si, k_e=self.k_e, out=o, flags=self.flags)
 
+    def set_active_mask(self, flags: Optional[Tensor], stride: int = 1) -> bool:
+        """Batched plans: later applications skip the far-field rows and
+        near-field leaves of instances with flags[k * stride] == 0 (their
+        output rows are then unspecified); None removes the mask.  Returns
+        False when the plan holds a single instance."""
+        if self.plan.n_instances <= 1:
+            return False
+        self.plan.set_instance_mask(flags, stride)
+        return True
+
 
 __all__ = ["DenseOperator", "FmmOperator"]

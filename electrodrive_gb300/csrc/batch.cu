@@ -66,6 +66,7 @@ int pack_batch(std::vector<DevTree> &trees, std::vector<DevLists> &lists, int dt
     T.dtype = dtype;
     T.n_points = P[K];
     T.n_nodes = N[K];
+    T.n_inst = K;
     T.n_leaves = Lf[K];
     T.max_level = max_level;
     T.depth_warnings = 0;
@@ -77,6 +78,12 @@ int pack_batch(std::vector<DevTree> &trees, std::vector<DevLists> &lists, int dt
         (rc = T.is_leaf.reserve(M)) || (rc = T.leaves.reserve(4 * std::max<int64_t>(T.n_leaves, 1))) ||
         (rc = T.level_nodes.reserve(4 * M)))
         return rc;
+    {
+        std::vector<int32_t> no(N.begin(), N.end());
+        if ((rc = T.inst_node_off.reserve(sizeof(int32_t) * (K + 1)))) return rc;
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(T.inst_node_off.p, no.data(), sizeof(int32_t) * (K + 1), cudaMemcpyHostToDevice, s));
+        EDFMM_CUDA_TRY(cudaStreamSynchronize(s));  // the host vector goes out of scope
+    }
     for (int i = 0; i < K; ++i) {
         DevTree &t = trees[i];
         T.depth_warnings += t.depth_warnings;

@@ -141,7 +141,32 @@ struct DevTree {
     DevBuf leaves;     // int32 ids of leaf nodes (ascending)
     std::vector<int32_t> level_offsets;  // host: level l nodes = level_nodes[off[l], off[l+1])
     DevBuf level_nodes;                  // int32 node ids grouped by level
+    // batched plans: instance k owns nodes inst_node_off[k] .. inst_node_off[k+1]-1
+    int n_inst = 0;
+    DevBuf inst_node_off;  // int32 x (n_inst + 1)
 };
+
+// Per-instance activity of a batched plan's matvec: instance k is active
+// when flags[k * stride] != 0 (a column of the batched GMRES state).  M2L
+// rows and near-field leaves of inactive instances are skipped; their
+// outputs are left unspecified (the batched solver does not read them).
+struct InstMask {
+    const int32_t *node_off = nullptr;  // NULL: no mask
+    int n_inst = 0;
+    const double *flags = nullptr;
+    int stride = 0;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ bool inst_active(const InstMask &m, int node) {
+    if (!m.node_off) return true;
+    int lo = 0, hi = m.n_inst - 1;  // last instance whose first node <= node
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (m.node_off[mid] <= node) lo = mid; else hi = mid - 1;
+    }
+    return m.flags[(int64_t)lo * m.stride] != 0.0;
+}
+#endif
 
 int tree_build(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth,
                DevTree &tree, cudaStream_t s);
@@ -188,6 +213,7 @@ struct FmmBuffers {
     DevBuf locals;      // complex T, n_nodes x nc_pad
     DevBuf translated;  // complex T, n_nodes x nc_pad: each node's multipole moved to its parent's centre
     ExtremeRows extreme, extreme_swapped;
+    InstMask mask;  // set around the steps of a batched solve
 };
 
 int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaStream_t s);
@@ -197,7 +223,7 @@ int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool sw
 // rotation-based M2L (m2l_rot.cu), orders 1..8, FP32 and FP64
 int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
-                   cudaStream_t s);
+                   const InstMask &mask, cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
                 FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);

@@ -896,7 +896,7 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
     }
     if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, tree.center.p,
                                 tree.half.p, stree.center.p, stree.half.p, sbuf.multipoles.p, buf.locals.p,
-                                buf.nc_pad, s))
+                                buf.nc_pad, buf.mask, s))
         return rc;
     if (sizeof(T) == 8) return EDFMM_OK;  // FP64 has the range for any scale ratio the tree produces
     // FP32: pairs whose source scale exceeds 256x the target's, skipped above

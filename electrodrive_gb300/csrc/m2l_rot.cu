@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? 3 : 1)
               const typename Vec4<T>::type *__restrict__ tcenter, const typename Vec4<T>::type *__restrict__ thalf,
               const typename Vec4<T>::type *__restrict__ center, const typename Vec4<T>::type *__restrict__ half,
               const typename Vec2<T>::type *__restrict__ Mexp, typename Vec2<T>::type *__restrict__ Lexp,
-              int nc_pad) {
+              int nc_pad, const InstMask mask) {
     using T2 = typename Vec2<T>::type;
     constexpr int NV = (P + 1) * (P + 1), NQ = (P + 1) * (P + 2) / 2, NT = kRotThreads;
     extern __shared__ __align__(16) unsigned char rot_smem[];
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? 3 : 1)
     AccC<T, NT> acc{sq + threadIdx.x};
     const int64_t t = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const bool live = t < n_nodes;
+    const bool live = t < n_nodes && inst_active(mask, (int)t);
     typename Vec4<T>::type ct{};
     T iaL = T(1);
     int b = 0, e = 0;
@@ -367,7 +367,7 @@ inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <typename T, int P, bool V_IN_SMEM>
 int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal, const void *cen,
-               const void *hal, const void *Mx, void *Lx, int nc_pad, cudaStream_t s) {
+               const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
     using T2 = typename Vec2<T>::type;
     constexpr int NV = (P + 1) * (P + 1), NQ = (P + 1) * (P + 2) / 2, NT = kRotThreads;
@@ -378,7 +378,7 @@ int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tc
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot shared memory attribute: ") + cudaGetErrorString(attr));
     k_m2l_rot<T, P, V_IN_SMEM><<<nblk(M * 32, NT), NT, smem, s>>>(
         M, off, src, static_cast<const T4 *>(tcen), static_cast<const T4 *>(thal), static_cast<const T4 *>(cen),
-        static_cast<const T4 *>(hal), static_cast<const T2 *>(Mx), static_cast<T2 *>(Lx), nc_pad);
+        static_cast<const T4 *>(hal), static_cast<const T2 *>(Mx), static_cast<T2 *>(Lx), nc_pad, mask);
     EDFMM_LAUNCH_CHECK("k_m2l_rot");
     return EDFMM_OK;
 }
@@ -387,15 +387,17 @@ int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tc
 
 // Rotation-based M2L for expansion orders 1..8 (FP32: pairs with a source
 // scale above 256x the target's are left to the caller's generic kernel).
+// Rows of instances inactive under ``mask`` are skipped (their locals are
+// left as they were).
 int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
-                   cudaStream_t s) {
+                   const InstMask &mask, cudaStream_t s) {
     if (M <= 0) return EDFMM_OK;
 #define EDFMM_ROT_CASE(PP)                                                                                    \
     case PP:                                                                                                  \
         return dtype == EDFMM_F64                                                                             \
-                   ? launch_rot<double, PP, true>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, s)       \
-                   : launch_rot<float, PP, false>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, s);
+                   ? launch_rot<double, PP, true>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s) \
+                   : launch_rot<float, PP, false>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
     switch (p) {
         EDFMM_ROT_CASE(1)
         EDFMM_ROT_CASE(2)

@@ -84,6 +84,7 @@ template <typename T> struct NearParams {
     int near;
     int far;
     const T *add_in;  // tree-order near sums computed by an earlier pass (nullable)
+    InstMask mask;    // batched plans: leaves of inactive instances are skipped
     // epilogue
     int scatter;
     const int32_t *index_map;
@@ -342,6 +343,7 @@ template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 
     const int64_t w = (int64_t)blockIdx.x * 4 + wl;
     if (w >= P.n_leaves) return;
     const int t = P.leaves[w];
+    if (!inst_active(P.mask, t)) return;  // uniform over the warp; the kernel has no block barrier
     if (P.far) {
         const int nc = ncoef(P.p);
         for (int k = lane; k < nc; k += 32) sL[wl][k] = P.Lexp[(int64_t)t * P.nc_pad + k];
@@ -396,6 +398,7 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     P.near = a.near ? 1 : 0;
     P.far = a.far ? 1 : 0;
     P.add_in = static_cast<const T *>(a.add_in);
+    P.mask = a.src_tree ? InstMask{} : buf.mask;
     P.scatter = a.scatter ? 1 : 0;
     P.index_map = dptr<int32_t>(tree.index_map);
     P.sigma = static_cast<const T *>(a.sigma);

@@ -209,6 +209,23 @@ int edfmm_plan_rebuild_lists(edfmm_plan *p, double mac_theta, void *stream) {
     return EDFMM_OK;
 }
 
+int edfmm_plan_set_instance_mask(edfmm_plan *p, const double *flags_dev, int stride) {
+    if (int rc = check_plan(p)) return rc;
+    if (!flags_dev) {
+        p->fmm.mask = InstMask{};
+        return EDFMM_OK;
+    }
+    if (p->tree.n_inst <= 0) return fail(EDFMM_ERR_ARG, "the instance mask needs a batched plan");
+    if (stride < 1) return fail(EDFMM_ERR_ARG, "stride must be >= 1");
+    InstMask m;
+    m.node_off = dptr<int32_t>(p->tree.inst_node_off);
+    m.n_inst = p->tree.n_inst;
+    m.flags = flags_dev;
+    m.stride = stride;
+    p->fmm.mask = m;
+    return EDFMM_OK;
+}
+
 int edfmm_plan_set_order(edfmm_plan *p, int expansion_order, void *stream) {
     if (int rc = check_plan(p)) return rc;
     if (expansion_order < 1 || expansion_order > 10)

@@ -112,6 +112,12 @@ EDFMM_API int edfmm_plan_rebuild_lists(edfmm_plan *plan, double mac_theta, void 
  * electrodrive/fmm3d/config.py:90-106); reallocates the expansion buffers.
  */
 EDFMM_API int edfmm_plan_set_order(edfmm_plan *plan, int expansion_order, void *stream);
+/* Batched plans: from now on a matvec skips the M2L rows and near-field
+ * leaves of every instance k with flags_dev[k * stride] == 0.0 (FP64 device
+ * array, read when the kernels run, so a captured graph follows its changes);
+ * those instances' outputs are left unspecified.  NULL removes the mask.
+ * Used by the batched GMRES while instances sit out the rest of a cycle. */
+EDFMM_API int edfmm_plan_set_instance_mask(edfmm_plan *plan, const double *flags_dev, int stride);
 
 EDFMM_API int edfmm_plan_get_info(const edfmm_plan *plan, edfmm_plan_info *info_out);
 
