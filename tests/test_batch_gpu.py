@@ -129,3 +129,37 @@ def test_batched_learned_start_equals_per_instance_warm_start(cuda_lib):
     r_learned = segment_norms(system.b - system.op64(x0), system.offsets) / bn
     r_cold = segment_norms(system.b - system.op64(system.x0_cold), system.offsets) / bn
     assert bool((r_learned < r_cold).all()), (r_learned, r_cold)
+
+
+def test_instance_mask_skips_inactive_instances_only(cuda_lib):
+    """With an instance mask, the rows of active instances are bit-identical
+    to the unmasked matvec; the mask is read when the kernels run."""
+    from electrodrive_gb300._lib import Plan
+
+    sizes = [900, 2500, 400, 3000]
+    pts = _instances(8, sizes)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    allp = torch.as_tensor(np.concatenate(pts), dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(9)
+    sigma = torch.as_tensor(rng.uniform(-1, 1, off[-1]), dtype=torch.float32, device="cuda")
+    areas = torch.full((int(off[-1]),), 1e-3, dtype=torch.float32, device="cuda")
+    plan = Plan(allp, leaf_size=32, expansion_order=8, instance_offsets=off)
+    full = plan.matvec(sigma, areas, None, k_e=1.0).clone()
+    state = torch.zeros(4, 3, dtype=torch.float64, device="cuda")  # flags in column 1, stride 3
+    state[[0, 2], 1] = 1.0
+    plan.set_instance_mask(state[:, 1], 3)
+    try:
+        masked = plan.matvec(sigma, areas, None, k_e=1.0).clone()
+        for k in (0, 2):
+            a, b = int(off[k]), int(off[k + 1])
+            assert torch.equal(masked[a:b], full[a:b]), k
+        state[1, 1] = 1.0  # flags change on the device: the next matvec follows them
+        again = plan.matvec(sigma, areas, None, k_e=1.0).clone()
+        a, b = int(off[1]), int(off[2])
+        assert torch.equal(again[a:b], full[a:b])
+    finally:
+        plan.set_instance_mask(None)
+    assert torch.equal(plan.matvec(sigma, areas, None, k_e=1.0), full)
+    single = Plan(allp[:900].contiguous(), leaf_size=32)
+    with pytest.raises(Exception):
+        single.set_instance_mask(state[:, 1], 3)  # needs a batched plan
