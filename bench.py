@@ -648,6 +648,11 @@ def run_batch_workload(args, rank, world, local):
     x2.cpu()
     e2e_ms = 1e3 * (time.perf_counter() - t0)
     del sys2
+    # the same set-up once more, synchronised at each phase end, for its breakdown
+    setup_phases = {}
+    sys3 = BatchSystem(cases, device=dev, inner_leaf_size=tune["leaf_size"],
+                       inner_expansion_order=tune["expansion_order"], timings=setup_phases)
+    del sys3
     if rank == 0:
         order = tune["expansion_order"]
         flops_pair = m2l_flops_per_pair(order) if 1 <= order <= 8 else None
@@ -690,7 +695,8 @@ def run_batch_workload(args, rank, world, local):
                "e2e": {"value": world * K * 1e3 / e2e_ms, "unit": "solves/s",
                        "h2d_bytes_per_step": int(n_total * 8 * (3 + 1 + 9)), "d2h_bytes_per_step": int(8 * n_total),
                        "ms_per_step": e2e_ms, "includes": "batched set-up from the host meshes (trees, lists, "
-                                                           "self integrals, rhs), the solve and the read-back"},
+                                                           "self integrals, rhs), the solve and the read-back",
+                       "setup_phases_ms": setup_phases},
                "gpu_launches": int(launches), "clocks": clk.summary(),
                "roofline": {"kernel": f"k_m2l_rot<float, {order}> (M2L of the FP32 inner operator)", "bound": "fp32",
                             "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",

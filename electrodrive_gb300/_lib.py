@@ -70,6 +70,7 @@ def _declare(L):
         "edfmm_launch_count": (i64, []),
         "edfmm_plan_create": (i32, [_vp, i64, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_create_batch": (i32, [_vp, C.POINTER(i64), i32, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
+        "edfmm_plan_convert": (i32, [_vp, i32, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_destroy": (i32, [_vp]),
         "edfmm_targets_create": (i32, [_vp, _vp, i64, _vp, C.POINTER(_vp)]),
         "edfmm_targets_destroy": (i32, [_vp]),
@@ -110,6 +111,7 @@ def _declare(L):
         "edfmm_self_integrals": (i32, [_vp, _vp, i64, i32, i32, dbl, _vp, _vp]),
         "edfmm_near_targets_correct": (i32, [_vp, i64, _vp, _vp, _vp, _vp, i64, dbl, i32, i32, dbl, _vp, _vp]),
         "edfmm_near_create": (i32, [_vp, _vp, _vp, i64, dbl, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
+        "edfmm_near_convert": (i32, [_vp, i32, _vp, C.POINTER(_vp)]),
         "edfmm_near_destroy": (i32, [_vp]),
         "edfmm_near_num_pairs": (i64, [_vp]),
         "edfmm_near_export": (i32, [_vp, _vp, _vp, _vp]),
@@ -270,6 +272,21 @@ class Plan:
         info = PlanInfo()
         check(L.edfmm_plan_get_info(h, C.byref(info)), "edfmm_plan_get_info")
         self.info = info
+
+    def convert(self, dtype: torch.dtype, expansion_order: Optional[int] = None) -> "Plan":
+        """A plan in ``dtype`` (and ``expansion_order``, default this plan's)
+        over this plan's partition: tree, lists and instances copied, point
+        and node geometry cast, no new tree or list build."""
+        order = int(self.info.expansion_order if expansion_order is None else expansion_order)
+        h = _vp()
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_convert(self._h, dtype_code(dtype), order, stream_handle(self.device),
+                                               C.byref(h)), "edfmm_plan_convert")
+        out = Plan.__new__(Plan)
+        out.device, out.dtype, out.instance_offsets = self.device, dtype, self.instance_offsets
+        out._h, out._lib = h, self._lib
+        out._refresh_info()
+        return out
 
     @property
     def handle(self):

@@ -81,9 +81,21 @@ class BatchSystem:
 
     def __init__(self, cases: Sequence[Tuple[TriMesh, Dict[str, Any]]], *, leaf_size: int = 64,
                  expansion_order: int = 8, inner_leaf_size: Optional[int] = None,
-                 inner_expansion_order: Optional[int] = None, device=None):
+                 inner_expansion_order: Optional[int] = None, device=None,
+                 timings: Optional[Dict[str, float]] = None):
+        """``timings``, when given, receives the wall time in ms of each set-up
+        phase (the device is synchronised at every phase end, so pass it only
+        to measure)."""
         dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.device = dev
+        clock = [time.perf_counter()]
+
+        def mark(name):
+            if timings is not None:
+                torch.cuda.synchronize(dev)
+                now = time.perf_counter()
+                timings[name] = 1e3 * (now - clock[0])
+                clock[0] = now
         self.cases = list(cases)
         sizes = [m.n_panels for m, _ in self.cases]
         self.offsets = [0] + list(np.cumsum(sizes).astype(int))
@@ -95,9 +107,11 @@ class BatchSystem:
         PV = np.concatenate([m.vertices[m.triangles] for m, _ in self.cases])
         self.C64 = torch.as_tensor(C, dtype=torch.float64, device=dev)
         self.areas = torch.as_tensor(A, dtype=torch.float64, device=dev)
+        mark("host_concat_and_copy")
         I_self = self_integrals(PV, C, order=2, depth=3, device=dev)
         self.self_corr = I_self / self.areas.clamp_min(torch.finfo(torch.float64).tiny)
         self.diag = I_self.clamp_min(1e-18)
+        mark("self_integrals")
         b = torch.zeros(self.n, dtype=torch.float64, device=dev)
         for k, (m, spec) in enumerate(self.cases):
             a, e = self.offsets[k], self.offsets[k + 1]
@@ -106,13 +120,22 @@ class BatchSystem:
                 b[a:e] = -point_charge_potential(self.C64[a:e], ch)
         self.b = b
         self.x0_cold = b / self.diag
+        mark("rhs")
         self.op64 = self.make_operator(torch.float64, leaf_size, expansion_order)
+        mark("fp64_plan")
         self.op32 = self.make_operator(torch.float32, inner_leaf_size or leaf_size,
                                        inner_expansion_order or expansion_order)
+        mark("fp32_plan")
 
     def make_operator(self, dtype, leaf_size: int, expansion_order: int) -> FmmOperator:
-        plan = _lib.Plan(self.C64.to(dtype).contiguous(), leaf_size=leaf_size, expansion_order=expansion_order,
-                         instance_offsets=self.offsets)
+        """A batched operator; with the FP64 operator's leaf size it shares
+        that operator's partition (plan converted, no second tree build)."""
+        op64 = getattr(self, "op64", None)
+        if op64 is not None and leaf_size == int(op64.plan.info.leaf_size):
+            plan = op64.plan.convert(dtype, expansion_order)
+        else:
+            plan = _lib.Plan(self.C64.to(dtype).contiguous(), leaf_size=leaf_size, expansion_order=expansion_order,
+                             instance_offsets=self.offsets)
         return FmmOperator(plan, self.areas.to(dtype), self.self_corr.to(dtype))
 
     def solve(self, x0: Optional[Tensor] = None, rtol: float = 1e-6, inner_restart: int = 100,

@@ -93,6 +93,20 @@ class BEMOperator:
         return bool(fn(flags, stride)) if fn is not None else False
 
 
+def converted_operator(op, areas, self_corr: Tensor, *, dtype: torch.dtype, expansion_order: int,
+                       near: Optional[NearCorrection] = None) -> Optional[BEMOperator]:
+    """``op``'s FMM partition in another dtype and expansion order (its plan
+    converted: no second tree or list build), or None when ``op`` is not an
+    FMM operator."""
+    base = getattr(op, "base", op)
+    if not isinstance(base, FmmOperator):
+        return None
+    dev = base.plan.device
+    a = areas if isinstance(areas, Tensor) else torch.as_tensor(np.asarray(areas))
+    plan = base.plan.convert(dtype, expansion_order)
+    return BEMOperator(FmmOperator(plan, a.to(dev, dtype), self_corr.to(dev, dtype)), near)
+
+
 def build_operator(centroids, areas, self_corr: Tensor, *, dtype: torch.dtype, kind: str = "auto",
                    fmm_threshold: int = 20000, near: Optional[NearCorrection] = None, leaf_size: int = 64,
                    theta: float = 0.5, expansion_order: int = 8, device=None) -> BEMOperator:
@@ -203,9 +217,13 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
                         device=dev)
     op32 = None
     if mixed:
-        op32 = build_operator(C64, A64, self_corr.to(torch.float32), dtype=torch.float32, kind=operator,
-                              fmm_threshold=fmm_threshold, near=make_near(torch.float32), device=dev,
-                              expansion_order=inner_expansion_order or 8)
+        near32 = None if near is None else near.astype(torch.float32)
+        op32 = converted_operator(op, A64, self_corr, dtype=torch.float32, expansion_order=inner_expansion_order or 8,
+                                  near=near32)
+        if op32 is None:
+            op32 = build_operator(C64, A64, self_corr.to(torch.float32), dtype=torch.float32, kind=operator,
+                                  fmm_threshold=fmm_threshold, near=near32, device=dev,
+                                  expansion_order=inner_expansion_order or 8)
     charges = point_charges(spec)
     C_dev = C64.to(dev, dtype)
     V_free = point_charge_potential(C_dev, charges) if charges else torch.zeros(N, dtype=dtype, device=dev)
@@ -273,9 +291,15 @@ def assemble_system(mesh: TriMesh, spec: Any, *, kind: str = "dense", dtypes=(to
     A_dev = A64.to(dev)
     self_corr = I_self / A_dev.clamp_min(torch.finfo(torch.float64).tiny)
     ops = {}
+    nc0 = None
     for dt in dtypes:
-        nc = (NearCorrection(mesh.centroids, mesh.areas, PV, distance_factor=1.5, order=2, depth=depth_near, dtype=dt,
-                             device=dev) if near and mesh.n_panels > 1 else None)
+        nc = None
+        if near and mesh.n_panels > 1:
+            # one pair search and quadrature; the other dtypes cast its weights
+            if nc0 is None:
+                nc0 = NearCorrection(mesh.centroids, mesh.areas, PV, distance_factor=1.5, order=2, depth=depth_near,
+                                     dtype=dt, device=dev)
+            nc = nc0.astype(dt)
         ops[dt] = build_operator(C64, A64, self_corr.to(dt), dtype=dt, kind=kind, near=nc, device=dev)
     charges = point_charges(spec)
     V_free = point_charge_potential(C64.to(dev), charges) if charges else torch.zeros(mesh.n_panels, dtype=torch.float64,
@@ -303,10 +327,15 @@ def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: T
     ref = op64(probe).to(torch.float64).clone()
     stream = torch.cuda.current_stream(dev)
     trials, best = [], None
+    base64 = getattr(op64, "base", op64)
+    leaf64 = int(base64.plan.info.leaf_size) if isinstance(base64, FmmOperator) else None
     for leaf in leaf_sizes:
         for p in orders:
-            op = build_operator(centroids, areas, self_corr.to(torch.float32), dtype=torch.float32, kind="fmm",
-                                near=near, leaf_size=leaf, expansion_order=p, device=dev)
+            op = (converted_operator(op64, areas, self_corr, dtype=torch.float32, expansion_order=p, near=near)
+                  if leaf == leaf64 else None)
+            if op is None:
+                op = build_operator(centroids, areas, self_corr.to(torch.float32), dtype=torch.float32, kind="fmm",
+                                    near=near, leaf_size=leaf, expansion_order=p, device=dev)
             x = probe.float()
             op(x)
             times = []

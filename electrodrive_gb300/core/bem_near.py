@@ -59,6 +59,20 @@ class NearCorrection:
         self._h = h
         self.n_pairs = int(L.edfmm_near_num_pairs(h))
 
+    def astype(self, dtype: torch.dtype) -> "NearCorrection":
+        """The same pairs and FP64 weights for a solve in ``dtype`` (no new
+        pair search or quadrature; equal to building it with that dtype)."""
+        if dtype == self.dtype:
+            return self
+        out = NearCorrection.__new__(NearCorrection)
+        out.device, out.dtype, out._L, out.n, out.n_pairs = self.device, dtype, self._L, self.n, self.n_pairs
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self._L.edfmm_near_convert(self._h, _lib.dtype_code(dtype), _lib.stream_handle(self.device),
+                                                  C.byref(h)), "edfmm_near_convert")
+        out._h = h
+        return out
+
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             self._L.edfmm_near_destroy(self._h)

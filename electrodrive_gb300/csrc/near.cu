@@ -546,6 +546,47 @@ EDFMM_API int edfmm_near_create(const void *centroids_dev, const void *areas_dev
     return done(EDFMM_OK);
 }
 
+EDFMM_API int edfmm_near_convert(const edfmm_near *src, int dtype, void *stream, edfmm_near **out) {
+    if (!out) return fail(EDFMM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!src) return fail(EDFMM_ERR_ARG, "near handle is NULL");
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "bad dtype");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    edfmm_near *h = new edfmm_near();
+    h->n = src->n;
+    h->n_pairs = src->n_pairs;
+    h->max_row = src->max_row;
+    h->dtype = dtype;
+    int rc = EDFMM_OK;
+    auto done = [&](int r) {
+        if (r) delete h;
+        else *out = h;
+        return r;
+    };
+    const int64_t np = src->n_pairs;
+    if ((rc = h->row_off.reserve(sizeof(int32_t) * (h->n + 1)))) return done(rc);
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(h->row_off.p, src->row_off.p, sizeof(int32_t) * (h->n + 1),
+                                   cudaMemcpyDeviceToDevice, s));
+    if (src->cols.p) {
+        if ((rc = h->cols.reserve(4 * std::max<int64_t>(np, 1))) ||
+            (rc = h->w64.reserve(8 * std::max<int64_t>(np, 1))) ||
+            (rc = h->w.reserve((dtype == EDFMM_F64 ? 8 : 4) * std::max<int64_t>(np, 1))))
+            return done(rc);
+    }
+    if (np > 0) {
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(h->cols.p, src->cols.p, 4 * np, cudaMemcpyDeviceToDevice, s));
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(h->w64.p, src->w64.p, 8 * np, cudaMemcpyDeviceToDevice, s));
+        if (dtype == EDFMM_F64) {
+            EDFMM_CUDA_TRY(cudaMemcpyAsync(h->w.p, src->w64.p, 8 * np, cudaMemcpyDeviceToDevice, s));
+        } else {
+            k_cast<float><<<nb(np, 256), 256, 0, s>>>(dptr<double>(src->w64), dptr<float>(h->w), np);
+            EDFMM_LAUNCH_CHECK("k_cast");
+        }
+    }
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return done(EDFMM_OK);
+}
+
 EDFMM_API int edfmm_near_destroy(edfmm_near *h) {
     delete h;
     return EDFMM_OK;

@@ -66,6 +66,55 @@ __global__ void k_export_coeffs(int64_t M, int nc, int nc_pad, const Cplx<T> *in
     out[i] = in[node * nc_pad + c];
 }
 
+template <typename Tin, typename Tout>
+__global__ void k_cast_vals(const Tin *in, Tout *out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (Tout)in[i];
+}
+
+// whole-buffer device copy
+int clone_buf(const DevBuf &src, DevBuf &dst, cudaStream_t s) {
+    if (!src.p) return EDFMM_OK;
+    if (int rc = dst.reserve(src.bytes)) return rc;
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(dst.p, src.p, src.bytes, cudaMemcpyDeviceToDevice, s));
+    return EDFMM_OK;
+}
+
+// n values of the source dtype into a new buffer of the target dtype
+int cast_buf(const DevBuf &src, int sdt, DevBuf &dst, int ddt, int64_t n, cudaStream_t s) {
+    if (int rc = dst.reserve((ddt == EDFMM_F64 ? 8 : 4) * (size_t)std::max<int64_t>(n, 1))) return rc;
+    if (n <= 0) return EDFMM_OK;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    if (sdt == ddt) {
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(dst.p, src.p, (sdt == EDFMM_F64 ? 8 : 4) * (size_t)n,
+                                       cudaMemcpyDeviceToDevice, s));
+    } else if (sdt == EDFMM_F64) {
+        k_cast_vals<double, float><<<g, 256, 0, s>>>(dptr<double>(src), dptr<float>(dst), n);
+        EDFMM_LAUNCH_CHECK("k_cast_vals");
+    } else {
+        k_cast_vals<float, double><<<g, 256, 0, s>>>(dptr<float>(src), dptr<double>(dst), n);
+        EDFMM_LAUNCH_CHECK("k_cast_vals");
+    }
+    return EDFMM_OK;
+}
+
+int alloc_expansions(edfmm_plan *p, int dtype, int expansion_order, cudaStream_t s) {
+    p->fmm.p = expansion_order;
+    p->fmm.nc = num_coeffs(expansion_order);
+    p->fmm.nc_pad = (p->fmm.nc + 1) & ~1;
+    size_t esz = (dtype == EDFMM_F64 ? 16 : 8) * (size_t)p->fmm.nc_pad * (size_t)std::max<int64_t>(p->tree.n_nodes, 1);
+    int rc = p->fmm.multipoles.reserve(esz);
+    if (!rc) rc = p->fmm.locals.reserve(esz);
+    if (!rc) rc = p->fmm.translated.reserve(esz);
+    if (!rc) {
+        cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("plan set-up: ") + cudaGetErrorString(e));
+    }
+    return rc;
+}
+
 int check_plan(const edfmm_plan *p) {
     if (!p) return fail(EDFMM_ERR_ARG, "plan is NULL");
     return EDFMM_OK;
@@ -185,6 +234,57 @@ int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int 
             if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("plan set-up: ") + cudaGetErrorString(e));
         }
     }
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *plan_out = p;
+    return EDFMM_OK;
+}
+
+int edfmm_plan_convert(const edfmm_plan *src, int dtype, int expansion_order, void *stream, edfmm_plan **plan_out) {
+    if (!plan_out) return fail(EDFMM_ERR_ARG, "plan_out is NULL");
+    *plan_out = nullptr;
+    if (int rc = check_plan(src)) return rc;
+    if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "dtype must be EDFMM_F32 or EDFMM_F64");
+    if (expansion_order < 1 || expansion_order > 10)
+        return fail(EDFMM_ERR_UNSUPPORTED, "expansion_order must be in [1, 10]");
+    cudaStream_t s = S(stream);
+    edfmm_plan *p = new edfmm_plan();
+    cudaGetDevice(&p->device);
+    p->mac_theta = src->mac_theta;
+    p->leaf_size = src->leaf_size;
+    p->max_depth = src->max_depth;
+    const DevTree &a = src->tree;
+    DevTree &t = p->tree;
+    t.dtype = dtype;
+    t.n_points = a.n_points;
+    t.n_nodes = a.n_nodes;
+    t.n_leaves = a.n_leaves;
+    t.max_level = a.max_level;
+    t.depth_warnings = a.depth_warnings;
+    t.level_offsets = a.level_offsets;
+    t.n_inst = a.n_inst;
+    const DevLists &la = src->lists;
+    DevLists &l = p->lists;
+    l.n_p2p = la.n_p2p;
+    l.n_m2l = la.n_m2l;
+    l.p2p_interactions = la.p2p_interactions;
+    l.max_p2p_row = la.max_p2p_row;
+    l.max_m2l_row = la.max_m2l_row;
+    l.have_m2l_swapped = la.have_m2l_swapped;
+    int rc = EDFMM_OK;
+    if (!rc) rc = cast_buf(a.pts, a.dtype, t.pts, dtype, 4 * a.n_points, s);
+    if (!rc) rc = cast_buf(a.center, a.dtype, t.center, dtype, 4 * a.n_nodes, s);
+    if (!rc) rc = cast_buf(a.half, a.dtype, t.half, dtype, 4 * a.n_nodes, s);
+    const DevBuf *from[] = {&a.index_map, &a.range, &a.parent, &a.children, &a.level, &a.is_leaf, &a.leaves,
+                            &a.level_nodes, &a.inst_node_off, &la.p2p_off, &la.p2p_src, &la.m2l_off, &la.m2l_src,
+                            &la.m2l_swapped_off, &la.m2l_swapped_src};
+    DevBuf *to[] = {&t.index_map, &t.range, &t.parent, &t.children, &t.level, &t.is_leaf, &t.leaves,
+                    &t.level_nodes, &t.inst_node_off, &l.p2p_off, &l.p2p_src, &l.m2l_off, &l.m2l_src,
+                    &l.m2l_swapped_off, &l.m2l_swapped_src};
+    for (size_t i = 0; !rc && i < sizeof(from) / sizeof(from[0]); ++i) rc = clone_buf(*from[i], *to[i], s);
+    if (!rc) rc = alloc_expansions(p, dtype, expansion_order, s);  // synchronises the stream
     if (rc) {
         delete p;
         return rc;

@@ -98,6 +98,14 @@ EDFMM_API int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, in
 EDFMM_API int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int n_instances, int dtype,
                                       int leaf_size, int max_depth, double mac_theta, int expansion_order,
                                       void *stream, edfmm_plan **plan_out);
+/*
+ * A plan in another dtype and expansion order over the same partition: the
+ * source plan's tree, lists and instance layout are copied and its point and
+ * node geometry cast to `dtype` (no new tree or list build).  The source plan
+ * is not modified; charges are set on the new plan as on any other.
+ */
+EDFMM_API int edfmm_plan_convert(const edfmm_plan *plan, int dtype, int expansion_order, void *stream,
+                                 edfmm_plan **plan_out);
 EDFMM_API int edfmm_plan_destroy(edfmm_plan *plan);
 
 /*
@@ -333,6 +341,9 @@ typedef struct edfmm_near edfmm_near;
 EDFMM_API int edfmm_near_create(const void *centroids_dev, const void *areas_dev, const void *panel_vertices_dev,
                                 int64_t n, double distance_factor, int quad_order, int depth, double k_e, int dtype,
                                 void *stream, edfmm_near **near_out);
+/* The same pairs and FP64 weights held for another solve dtype (no new pair
+ * search or quadrature): the result equals edfmm_near_create with `dtype`. */
+EDFMM_API int edfmm_near_convert(const edfmm_near *near_set, int dtype, void *stream, edfmm_near **near_out);
 EDFMM_API int edfmm_near_destroy(edfmm_near *near_set);
 EDFMM_API int64_t edfmm_near_num_pairs(const edfmm_near *near_set);
 /* (P, 2) int64 (i, j) pairs in row order and FP64 weights; either may be NULL */

@@ -123,6 +123,17 @@ def test_new_entry_points_reject_bad_arguments_before_touching_the_gpu(edlib):
     assert edlib.edfmm_bgmres_arnoldi(10, 0, 2, None, 5, 8, 8, None, None, None, None, None, None, None) == E
     assert edlib.edfmm_bgmres_update(10, 0, 2, None, 5, 8, 9, None, None, None, None, None) == E
     assert int(edlib.edfmm_bgmres_state_cols(40)) == 50
+    # near-set conversion: NULL handle or output, bad dtype
+    import ctypes
+    h = ctypes.c_void_p()
+    assert edlib.edfmm_near_convert(None, 0, None, ctypes.byref(h)) == E
+    assert edlib.edfmm_near_convert(None, 0, None, None) == E
+    assert edlib.edfmm_near_convert(ctypes.c_void_p(1), 7, None, ctypes.byref(h)) == E and not h.value
+    # plan conversion: NULL plan or output, bad dtype, order out of range
+    assert edlib.edfmm_plan_convert(None, 0, 8, None, ctypes.byref(h)) == E and not h.value
+    assert edlib.edfmm_plan_convert(ctypes.c_void_p(1), 0, 8, None, None) == E
+    assert edlib.edfmm_plan_convert(ctypes.c_void_p(1), 5, 8, None, ctypes.byref(h)) == E
+    assert edlib.edfmm_plan_convert(ctypes.c_void_p(1), 0, 11, None, ctypes.byref(h)) == _lib.EDFMM_ERR_UNSUPPORTED
     assert int(edlib.edfmm_bgmres_work_bytes(3, 2000, 40)) > 0
 
 

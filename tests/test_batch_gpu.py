@@ -163,3 +163,58 @@ def test_instance_mask_skips_inactive_instances_only(cuda_lib):
     single = Plan(allp[:900].contiguous(), leaf_size=32)
     with pytest.raises(Exception):
         single.set_instance_mask(state[:, 1], 3)  # needs a batched plan
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_converted_plan_shares_the_partition(cuda_lib, batched):
+    """edfmm_plan_convert: same dtype and order gives a bit-identical matvec;
+    an FP32 plan converted from an FP64 one has the FP64 plan's tree and
+    lists (geometry cast) and its matvec is within FP32 rounding of the FP64
+    one; a batched plan keeps its instances (the mask works on the copy)."""
+    from electrodrive_gb300._lib import Plan
+
+    sizes = [1500, 4000, 700] if batched else [6000]
+    pts = _instances(11, sizes)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    allp = torch.as_tensor(np.concatenate(pts), dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(12)
+    sigma = torch.as_tensor(rng.uniform(-1, 1, off[-1]), dtype=torch.float64, device="cuda")
+    areas = torch.full((int(off[-1]),), 1e-3, dtype=torch.float64, device="cuda")
+    src = Plan(allp, leaf_size=32, expansion_order=8, instance_offsets=off if batched else None)
+    v64 = src.matvec(sigma, areas, None, k_e=1.0).clone()
+    same = src.convert(torch.float64)
+    assert torch.equal(same.matvec(sigma, areas, None, k_e=1.0), v64)
+    p32 = src.convert(torch.float32, 8)
+    assert p32.dtype == torch.float32 and p32.info.expansion_order == 8
+    for f in ("n_points", "n_nodes", "n_leaves", "n_m2l_pairs", "n_p2p_pairs", "p2p_interactions"):
+        assert getattr(p32.info, f) == getattr(src.info, f), f
+    t64, t32 = src.export_tree(), p32.export_tree()
+    assert torch.equal(t64["index_map"], t32["index_map"])
+    assert torch.equal(t64["node_children"], t32["node_children"])
+    assert torch.equal(t64["node_centers"].float(), t32["node_centers"])
+    l64, l32 = src.export_lists(), p32.export_lists()
+    assert all(torch.equal(a, b) for a, b in zip(l64, l32))
+    v32 = p32.matvec(sigma.float(), areas.float(), None, k_e=1.0).double()
+    err = float(torch.linalg.norm(v32 - v64) / torch.linalg.norm(v64))
+    fresh = Plan(allp.float(), leaf_size=32, expansion_order=8, instance_offsets=off if batched else None)
+    vf = fresh.matvec(sigma.float(), areas.float(), None, k_e=1.0).double()
+    err_fresh = float(torch.linalg.norm(vf - v64) / torch.linalg.norm(v64))
+    # as close to the FP64 operator as an FP32 plan built from the FP32 points
+    assert err < 1e-5 and err < 2 * err_fresh + 1e-7, (err, err_fresh)
+    p6 = src.convert(torch.float32, 6)
+    assert p6.info.expansion_order == 6 and p6.info.n_m2l_pairs == src.info.n_m2l_pairs
+    v6 = p6.matvec(sigma.float(), areas.float(), None, k_e=1.0).double()
+    assert float(torch.linalg.norm(v6 - v64) / torch.linalg.norm(v64)) < 1e-4
+    del src  # the copies own their buffers
+    assert torch.equal(p32.matvec(sigma.float(), areas.float(), None, k_e=1.0).double(), v32)
+    if batched:
+        assert p32.n_instances == len(sizes)
+        state = torch.zeros(len(sizes), dtype=torch.float64, device="cuda")
+        state[1] = 1.0
+        p32.set_instance_mask(state, 1)
+        try:
+            m = p32.matvec(sigma.float(), areas.float(), None, k_e=1.0).double()
+        finally:
+            p32.set_instance_mask(None)
+        a, b = int(off[1]), int(off[2])
+        assert torch.equal(m[a:b], v32[a:b])

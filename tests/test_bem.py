@@ -92,6 +92,15 @@ def test_gpu_near_field_matches_reference(cuda_lib, name):
     o32 = torch.zeros(sig.shape[0], device="cuda")
     nc32.apply(sig.float(), None, o32)
     assert rel(o32.cpu().numpy(), NEAR[f"{name}__v_corr"]) < 1e-5
+    # the FP32 set cast from the FP64 one (no second pair search) is the same set
+    cv = nc.astype(torch.float32)
+    assert cv.n_pairs == nc32.n_pairs
+    pc, wc = cv.export()
+    assert torch.equal(pc, pairs) and torch.equal(wc, w)
+    oc = torch.zeros_like(o32)
+    cv.apply(sig.float(), None, oc)
+    assert torch.equal(oc, o32)
+    assert nc.astype(torch.float64) is nc
 
 
 @pytest.mark.gpu
