@@ -38,6 +38,24 @@ void count_launch(int n = 1);
 // ---------------------------------------------------------------------------
 // device buffer (owning)
 // ---------------------------------------------------------------------------
+// Blocks released while a BlockCacheScope is active on this thread are kept
+// for the scope's later reserves instead of being freed: a build that runs on
+// ONE stream then reuses its temporaries in stream order without a
+// cudaMalloc / cudaFree (which synchronises the device) per temporary.  The
+// scope frees what it still holds when it ends.
+struct BlockCache;
+BlockCache *block_cache();  // this thread's active cache or NULL
+void *block_cache_take(BlockCache *c, size_t nbytes, size_t *got);
+void block_cache_put(BlockCache *c, void *p, size_t nbytes);
+struct BlockCacheScope {
+    BlockCacheScope();
+    ~BlockCacheScope();
+    BlockCacheScope(const BlockCacheScope &) = delete;
+    BlockCacheScope &operator=(const BlockCacheScope &) = delete;
+    BlockCache *prev;
+    BlockCache *cache;
+};
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -60,7 +78,10 @@ struct DevBuf {
     }
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (BlockCache *c = block_cache()) block_cache_put(c, p, bytes);
+            else cudaFree(p);
+        }
         p = nullptr;
         bytes = 0;
     }
@@ -69,6 +90,14 @@ struct DevBuf {
         if (nbytes <= bytes && p) return EDFMM_OK;
         release();
         size_t want = nbytes ? nbytes : 16;
+        if (BlockCache *c = block_cache()) {
+            size_t got = 0;
+            if (void *q = block_cache_take(c, want, &got)) {
+                p = q;
+                bytes = got;
+                return EDFMM_OK;
+            }
+        }
         cudaError_t e = cudaMalloc(&p, want);
         if (e != cudaSuccess) {
             p = nullptr;

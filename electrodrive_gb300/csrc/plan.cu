@@ -2,6 +2,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "edfmm_internal.cuh"
@@ -122,6 +123,36 @@ int check_plan(const edfmm_plan *p) {
 
 }  // namespace
 
+struct BlockCache {
+    std::multimap<size_t, void *> free_blocks;  // by size
+};
+
+namespace {
+thread_local BlockCache *g_block_cache = nullptr;
+}
+
+BlockCache *block_cache() { return g_block_cache; }
+
+void *block_cache_take(BlockCache *c, size_t nbytes, size_t *got) {
+    // the smallest held block that fits, unless it is more than twice the request
+    auto it = c->free_blocks.lower_bound(nbytes);
+    if (it == c->free_blocks.end() || it->first > 2 * nbytes + 256) return nullptr;
+    void *p = it->second;
+    *got = it->first;
+    c->free_blocks.erase(it);
+    return p;
+}
+
+void block_cache_put(BlockCache *c, void *p, size_t nbytes) { c->free_blocks.emplace(nbytes, p); }
+
+BlockCacheScope::BlockCacheScope() : prev(g_block_cache), cache(new BlockCache()) { g_block_cache = cache; }
+
+BlockCacheScope::~BlockCacheScope() {
+    g_block_cache = prev;
+    for (auto &kv : cache->free_blocks) cudaFree(kv.second);  // cudaFree waits for the device
+    delete cache;
+}
+
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int code, const std::string &msg) {
     g_last_error = msg;
@@ -161,6 +192,7 @@ int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_siz
     p->leaf_size = leaf_size;
     p->max_depth = max_depth;
     cudaStream_t s = S(stream);
+    BlockCacheScope cache_scope;  // the build runs on `s` alone
     rc = tree_build(points_dev, n, dtype, leaf_size, max_depth, p->tree, s);
     if (!rc) rc = lists_build(p->tree, mac_theta, p->lists, s);
     if (!rc) {
@@ -204,6 +236,8 @@ int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int 
     if (rc) return rc;
     cudaStream_t s = S(stream);
     const size_t esz_pt = (dtype == EDFMM_F64 ? 8 : 4) * 3;
+    // every build below runs on `s`: temporaries are recycled in stream order
+    BlockCacheScope cache_scope;
     std::vector<DevTree> trees(n_instances);
     std::vector<DevLists> lists(n_instances);
     for (int i = 0; i < n_instances; ++i) {
