@@ -87,6 +87,31 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_scan(const int32_t *in, i
     }
 }
 
+// n <= one tile: the whole scan and its total in a single launch (most scans
+// of the per-level tree and list builds are this small)
+__global__ void __launch_bounds__(kScanThreads) k_scan_one_tile(const int32_t *in, int32_t *out, int64_t n,
+                                                                int64_t *total) {
+    __shared__ int64_t sw[32];
+    const int64_t base = (int64_t)threadIdx.x * kScanItems;
+    int64_t v[kScanItems];
+    int64_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        acc += v[k];
+    }
+    int64_t tot;
+    int64_t ex = block_exclusive_scan(acc, sw, &tot);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k;
+        if (i < n) out[i] = (int32_t)ex;
+        ex += v[k];
+    }
+    if (threadIdx.x == 0 && total) *total = tot;
+}
+
 }  // namespace
 
 size_t scan_tmp_bytes(int64_t n) {
@@ -100,6 +125,11 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, int64_t *total_de
         return EDFMM_OK;
     }
     int64_t nt = (n + kScanTile - 1) / kScanTile;
+    if (nt == 1) {
+        k_scan_one_tile<<<1, kScanThreads, 0, s>>>(in, out, n, total_dev);
+        EDFMM_LAUNCH_CHECK("k_scan_one_tile");
+        return EDFMM_OK;
+    }
     int64_t *sums = static_cast<int64_t *>(tmp);
     k_tile_sums<<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums);
     EDFMM_LAUNCH_CHECK("k_tile_sums");
