@@ -104,11 +104,19 @@ class BatchSystem:
         A = np.concatenate([m.areas for m, _ in self.cases])
         self.normals = torch.as_tensor(np.concatenate([m.normals for m, _ in self.cases]), dtype=torch.float64,
                                        device=dev)
-        PV = np.concatenate([m.vertices[m.triangles] for m, _ in self.cases])
+        # panel vertex triples gathered on the device from the (smaller)
+        # vertex and triangle arrays
+        vbase = np.concatenate([[0], np.cumsum([m.vertices.shape[0] for m, _ in self.cases])])
+        V = torch.as_tensor(np.concatenate([m.vertices for m, _ in self.cases]), dtype=torch.float64, device=dev)
+        tri = torch.as_tensor(np.concatenate([np.asarray(m.triangles, dtype=np.int64) + vbase[k]
+                                              for k, (m, _) in enumerate(self.cases)]), device=dev)
+        PV = V[tri]
+        # host -> device bytes of the set-up (centroids, areas, normals, vertices, triangles)
+        self.h2d_bytes = int(8 * (3 + 1 + 3) * self.n + V.numel() * 8 + tri.numel() * 8)
         self.C64 = torch.as_tensor(C, dtype=torch.float64, device=dev)
         self.areas = torch.as_tensor(A, dtype=torch.float64, device=dev)
         mark("host_concat_and_copy")
-        I_self = self_integrals(PV, C, order=2, depth=3, device=dev)
+        I_self = self_integrals(PV, self.C64, order=2, depth=3, device=dev)
         self.self_corr = I_self / self.areas.clamp_min(torch.finfo(torch.float64).tiny)
         self.diag = I_self.clamp_min(1e-18)
         mark("self_integrals")
