@@ -261,34 +261,52 @@ __global__ void k_near_scan(const double *cent, const double *radii, int64_t n, 
 
 __global__ void k_set_last32(int32_t *off, int64_t rows, const int64_t *total) { off[rows] = (int32_t)*total; }
 
+// K_E w / max(|t - y|, 1e-12) at y = a + u (b - a) + v (c - a)
+__device__ __forceinline__ double grid_term(V3 a, V3 e1, V3 e2, double u, double v, V3 t) {
+    const double dx = t.x - fma(v, e2.x, fma(u, e1.x, a.x));
+    const double dy = t.y - fma(v, e2.y, fma(u, e1.y, a.y));
+    const double dz = t.z - fma(v, e2.z, fma(u, e1.z, a.z));
+    return rsqrt(fmax(fma(dz, dz, fma(dy, dy, dx * dx)), 1e-24));
+}
+
+// The base rule on the 4^depth triangles of uniform midpoint refinement of
+// (a, b, c) (the reference refines recursively by edge midpoints).  The
+// leaves are the cells of the barycentric grid of step h = 2^-depth: the
+// upright cell (i, j) has corners (i, j), (i+1, j), (i, j+1) and the inverted
+// one (i+1, j), (i, j+1), (i+1, j+1), in units of h along b - a and c - a;
+// every leaf has area(a, b, c) / 4^depth.  Each point costs one FP64 rsqrt
+// instead of a square root and a division, and no leaf geometry is rebuilt.
 __device__ double uniform_sum(V3 a, V3 b, V3 c, V3 t, int order, int depth, double ke) {
-    // iterative uniform refinement: enumerate the 4^depth leaves by their
-    // base-4 digit string (child order v0-corner, v1-corner, v2-corner, middle)
-    const int leaves = 1 << (2 * depth);
+    const double area = tri_area(a, b, c);
+    if (!(area > 0.0)) return 0.0;
+    const int m = 1 << depth;
+    const double h = 1.0 / (double)m;
+    const V3 e1{b.x - a.x, b.y - a.y, b.z - a.z}, e2{c.x - a.x, c.y - a.y, c.z - a.z};
     double s = 0.0;
-    for (int leaf = 0; leaf < leaves; ++leaf) {
-        V3 p = a, q = b, r = c;
-        for (int d = depth - 1; d >= 0; --d) {
-            const int digit = (leaf >> (2 * d)) & 3;
-            const V3 m01 = mid(p, q), m12 = mid(q, r), m20 = mid(r, p);
-            if (digit == 0) {
-                q = m01;
-                r = m20;
-            } else if (digit == 1) {
-                p = m01;
-                r = m12;
-            } else if (digit == 2) {
-                p = m20;
-                q = m12;
-            } else {
-                p = m01;
-                q = m12;
-                r = m20;
+    if (order <= 1) {
+        // leaf centroids: upright (i + 1/3, j + 1/3), inverted (i + 2/3, j + 2/3)
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; i + j < m; ++j) {
+                s += grid_term(a, e1, e2, (i + 1.0 / 3.0) * h, (j + 1.0 / 3.0) * h, t);
+                if (i + j < m - 1) s += grid_term(a, e1, e2, (i + 2.0 / 3.0) * h, (j + 2.0 / 3.0) * h, t);
+            }
+        return ke * (area * h * h) * s;
+    }
+    // points 2/3 at one corner, 1/6 at the others: upright cell offsets
+    // (2/3, 1/6)... in (i, j) units, inverted cell the mirrored ones
+    const double p = 2.0 / 3.0, q = 1.0 / 6.0;
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; i + j < m; ++j) {
+            s += grid_term(a, e1, e2, (i + q) * h, (j + q) * h, t);
+            s += grid_term(a, e1, e2, (i + p) * h, (j + q) * h, t);
+            s += grid_term(a, e1, e2, (i + q) * h, (j + p) * h, t);
+            if (i + j < m - 1) {
+                s += grid_term(a, e1, e2, (i + 1.0 - q) * h, (j + 1.0 - q) * h, t);
+                s += grid_term(a, e1, e2, (i + 1.0 - p) * h, (j + 1.0 - q) * h, t);
+                s += grid_term(a, e1, e2, (i + 1.0 - q) * h, (j + 1.0 - p) * h, t);
             }
         }
-        s += rule_sum(p, q, r, t, order, ke);
-    }
-    return s;
+    return ke * (area * h * h / 3.0) * s;
 }
 
 __global__ void k_near_weights_rows(const double *__restrict__ cent, const double *__restrict__ areas,
