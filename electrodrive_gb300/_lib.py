@@ -29,6 +29,11 @@ EDFMM_F64 = 1
 EDFMM_REFERENCE_PAIR_ORDER = 1
 EDFMM_NO_FARFIELD = 2
 EDFMM_NO_NEARFIELD = 4
+EDFMM_TARGETS_M2L = 1
+EDFMM_TARGETS_L2L = 2
+EDFMM_TARGETS_L2P = 3
+EDFMM_TARGETS_P2P = 4
+EDFMM_TARGETS_LOCALS = 5
 
 
 class EdfmmError(RuntimeError):
@@ -68,6 +73,7 @@ def _declare(L):
         "edfmm_last_error": (C.c_char_p, []),
         "edfmm_version": (C.c_char_p, []),
         "edfmm_launch_count": (i64, []),
+        "edfmm_block_cache_selfcheck": (i32, [C.POINTER(i64)]),
         "edfmm_plan_create": (i32, [_vp, i64, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_create_batch": (i32, [_vp, C.POINTER(i64), i32, i32, i32, i32, dbl, i32, _vp, C.POINTER(_vp)]),
         "edfmm_plan_convert": (i32, [_vp, i32, i32, _vp, C.POINTER(_vp)]),
@@ -78,6 +84,8 @@ def _declare(L):
         "edfmm_targets_export_lists": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_targets_potential": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
         "edfmm_targets_field": (i32, [_vp, _vp, _vp, dbl, _vp, i32, _vp]),
+        "edfmm_targets_create_from_plan": (i32, [_vp, _vp, dbl, _vp, C.POINTER(_vp)]),
+        "edfmm_targets_stage": (i32, [_vp, i32, _vp, _vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
         "edfmm_plan_set_instance_mask": (i32, [_vp, _vp, i32]),
@@ -441,6 +449,45 @@ class Targets:
         v = [C.c_int64() for _ in range(4)]
         check(L.edfmm_targets_info(h, *[C.byref(x) for x in v]), "edfmm_targets_info")
         self.n_nodes, self.n_p2p_pairs, self.n_m2l_pairs, self.p2p_interactions = (int(x.value) for x in v)
+
+    @classmethod
+    def from_plan(cls, plan: "Plan", target_plan: "Plan", mac_theta: float) -> "Targets":
+        """Two-tree lists between ``plan``'s tree and the tree ``target_plan``
+        already holds (copied), built with ``mac_theta``."""
+        if target_plan.dtype != plan.dtype or target_plan.device != plan.device:
+            raise ValueError("source and target trees must share a device and dtype")
+        self = cls.__new__(cls)
+        self.plan = plan
+        self.device = plan.device
+        self.n = int(target_plan.info.n_points)
+        self.order = int(plan.info.expansion_order)
+        self._lib = plan._lib
+        h = _vp()
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_targets_create_from_plan(plan.handle, target_plan.handle, float(mac_theta),
+                                                           stream_handle(self.device), C.byref(h)),
+                  "edfmm_targets_create_from_plan")
+        self._h = h
+        v = [C.c_int64() for _ in range(4)]
+        check(self._lib.edfmm_targets_info(h, *[C.byref(x) for x in v]), "edfmm_targets_info")
+        self.n_nodes, self.n_p2p_pairs, self.n_m2l_pairs, self.p2p_interactions = (int(x.value) for x in v)
+        return self
+
+    def stage(self, stage: int, out: Optional[torch.Tensor] = None) -> Optional[torch.Tensor]:
+        """One two-tree stage (EDFMM_TARGETS_*) on the source plan's current
+        multipoles / charges; L2P and P2P return tree-order potentials of the
+        target points, LOCALS the target local expansions."""
+        dt = self.plan.dtype
+        if stage in (EDFMM_TARGETS_L2P, EDFMM_TARGETS_P2P) and out is None:
+            out = torch.empty(self.n, dtype=dt, device=self.device)
+        elif stage == EDFMM_TARGETS_LOCALS and out is None:
+            p = int(self.plan.info.expansion_order)
+            cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+            out = torch.empty(self.n_nodes, (p + 1) * (p + 2) // 2, dtype=cdt, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_targets_stage(self._h, int(stage), ptr(out), stream_handle(self.device)),
+                  "edfmm_targets_stage")
+        return out
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

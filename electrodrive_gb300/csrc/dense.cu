@@ -317,7 +317,9 @@ using namespace edfmm;
 // device image: every GPU that loads the library holds it until the process
 // exits.  Host code must not pass the array's name to a kernel (on the host
 // it is only a stand-in symbol); its device address is looked up once per
-// device with cudaGetSymbolAddress, with that device current.
+// device with cudaGetSymbolAddress, with that device current, and kept for
+// the life of the process (a cudaDeviceReset would make it stale, so the
+// entry point is not for use after one).
 // ---------------------------------------------------------------------------
 #define EDFMM_DENSE_NOALLOC_SCRATCH_BYTES (8u << 20)
 #define EDFMM_DENSE_NOALLOC_MAX_N 262144

@@ -47,6 +47,11 @@ struct BlockCache;
 BlockCache *block_cache();  // this thread's active cache or NULL
 void *block_cache_take(BlockCache *c, size_t nbytes, size_t *got);
 void block_cache_put(BlockCache *c, void *p, size_t nbytes);
+// frees every block the cache holds (cudaFree waits for the device)
+void block_cache_trim(BlockCache *c);
+// cudaMalloc that, when it fails inside a cache scope, frees the cached
+// blocks and tries once more (a held block may be what the device lacks)
+cudaError_t malloc_or_trim(void **p, size_t nbytes);
 struct BlockCacheScope {
     BlockCacheScope();
     ~BlockCacheScope();
@@ -58,21 +63,25 @@ struct BlockCacheScope {
 
 struct DevBuf {
     void *p = nullptr;
-    size_t bytes = 0;
+    size_t bytes = 0;  // size of the block held
+    size_t used = 0;   // size last asked for (a cached block may be larger)
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) {
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes), used(o.used) {
         o.p = nullptr;
         o.bytes = 0;
+        o.used = 0;
     }
     DevBuf &operator=(DevBuf &&o) noexcept {
         if (this != &o) {
             release();
             p = o.p;
             bytes = o.bytes;
+            used = o.used;
             o.p = nullptr;
             o.bytes = 0;
+            o.used = 0;
         }
         return *this;
     }
@@ -84,10 +93,14 @@ struct DevBuf {
         }
         p = nullptr;
         bytes = 0;
+        used = 0;
     }
     // grows (never shrinks); contents are not preserved
     int reserve(size_t nbytes) {
-        if (nbytes <= bytes && p) return EDFMM_OK;
+        if (nbytes <= bytes && p) {
+            used = nbytes;
+            return EDFMM_OK;
+        }
         release();
         size_t want = nbytes ? nbytes : 16;
         if (BlockCache *c = block_cache()) {
@@ -95,16 +108,39 @@ struct DevBuf {
             if (void *q = block_cache_take(c, want, &got)) {
                 p = q;
                 bytes = got;
+                used = want;
                 return EDFMM_OK;
             }
         }
-        cudaError_t e = cudaMalloc(&p, want);
+        cudaError_t e = malloc_or_trim(&p, want);
         if (e != cudaSuccess) {
             p = nullptr;
             return fail(EDFMM_ERR_ALLOC, std::string("cudaMalloc of ") + std::to_string(want) +
                                              " bytes failed: " + cudaGetErrorString(e));
         }
         bytes = want;
+        used = want;
+        return EDFMM_OK;
+    }
+    // A buffer that outlives its build (a plan's tree, lists, expansions)
+    // and received a cached block well above its size moves to a block of
+    // its own size (contents copied in stream order), so the plan holds no
+    // slack for its lifetime.
+    int shrink_to_fit(cudaStream_t s) {
+        if (!p || bytes <= used + used / 8 + 4096) return EDFMM_OK;
+        void *q = nullptr;
+        cudaError_t e = malloc_or_trim(&q, used);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(q, p, used, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) {
+            if (q) cudaFree(q);
+            return fail(EDFMM_ERR_ALLOC, std::string("exact-size copy of a plan buffer failed: ") +
+                                             cudaGetErrorString(e));
+        }
+        const size_t keep = used;
+        release();  // the cache frees it only after the device is done with it
+        p = q;
+        bytes = keep;
+        used = keep;
         return EDFMM_OK;
     }
     template <class U> U *as() const { return static_cast<U *>(p); }

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include "edfmm_internal.cuh"
 
@@ -448,13 +449,14 @@ EDFMM_API int edfmm_near_create(const void *centroids_dev, const void *areas_dev
     if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "bad dtype");
     if (n > 0 && (!centroids_dev || !areas_dev || !panel_vertices_dev)) return fail(EDFMM_ERR_ARG, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    edfmm_near *h = new edfmm_near();
+    // owned until success: an early return (EDFMM_CUDA_TRY included) frees it
+    std::unique_ptr<edfmm_near> owned(new edfmm_near());
+    edfmm_near *h = owned.get();
     h->n = n;
     h->dtype = dtype;
     int rc = EDFMM_OK;
     auto done = [&](int r) {
-        if (r) delete h;
-        else *out = h;
+        if (!r) *out = owned.release();
         return r;
     };
     if ((rc = h->row_off.reserve(sizeof(int32_t) * (n + 1)))) return done(rc);
@@ -570,15 +572,16 @@ EDFMM_API int edfmm_near_convert(const edfmm_near *src, int dtype, void *stream,
     if (!src) return fail(EDFMM_ERR_ARG, "near handle is NULL");
     if (dtype != EDFMM_F32 && dtype != EDFMM_F64) return fail(EDFMM_ERR_ARG, "bad dtype");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    edfmm_near *h = new edfmm_near();
+    // owned until success: an early return (EDFMM_CUDA_TRY included) frees it
+    std::unique_ptr<edfmm_near> owned(new edfmm_near());
+    edfmm_near *h = owned.get();
     h->n = src->n;
     h->n_pairs = src->n_pairs;
     h->max_row = src->max_row;
     h->dtype = dtype;
     int rc = EDFMM_OK;
     auto done = [&](int r) {
-        if (r) delete h;
-        else *out = h;
+        if (!r) *out = owned.release();
         return r;
     };
     const int64_t np = src->n_pairs;

@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 
 #include "edfmm_internal.cuh"
@@ -116,6 +117,18 @@ int alloc_expansions(edfmm_plan *p, int dtype, int expansion_order, cudaStream_t
     return rc;
 }
 
+// Plan buffers built inside a BlockCacheScope may sit in cached blocks larger
+// than they need; move those to exact-size blocks before the plan is handed out.
+int shrink_tree_lists(DevTree &t, DevLists &l, cudaStream_t s) {
+    DevBuf *bufs[] = {&t.pts,      &t.index_map,     &t.center,      &t.half,    &t.range,
+                      &t.parent,   &t.children,      &t.level,       &t.is_leaf, &t.leaves,
+                      &t.level_nodes, &t.inst_node_off, &l.p2p_off,  &l.p2p_src, &l.m2l_off,
+                      &l.m2l_src,  &l.m2l_swapped_off, &l.m2l_swapped_src};
+    for (DevBuf *b : bufs)
+        if (int rc = b->shrink_to_fit(s)) return rc;
+    return EDFMM_OK;
+}
+
 int check_plan(const edfmm_plan *p) {
     if (!p) return fail(EDFMM_ERR_ARG, "plan is NULL");
     return EDFMM_OK;
@@ -144,6 +157,22 @@ void *block_cache_take(BlockCache *c, size_t nbytes, size_t *got) {
 }
 
 void block_cache_put(BlockCache *c, void *p, size_t nbytes) { c->free_blocks.emplace(nbytes, p); }
+
+void block_cache_trim(BlockCache *c) {
+    for (auto &kv : c->free_blocks) cudaFree(kv.second);
+    c->free_blocks.clear();
+}
+
+cudaError_t malloc_or_trim(void **p, size_t nbytes) {
+    cudaError_t e = cudaMalloc(p, nbytes);
+    BlockCache *c = block_cache();
+    if (e == cudaErrorMemoryAllocation && c && !c->free_blocks.empty()) {
+        (void)cudaGetLastError();  // clear the failed allocation's error state
+        block_cache_trim(c);
+        e = cudaMalloc(p, nbytes);
+    }
+    return e;
+}
 
 BlockCacheScope::BlockCacheScope() : prev(g_block_cache), cache(new BlockCache()) { g_block_cache = cache; }
 
@@ -195,6 +224,7 @@ int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_siz
     BlockCacheScope cache_scope;  // the build runs on `s` alone
     rc = tree_build(points_dev, n, dtype, leaf_size, max_depth, p->tree, s);
     if (!rc) rc = lists_build(p->tree, mac_theta, p->lists, s);
+    if (!rc) rc = shrink_tree_lists(p->tree, p->lists, s);
     if (!rc) {
         p->fmm.p = expansion_order;
         p->fmm.nc = num_coeffs(expansion_order);
@@ -203,6 +233,9 @@ int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, int leaf_siz
         rc = p->fmm.multipoles.reserve(esz);
         if (!rc) rc = p->fmm.locals.reserve(esz);
         if (!rc) rc = p->fmm.translated.reserve(esz);
+        if (!rc) rc = p->fmm.multipoles.shrink_to_fit(s);
+        if (!rc) rc = p->fmm.locals.shrink_to_fit(s);
+        if (!rc) rc = p->fmm.translated.shrink_to_fit(s);
         if (!rc) {
             cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
             if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
@@ -253,6 +286,7 @@ int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int 
     rc = pack_batch(trees, lists, dtype, p->tree, p->lists, s);
     trees.clear();
     lists.clear();
+    if (!rc) rc = shrink_tree_lists(p->tree, p->lists, s);
     if (!rc) {
         p->fmm.p = expansion_order;
         p->fmm.nc = num_coeffs(expansion_order);
@@ -261,6 +295,9 @@ int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int 
         rc = p->fmm.multipoles.reserve(esz);
         if (!rc) rc = p->fmm.locals.reserve(esz);
         if (!rc) rc = p->fmm.translated.reserve(esz);
+        if (!rc) rc = p->fmm.multipoles.shrink_to_fit(s);
+        if (!rc) rc = p->fmm.locals.shrink_to_fit(s);
+        if (!rc) rc = p->fmm.translated.shrink_to_fit(s);
         if (!rc) {
             cudaError_t e = cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s);
             if (e == cudaSuccess) e = cudaMemsetAsync(p->fmm.locals.p, 0, esz, s);
@@ -324,6 +361,35 @@ int edfmm_plan_convert(const edfmm_plan *src, int dtype, int expansion_order, vo
         return rc;
     }
     *plan_out = p;
+    return EDFMM_OK;
+}
+
+int edfmm_block_cache_selfcheck(int64_t *results_host) {
+    if (!results_host) return fail(EDFMM_ERR_ARG, "results_host is NULL");
+    for (int i = 0; i < 4; ++i) results_host[i] = 0;
+    BlockCacheScope scope;
+    void *small_block = nullptr;
+    {
+        DevBuf a, b;
+        if (int rc = a.reserve(1 << 20)) return rc;
+        if (int rc = b.reserve(3 << 20)) return rc;
+        small_block = a.p;
+    }  // both blocks now held by the cache
+    // larger than anything cached: a fresh allocation
+    DevBuf big;
+    if (int rc = big.reserve(16 << 20)) return rc;
+    results_host[0] = (big.p != nullptr && big.bytes == (16u << 20)) ? 1 : 0;
+    // within 2x of a cached block: the 1 MiB block is reused
+    DevBuf reuse;
+    if (int rc = reuse.reserve(700 << 10)) return rc;
+    results_host[1] = (reuse.p == small_block && reuse.bytes == (1u << 20)) ? 1 : 0;
+    // a persistent buffer that took the 3 MiB block for 2 MiB moves to 2 MiB
+    DevBuf keep;
+    if (int rc = keep.reserve(2 << 20)) return rc;
+    results_host[2] = keep.bytes == (3u << 20) ? 1 : 0;
+    if (int rc = keep.shrink_to_fit(nullptr)) return rc;
+    results_host[3] = (keep.bytes == (2u << 20) && keep.used == (2u << 20)) ? 1 : 0;
+    EDFMM_CUDA_TRY(cudaDeviceSynchronize());
     return EDFMM_OK;
 }
 
@@ -617,6 +683,97 @@ int edfmm_targets_create(edfmm_plan *p, const void *targets_dev, int64_t m, void
     }
     *out = t;
     return EDFMM_OK;
+}
+
+int edfmm_targets_create_from_plan(edfmm_plan *p, const edfmm_plan *tp, double mac_theta, void *stream,
+                                   edfmm_targets **out) {
+    if (!out) return fail(EDFMM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (int rc = check_plan(p)) return rc;
+    if (int rc = check_plan(tp)) return rc;
+    if (tp->tree.dtype != p->tree.dtype) return fail(EDFMM_ERR_ARG, "source and target plans must share a dtype");
+    if (p->tree.n_inst > 0 || tp->tree.n_inst > 0)
+        return fail(EDFMM_ERR_UNSUPPORTED, "batched plans have no two-tree lists");
+    if (!(mac_theta > 0.0 && mac_theta < 1.0)) return fail(EDFMM_ERR_ARG, "mac_theta must be in (0, 1)");
+    cudaStream_t s = S(stream);
+    std::unique_ptr<edfmm_targets> t(new edfmm_targets());
+    t->plan = p;
+    const DevTree &a = tp->tree;
+    DevTree &tt = t->tree;
+    tt.dtype = a.dtype;
+    tt.n_points = a.n_points;
+    tt.n_nodes = a.n_nodes;
+    tt.n_leaves = a.n_leaves;
+    tt.max_level = a.max_level;
+    tt.depth_warnings = a.depth_warnings;
+    tt.level_offsets = a.level_offsets;
+    const DevBuf *from[] = {&a.pts,     &a.index_map, &a.center, &a.half,   &a.range,
+                            &a.parent,  &a.children,  &a.level,  &a.is_leaf, &a.leaves, &a.level_nodes};
+    DevBuf *to[] = {&tt.pts,    &tt.index_map, &tt.center, &tt.half,    &tt.range,
+                    &tt.parent, &tt.children,  &tt.level,  &tt.is_leaf, &tt.leaves, &tt.level_nodes};
+    int rc = EDFMM_OK;
+    for (size_t i = 0; !rc && i < sizeof(from) / sizeof(from[0]); ++i) rc = clone_buf(*from[i], *to[i], s);
+    if (!rc) rc = lists_build_two(p->tree, tt, mac_theta, t->lists, s);
+    if (!rc) {
+        t->buf.p = p->fmm.p;
+        t->buf.nc = p->fmm.nc;
+        t->buf.nc_pad = p->fmm.nc_pad;
+        const size_t esz = (tt.dtype == EDFMM_F64 ? 16 : 8) * (size_t)t->buf.nc_pad *
+                           (size_t)std::max<int64_t>(tt.n_nodes, 1);
+        rc = t->buf.locals.reserve(esz);
+        if (!rc) {
+            cudaError_t e = cudaMemsetAsync(t->buf.locals.p, 0, esz, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = fail(EDFMM_ERR_CUDA, std::string("target set-up: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc) return rc;
+    *out = t.release();
+    return EDFMM_OK;
+}
+
+int edfmm_targets_stage(edfmm_targets *t, int stage, void *out_dev, void *stream) {
+    if (!t) return fail(EDFMM_ERR_ARG, "targets is NULL");
+    edfmm_plan *p = t->plan;
+    if (int rc = check_plan(p)) return rc;
+    if (t->buf.p != p->fmm.p)
+        return fail(EDFMM_ERR_STATE, "the source plan's expansion order changed after the targets were created");
+    cudaStream_t s = S(stream);
+    const int64_t M = t->tree.n_nodes;
+    switch (stage) {
+    case EDFMM_TARGETS_M2L:
+        return run_m2l_two(t->tree, p->tree, t->lists, p->fmm, t->buf, s);
+    case EDFMM_TARGETS_L2L:
+        return run_l2l(t->tree, t->buf, s);
+    case EDFMM_TARGETS_L2P:
+    case EDFMM_TARGETS_P2P: {
+        if (t->tree.n_points == 0) return EDFMM_OK;
+        if (!out_dev) return fail(EDFMM_ERR_ARG, "output is NULL");
+        NearArgs a;
+        a.out = out_dev;
+        a.near = stage == EDFMM_TARGETS_P2P;
+        a.far = stage == EDFMM_TARGETS_L2P;
+        a.src_tree = &p->tree;
+        return run_p2p_l2p(t->tree, t->lists, t->buf, a, s);
+    }
+    case EDFMM_TARGETS_LOCALS: {
+        if (M == 0) return EDFMM_OK;
+        if (!out_dev) return fail(EDFMM_ERR_ARG, "output is NULL");
+        const int nc = t->buf.nc;
+        if (t->tree.dtype == EDFMM_F64)
+            k_export_coeffs<double><<<nblk(M * nc, 256), 256, 0, s>>>(M, nc, t->buf.nc_pad,
+                                                                      dptr<Cplx<double>>(t->buf.locals),
+                                                                      static_cast<Cplx<double> *>(out_dev));
+        else
+            k_export_coeffs<float><<<nblk(M * nc, 256), 256, 0, s>>>(M, nc, t->buf.nc_pad,
+                                                                     dptr<Cplx<float>>(t->buf.locals),
+                                                                     static_cast<Cplx<float> *>(out_dev));
+        EDFMM_LAUNCH_CHECK("k_export_coeffs");
+        return EDFMM_OK;
+    }
+    default:
+        return fail(EDFMM_ERR_ARG, "unknown targets stage");
+    }
 }
 
 int edfmm_targets_destroy(edfmm_targets *t) {

@@ -4,12 +4,14 @@
 The pair sets and their (tgt, src) order are bit-identical to the
 reference's.  Pairs are kept as (K, 2) int64 tensors on the GPU; the
 reference's Python list views (``p2p_pairs``, ``u_list`` ...) are materialised
-on first access only.
+on first access only.  Lists between a source tree and a distinct target
+tree hold a handle of libedfmm's two-tree evaluation object, through which
+the tree-level P2P, M2L, L2L and L2P run between the two trees.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional, Tuple
+from typing import Any, Dict, List, Optional, Tuple
 
 import torch
 from torch import Tensor
@@ -44,6 +46,11 @@ class InteractionLists:
     truncated: bool = False
     stats: Optional[InteractionStats] = field(default=None, repr=False)
     _cache: dict = field(default_factory=dict, repr=False)
+    # two-tree lists: libedfmm's evaluation object (source plan + copy of the
+    # target tree + these lists + the target locals)
+    targets: Optional[Any] = field(default=None, repr=False)
+    source_tree: Optional[FmmTree] = field(default=None, repr=False)
+    target_tree: Optional[FmmTree] = field(default=None, repr=False)
 
     @property
     def num_p2p_pairs(self) -> int:
@@ -111,8 +118,10 @@ def build_interaction_lists(source_tree: FmmTree, target_tree: Optional[FmmTree]
                             max_pairs: Optional[int] = None, sort_pairs: bool = True) -> InteractionLists:
     """Classify node pairs into P2P (near) and M2L (far) lists with the reference MAC.
 
-    Only the same-tree case (sources == targets, the BEM operator) is
-    supported on the GPU; ``sort_pairs`` is accepted for signature
+    With ``target_tree`` None or the source tree itself, the same-tree lists
+    of the operator; with a distinct target tree, the two-tree lists
+    (sources = source-tree nodes, targets = target-tree nodes) of
+    interaction_lists.py:531-577.  ``sort_pairs`` is accepted for signature
     compatibility (the output is always sorted by (tgt, src)).
     """
     if target_tree is None:
@@ -122,7 +131,7 @@ def build_interaction_lists(source_tree: FmmTree, target_tree: Optional[FmmTree]
     if mac_theta >= 1.0:
         raise ValueError("mac_theta should be < 1.0 for a meaningful MAC")
     if target_tree is not source_tree:
-        raise NotImplementedError("distinct source and target trees are not supported by electrodrive_gb300")
+        return _build_two_tree_lists(source_tree, target_tree, float(mac_theta), max_pairs)
     plan = source_tree.plan
     plan.rebuild_lists(float(mac_theta))
     p2p, m2l = plan.export_lists()
@@ -134,15 +143,50 @@ def build_interaction_lists(source_tree: FmmTree, target_tree: Optional[FmmTree]
                             same_tree=True, stats=stats)
 
 
+def _build_two_tree_lists(source_tree: FmmTree, target_tree: FmmTree, mac_theta: float,
+                          max_pairs: Optional[int]) -> InteractionLists:
+    from .. import _lib
+
+    if source_tree.device != target_tree.device:
+        raise ValueError("source and target trees must be on the same device")
+    if source_tree.dtype != target_tree.dtype:
+        raise ValueError(f"source and target trees must share a dtype ({source_tree.dtype} vs {target_tree.dtype})")
+    handle = _lib.Targets.from_plan(source_tree.plan, target_tree.plan, mac_theta)
+    p2p, m2l = handle.export_lists()
+    if max_pairs is not None and p2p.shape[0] + m2l.shape[0] > max_pairs:
+        raise RuntimeError("Interaction list truncated-MAC is likely misconfigured or pair count exploded.")
+    stats = InteractionStats(num_p2p_pairs=int(p2p.shape[0]), num_m2l_pairs=int(m2l.shape[0]))
+    return InteractionLists(p2p=p2p, m2l=m2l, mac_theta=mac_theta, n_nodes=target_tree.n_nodes, same_tree=False,
+                            stats=stats, targets=handle, source_tree=source_tree, target_tree=target_tree)
+
+
+def two_tree_handle(source_tree: FmmTree, target_tree: FmmTree, lists: Optional[InteractionLists],
+                    mac_theta: float) -> Any:
+    """The two-tree evaluation object for (source_tree, target_tree): the one
+    ``lists`` carries when it was built for these trees at the source plan's
+    current expansion order, else a fresh one."""
+    if (lists is not None and lists.targets is not None and lists.source_tree is source_tree
+            and lists.target_tree is target_tree
+            and lists.targets.order == int(source_tree.plan.info.expansion_order)):
+        return lists.targets
+    theta = lists.mac_theta if lists is not None else mac_theta
+    fresh = _build_two_tree_lists(source_tree, target_tree, float(theta), None)
+    if lists is not None and lists.targets is not None:
+        lists.targets = fresh.targets
+    return fresh.targets
+
+
 def verify_interaction_lists(source_tree: FmmTree, target_tree: FmmTree, lists: InteractionLists) -> None:
     """Structural checks of interaction_lists.py:580-622 on the tensors."""
-    n = source_tree.n_nodes
+    ns, nt = source_tree.n_nodes, target_tree.n_nodes
     for t in (lists.p2p, lists.m2l):
         if t.numel():
-            assert int(t.min()) >= 0 and int(t.max()) < n, "pair index out of range"
-    leaf = source_tree.node_is_leaf
+            assert int(t[:, 0].min()) >= 0 and int(t[:, 0].max()) < ns, "source index out of range"
+            assert int(t[:, 1].min()) >= 0 and int(t[:, 1].max()) < nt, "target index out of range"
     if lists.p2p.numel():
-        assert bool(leaf[lists.p2p[:, 0]].all() and leaf[lists.p2p[:, 1]].all()), "p2p pair with a non-leaf node"
+        assert bool(source_tree.node_is_leaf[lists.p2p[:, 0]].all()
+                    and target_tree.node_is_leaf[lists.p2p[:, 1]].all()), "p2p pair with a non-leaf node"
 
 
-__all__ = ["InteractionStats", "InteractionLists", "build_interaction_lists", "verify_interaction_lists"]
+__all__ = ["InteractionStats", "InteractionLists", "build_interaction_lists", "two_tree_handle",
+           "verify_interaction_lists"]

@@ -5,11 +5,14 @@ operate on the expansion buffers of the tree's device plan.  The expansions
 are analytic complex solid harmonics (Condon-Shortley phase) scaled per node
 by its radius, not the reference's least-squares proxy fits; they agree with
 the reference in the potential they produce, not coefficient by coefficient.
+With distinct source and target trees, ``m2l`` fills the target tree's locals
+(held by the two-tree evaluation object of the interaction lists) and
+``l2l`` / ``l2p`` on those locals run in the target tree.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass
-from typing import Optional
+from typing import Any, Optional
 
 import torch
 from torch import Tensor
@@ -35,9 +38,13 @@ class MultipoleCoefficients:
 @dataclass
 class LocalCoefficients:
     tree: FmmTree
+    # two-tree evaluation object when the locals belong to a target tree
+    targets: Optional[Any] = None
 
     @property
     def data(self) -> Tensor:
+        if self.targets is not None:
+            return self.targets.stage(_lib.EDFMM_TARGETS_LOCALS)
         return self.tree.plan.expansions()[1]
 
 
@@ -82,7 +89,20 @@ def m2l(source_tree: FmmTree, target_tree: FmmTree, multipoles: MultipoleCoeffic
         stats: Optional[MultipoleOpStats] = None, lists: Optional[InteractionLists] = None,
         reference_pair_order: bool = False):
     if target_tree is not source_tree:
-        raise NotImplementedError("distinct source and target trees are not supported by electrodrive_gb300")
+        # source -> target translation over the two-tree M2L list (the pairs
+        # are applied as listed, (src, tgt); the reference's swapped unpacking,
+        # multipole_operators.py:1671, has no meaning between two trees)
+        from .interaction_lists import two_tree_handle
+
+        if lists is not None and lists.truncated:
+            raise RuntimeError("FMM M2L interaction lists were truncated. Increase max_pairs or relax mac_theta so "
+                               "that all far-field pairs are represented.")
+        _prepare(source_tree, cfg)
+        handle = two_tree_handle(source_tree, target_tree, lists, float(cfg.mac_theta))
+        handle.stage(_lib.EDFMM_TARGETS_M2L)
+        if stats is not None:
+            stats.m2l_calls += int(handle.n_m2l_pairs)
+        return LocalCoefficients(tree=target_tree, targets=handle)
     plan = _prepare(source_tree, cfg)
     if lists is not None and plan.info.mac_theta != lists.mac_theta:
         plan.rebuild_lists(lists.mac_theta)
@@ -94,6 +114,13 @@ def m2l(source_tree: FmmTree, target_tree: FmmTree, multipoles: MultipoleCoeffic
 
 
 def l2l(tree: FmmTree, locals_: LocalCoefficients, cfg: FmmConfig, stats: Optional[MultipoleOpStats] = None):
+    if locals_.targets is not None:
+        if locals_.tree is not tree:
+            raise ValueError("l2l: locals_ belong to another tree")
+        locals_.targets.stage(_lib.EDFMM_TARGETS_L2L)
+        if stats is not None:
+            stats.l2l_calls += max(tree.n_nodes - 1, 0)
+        return locals_
     _prepare(tree, cfg).stage("l2l")
     if stats is not None:
         stats.l2l_calls += max(tree.n_nodes - 1, 0)
@@ -102,6 +129,13 @@ def l2l(tree: FmmTree, locals_: LocalCoefficients, cfg: FmmConfig, stats: Option
 
 def l2p(tree: FmmTree, locals_: LocalCoefficients, cfg: FmmConfig, stats: Optional[MultipoleOpStats] = None) -> Tensor:
     """Far-field potential at the tree points, TREE order, pure 1/r kernel."""
+    if locals_.targets is not None:
+        if locals_.tree is not tree:
+            raise ValueError("l2p: locals_ belong to another tree")
+        out = locals_.targets.stage(_lib.EDFMM_TARGETS_L2P)
+        if stats is not None:
+            stats.l2p_calls += int(tree.node_is_leaf.sum())
+        return out
     out = _prepare(tree, cfg).l2p()
     if stats is not None:
         stats.l2p_calls += int(tree.node_is_leaf.sum())

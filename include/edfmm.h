@@ -67,6 +67,16 @@ typedef struct {
     double mac_theta;
 } edfmm_plan_info;
 
+/*
+ * Self-check of the library's build-time block cache (no counterpart in the
+ * reference): inside one cache scope it reserves and releases two blocks,
+ * reserves a block larger than any cached one, a block that reuses a cached
+ * one, and shrinks a buffer that received an oversized cached block to its
+ * exact size.  results_host[0..3] are set to 1 for each step that behaved.
+ * Allocates about 22 MiB of device memory for the duration of the call.
+ */
+EDFMM_API int edfmm_block_cache_selfcheck(int64_t *results_host);
+
 /* Thread-local description of the most recent failure. */
 EDFMM_API const char *edfmm_last_error(void);
 
@@ -212,6 +222,9 @@ EDFMM_API int edfmm_dense_matvec(const void *centroids_dev, const void *sigma_de
  * (use edfmm_dense_matvec).  The caller still provides all inputs and `out`.
  * The first call on each device looks up the array's device address with
  * cudaGetSymbolAddress; make that first call before any stream capture.
+ * The address is kept for the life of the process, so do not call this
+ * entry point after cudaDeviceReset (or anything else that recreates the
+ * device's primary context) in the same process.
  * All calls share the array, so calls whose work overlaps on the GPU (on
  * different streams, or on different host threads without ordering) race;
  * order them on one stream.  Each call rewrites every scratch slot it reads,
@@ -415,6 +428,38 @@ EDFMM_API int edfmm_targets_potential(edfmm_targets *targets, const void *sigma_
                                       void *out_dev, int flags, void *stream);
 EDFMM_API int edfmm_targets_field(edfmm_targets *targets, const void *sigma_dev, const void *areas_dev, double k_e,
                                   void *out_dev, int flags, void *stream);
+
+/*
+ * Two-tree lists over a target tree the caller already built as a plan of its
+ * own (build_interaction_lists(source_tree, target_tree, mac_theta),
+ * electrodrive/fmm3d/interaction_lists.py:531-577): the target plan's tree is
+ * copied (so the target plan may be destroyed afterwards), the lists between
+ * the source plan's tree and it are built with `mac_theta`, and the target
+ * locals are allocated at the source plan's expansion order.  Both plans must
+ * share a dtype and be unbatched.
+ */
+EDFMM_API int edfmm_targets_create_from_plan(edfmm_plan *source_plan, const edfmm_plan *target_plan, double mac_theta,
+                                             void *stream, edfmm_targets **targets_out);
+/*
+ * The reference's tree-level stages between a source tree and a target tree
+ * (electrodrive/fmm3d/multipole_operators.py:1630-1765 and
+ * electrodrive/fmm3d/kernels_gpu.py:242-274 with distinct trees), on the
+ * source plan's current multipoles and charges:
+ *   EDFMM_TARGETS_M2L     target locals = M2L over the two-tree M2L list
+ *   EDFMM_TARGETS_L2L     parent-to-child local translation in the target tree
+ *   EDFMM_TARGETS_L2P     out[i] = far potential at target point i (tree order, 1/r)
+ *   EDFMM_TARGETS_P2P     out[i] = sum over the two-tree P2P list of q_j / max(r, eps)
+ *                         (tree order; no self exclusion between distinct trees)
+ *   EDFMM_TARGETS_LOCALS  out = the target locals, (n_target_nodes, (p+1)(p+2)/2) complex
+ * Returns EDFMM_ERR_STATE when the source plan's expansion order changed since
+ * the targets were created.
+ */
+#define EDFMM_TARGETS_M2L 1
+#define EDFMM_TARGETS_L2L 2
+#define EDFMM_TARGETS_L2P 3
+#define EDFMM_TARGETS_P2P 4
+#define EDFMM_TARGETS_LOCALS 5
+EDFMM_API int edfmm_targets_stage(edfmm_targets *targets, int stage, void *out_dev, void *stream);
 
 /*
  * Point-cloud warm-start network (no counterpart in the reference: it maps

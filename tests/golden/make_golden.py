@@ -1,8 +1,8 @@
 """Write the golden fixtures in this folder by running the reference itself.
 
-Run in a checkout where the reference project is importable, e.g.::
+Run with REFERENCE_ROOT set to a checkout of the reference project::
 
-    REFERENCE_ROOT=/root/reference python tests/golden/make_golden.py
+    REFERENCE_ROOT=<path of the reference checkout> python tests/golden/make_golden.py
 
 Nothing at test time imports the reference; the tests read only the .npz
 files written here.  Each fixture records which reference routine produced
@@ -32,7 +32,9 @@ from types import SimpleNamespace
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("REFERENCE_ROOT")
+if not REF:
+    sys.exit("set REFERENCE_ROOT to the reference checkout (the project that provides the electrodrive package)")
 sys.path.insert(0, REF)
 os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
 sys.dont_write_bytecode = True
@@ -298,20 +300,23 @@ def save_targets_cases():
     """electrodrive/fmm3d/interaction_lists.py:531 build_interaction_lists
     between a source tree and a separate target tree."""
     out = {}
+    # (source kind, n, seed, target kind, n, seed, dtype, source leaf, theta, shift, target leaf)
     cases = {
-        "shifted_f32": ("uniform", 2000, 21, "uniform", 900, 22, torch.float32, 32, 0.5, 0.6),
-        "sphere_in_cube_f64": ("sphere", 1500, 23, "uniform", 700, 24, torch.float64, 24, 0.5, -0.5),
+        "shifted_f32": ("uniform", 2000, 21, "uniform", 900, 22, torch.float32, 32, 0.5, 0.6, 32),
+        "sphere_in_cube_f64": ("sphere", 1500, 23, "uniform", 700, 24, torch.float64, 24, 0.5, -0.5, 24),
+        "leaf32_vs_leaf10_f32": ("clusters", 2500, 25, "uniform", 1200, 26, torch.float32, 32, 0.45, 0.1, 10),
     }
-    for name, (ks, ns, ss, kt, nt, st, dtype, leaf, theta, shift) in cases.items():
+    for name, (ks, ns, ss, kt, nt, st, dtype, leaf, theta, shift, tleaf) in cases.items():
         src = gen_points(ks, ns, ss, dtype)
         tgt = gen_points(kt, nt, st, dtype) * 2.0 + shift
         tgt = tgt.to(dtype)
         stree = build_fmm_tree(src, leaf_size=leaf)
-        ttree = build_fmm_tree(tgt, leaf_size=leaf)
+        ttree = build_fmm_tree(tgt, leaf_size=tleaf)
         lists = build_interaction_lists(stree, ttree, mac_theta=theta)
         out[f"{name}__sources"] = src.numpy()
         out[f"{name}__targets"] = tgt.numpy()
         out[f"{name}__meta"] = np.array([leaf, theta])
+        out[f"{name}__target_leaf"] = np.array([tleaf])
         out[f"{name}__p2p_pairs"] = np.asarray(lists.p2p_pairs, dtype=np.int32).reshape(-1, 2)
         out[f"{name}__m2l_pairs"] = np.asarray(lists.m2l_pairs, dtype=np.int32).reshape(-1, 2)
         out[f"{name}__target_index_map"] = ttree.index_map.numpy().astype(np.int32)

@@ -26,12 +26,15 @@ def _call(lib, fn, c, s, a, si, out, dtype_code):
     return getattr(lib, fn)(vp(c), vp(s), vp(a), vp(si), s.shape[0], dtype_code, K_E, vp(out), stream)
 
 
-@pytest.mark.parametrize("dt,tol", [(torch.float64, 1e-12), (torch.float32, 2e-6)])
-def test_noalloc_matches_allocating_entry_point_twice(cuda_lib, dt, tol):
+@pytest.mark.parametrize("dt,tol,sizes", [(torch.float64, 1e-12, (5120, 40000, 262144)),
+                                           (torch.float32, 2e-6, (5120, 40000))])
+def test_noalloc_matches_allocating_entry_point_twice(cuda_lib, dt, tol, sizes):
+    # 262144 is the entry point's limit, where its FP64 partial sums take the
+    # largest share of the fixed array
     from electrodrive_gb300 import _lib
 
     code = _lib.dtype_code(dt)
-    for n, seed in ((5120, 1), (40000, 2)):
+    for n, seed in zip(sizes, (1, 2, 3)):
         g = torch.Generator().manual_seed(seed)
         c = torch.rand(n, 3, generator=g, dtype=torch.float64).to("cuda", dt)
         a = (0.5 + torch.rand(n, generator=g, dtype=torch.float64)).to("cuda", dt) / n
