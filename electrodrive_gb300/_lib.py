@@ -29,6 +29,8 @@ EDFMM_F64 = 1
 EDFMM_REFERENCE_PAIR_ORDER = 1
 EDFMM_NO_FARFIELD = 2
 EDFMM_NO_NEARFIELD = 4
+EDFMM_ARITH_NATIVE = 0
+EDFMM_ARITH_TWO_FLOAT = 1
 EDFMM_TARGETS_M2L = 1
 EDFMM_TARGETS_L2L = 2
 EDFMM_TARGETS_L2P = 3
@@ -88,6 +90,7 @@ def _declare(L):
         "edfmm_targets_stage": (i32, [_vp, i32, _vp, _vp]),
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
+        "edfmm_plan_set_arithmetic": (i32, [_vp, i32, _vp]),
         "edfmm_plan_set_instance_mask": (i32, [_vp, _vp, i32]),
         "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
         "edfmm_plan_export_tree": (i32, [_vp] * 11),
@@ -321,6 +324,18 @@ class Plan:
             check(self._lib.edfmm_plan_rebuild_lists(self._h, float(mac_theta), stream_handle(self.device)),
                   "edfmm_plan_rebuild_lists")
         self._refresh_info()
+
+    def set_arithmetic(self, mode: str):
+        """FP64 plans: "two_float" runs M2L and the near field in two-float
+        arithmetic on the FP32 pipe (about 48 significant bits); "native"
+        restores IEEE FP64."""
+        code = {"native": EDFMM_ARITH_NATIVE, "two_float": EDFMM_ARITH_TWO_FLOAT}.get(mode)
+        if code is None:
+            raise ValueError(f"arithmetic must be 'native' or 'two_float', got {mode!r}")
+        with torch.cuda.device(self.device):
+            check(self._lib.edfmm_plan_set_arithmetic(self._h, code, stream_handle(self.device)),
+                  "edfmm_plan_set_arithmetic")
+        self.arithmetic = mode
 
     def set_order(self, p: int):
         with torch.cuda.device(self.device):

@@ -1,14 +1,14 @@
-"""BEM solve on the GPU (electrodrive/core/bem.py:1550-2695, one pass).
+"""BEM solve on the GPU (electrodrive/core/bem.py:1550-2695).
 
-``bem_solve(spec, cfg)`` runs the reference's solve section for a single
-mesh resolution (``cfg.initial_h``): mesh -> self integrals (adaptive
-near-singular quadrature, depth 3 for spheres / two planes, else 4) ->
-optional near-pair corrections (``cfg.use_near_quadrature_matvec``) ->
-single-layer operator (dense below ``fmm_threshold`` panels, FMM above) ->
-``b = bc - V_free``, ``x0 = b / I_self`` -> Jacobi-preconditioned restarted
-GMRES -> surface charge density.  The reference's h-refinement loop, energy
-bookkeeping, control-file polling and damped-Jacobi fallback are not part of
-this operator path.
+``bem_solve(spec, cfg)`` runs the reference's h-refinement loop; each pass:
+mesh -> self integrals (adaptive near-singular quadrature, depth 3 for
+spheres / two planes, else 4) -> optional near-pair corrections
+(``cfg.use_near_quadrature_matvec``) -> single-layer operator (dense below
+``fmm_threshold`` panels, FMM above) -> ``b = bc - V_free``,
+``x0 = b / I_self`` -> Jacobi-preconditioned restarted GMRES (retried without
+the preconditioner, then damped Jacobi, when it fails) -> surface charge
+density, boundary residual and capacitive energy.  Control-file polling,
+telemetry and run manifests are not part of this operator path.
 
 ``solve_mixed`` is the FP32-inner / FP64-outer iterative refinement solver:
 the FP64 operator computes the true residual, an FP32 GMRES solves the
@@ -87,6 +87,11 @@ class BEMOperator:
             self.near.apply(sigma, v, v)
         return v
 
+    def graph_state(self) -> tuple:
+        """Forwarded to the base operator (captured graphs depend on it)."""
+        fn = getattr(self.base, "graph_state", None)
+        return fn() if fn is not None else ()
+
     def set_active_mask(self, flags: Optional[Tensor], stride: int = 1) -> bool:
         """Forwarded to the FMM base operator (batched plans only)."""
         fn = getattr(self.base, "set_active_mask", None)
@@ -138,6 +143,8 @@ class BEMSolution:
     near_quad_order: int = 2
     near_quad_dist_factor: float = 1.5
     near_quad_max_depth: Optional[int] = None
+    # diagnostics of the pass that produced the solution (energy_A)
+    meta: Dict[str, Any] = field(default_factory=dict)
 
     def eval(self, points: Tensor) -> Tensor:
         """Total potential V_free + V_induced at points (N, 3): the dense induced
@@ -165,28 +172,47 @@ class BEMSolution:
         return v, e
 
 
-def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,
-              *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
-              use_graph: bool = True, self_integral: str = "auto", mixed: bool = False, mixed_rtol: float = 1e-6,
-              inner_restart: int = 40, inner_expansion_order: Optional[int] = None) -> Dict[str, Any]:
-    """One solve pass.  ``self_integral``: "auto" follows the reference
-    (quadrature self terms only when a near-quadrature option is on, else the
-    equal-area disk value 2 pi K_E sqrt(A / pi), bem.py:1747-1816), or force
-    "quadrature" / "disk".  ``mixed=True`` builds the operator (and the near
-    correction) in FP64 and FP32 and solves with :func:`solve_mixed` to an FP64
-    relative true residual of ``mixed_rtol`` (``cfg.fp64`` is then ignored)."""
-    if differentiable:
-        raise NotImplementedError("the differentiable (xitorch) path is not part of electrodrive_gb300")
-    cfg = cfg or BEMConfig()
-    _lib.load_library()
-    dev = torch.device("cuda", torch.cuda.current_device())
-    dtype = torch.float64 if (getattr(cfg, "fp64", False) or mixed) else torch.float32
-    h = float(getattr(cfg, "initial_h", 0.2))
-    t0 = time.perf_counter()
-    mesh = mesh if mesh is not None else generate_mesh(spec, h)
+def jacobi_fallback_solve(A, b: Tensor, diag: Tensor, *, maxiter: int = 1024, tol: float = 1e-6,
+                          omega: float = 0.8) -> Tuple[Tensor, Dict[str, Any]]:
+    """Damped Jacobi iteration x <- x + omega D^-1 (b - A x) from x = 0, the
+    reference's last resort after GMRES fails (bem.py:1156-1251): stops when
+    ||b - A x|| <= tol max(||b||, 1), on a non-finite residual, or after
+    ``maxiter`` sweeps; returns (x, info) with the reference's info keys."""
+    x = torch.zeros_like(b)
+    dinv = 1.0 / diag.to(b.dtype).clamp_min(1e-18)
+    r = b - A(x)
+    r0 = float(torch.linalg.norm(r))
+    if not math.isfinite(r0):
+        return x, {"iters": 0, "resid": r0, "success": False, "solver": "jacobi_fallback"}
+    target = tol * max(r0, 1.0)
+    it, rn = 0, r0
+    for k in range(maxiter):
+        it = k + 1
+        x = x + omega * dinv * r
+        r = b - A(x)
+        rn = float(torch.linalg.norm(r))
+        if not math.isfinite(rn):
+            return x, {"iters": it, "resid": rn, "success": False, "solver": "jacobi_fallback"}
+        if rn <= target:
+            return x, {"iters": it, "resid": rn, "success": True, "solver": "jacobi_fallback"}
+    return x, {"iters": it, "resid": rn, "success": False, "solver": "jacobi_fallback"}
+
+
+def _info_ok(info: Dict[str, Any]) -> Tuple[bool, float, int]:
+    try:
+        resid = float(info.get("resid", float("inf")))
+    except Exception:
+        resid = float("inf")
+    return bool(info.get("success", True)), resid, int(info.get("code", 0) or 0)
+
+
+def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtype, mixed: bool, mixed_rtol: float,
+                inner_restart: int, inner_expansion_order: Optional[int], operator: str, fmm_threshold: int,
+                use_graph: bool, self_integral: str, logger, fp64_arithmetic: str = "native") -> Dict[str, Any]:
+    """One refinement pass of bem.py:1629-2404 on a given mesh: set-up, the
+    linear solve with its retry and fallback chain, and the pass results.
+    Returns {"error": msg} on a failure the reference reports as an error."""
     N = mesh.n_panels
-    if N == 0:
-        return {"error": "empty mesh"}
     C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
     A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
     PV = mesh.vertices[mesh.triangles]
@@ -204,19 +230,17 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     tiny = torch.finfo(dtype).tiny
     self_corr = (I_self / A_dev.clamp_min(tiny)).to(dtype)
     want_near = bool(getattr(cfg, "use_near_quadrature_matvec", False)) and N > 1
-
-    def make_near(dt):
-        if not want_near:
-            return None
-        return NearCorrection(mesh.centroids, mesh.areas, PV,
+    near = None
+    if want_near:
+        near = NearCorrection(mesh.centroids, mesh.areas, PV,
                               distance_factor=float(getattr(cfg, "near_quadrature_distance_factor", 1.5)),
-                              order=order, depth=depth_near, dtype=dt, device=dev)
-
-    near = make_near(dtype)
+                              order=order, depth=depth_near, dtype=dtype, device=dev)
     op = build_operator(C64, A64, self_corr, dtype=dtype, kind=operator, fmm_threshold=fmm_threshold, near=near,
                         device=dev)
     op32 = None
     if mixed:
+        if isinstance(op.base, FmmOperator) and fp64_arithmetic != "native":
+            op.base.plan.set_arithmetic(fp64_arithmetic)
         near32 = None if near is None else near.astype(torch.float32)
         op32 = converted_operator(op, A64, self_corr, dtype=torch.float32, expansion_order=inner_expansion_order or 8,
                                   near=near32)
@@ -228,25 +252,191 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     C_dev = C64.to(dev, dtype)
     V_free = point_charge_potential(C_dev, charges) if charges else torch.zeros(N, dtype=dtype, device=dev)
     bc = torch.as_tensor(bc_vector(spec, mesh), dtype=dtype, device=dev)
+    if not bool(torch.isfinite(bc).all()):
+        return {"error": "BEM BC vector contains NaN/Inf."}
+    if not bool(torch.isfinite(V_free).all()):
+        return {"error": "Free-space potential on centroids contains NaN/Inf."}
     b = bc - V_free
     diag = I_self.to(dtype).clamp_min(1e-18)
     x0 = b / diag
-    t_setup = time.perf_counter() - t0
+    if not bool(torch.isfinite(b).all()):
+        return {"error": "BEM RHS contains NaN/Inf."}
+    if not bool(torch.isfinite(diag).all()):
+        return {"error": "BEM diagonal (self-integrals) contains NaN/Inf."}
+    if not bool(torch.isfinite(x0).all()):
+        x0 = torch.zeros_like(b)
+    use_precond = bool(getattr(cfg, "use_precond", True))
+    restart = int(getattr(cfg, "gmres_restart", 256))
+    tol = float(getattr(cfg, "gmres_tol", 5e-8))
+    maxiter = int(getattr(cfg, "gmres_maxiter", 2000))
+
+    def plain(precond):
+        return gmres_restart(op, b, restart=restart, tol=tol, maxiter=maxiter, precond=precond,
+                             areas=A_dev.to(dtype), A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
+
+    sigma = info = None
     if mixed:
-        sigma, minfo = solve_mixed(op, op32, b, A_diag=diag if getattr(cfg, "use_precond", True) else None, x0=x0,
-                                   rtol=mixed_rtol, inner_restart=inner_restart, use_graph=use_graph)
+        x, minfo = solve_mixed(op, op32, b, A_diag=diag if use_precond else None, x0=x0, rtol=mixed_rtol,
+                               inner_restart=inner_restart, use_graph=use_graph)
         bn = float(torch.linalg.norm(b))
-        info = dict(iters=minfo["inner_iters"], resid=minfo["rel_resid"] * bn, success=minfo["success"],
-                    code=minfo["code"], tol_abs=mixed_rtol * bn, used_preconditioner=bool(getattr(cfg, "use_precond", True)),
-                    outer=minfo["outer"], matvec64=minfo["matvec64"], history=minfo["history"], precision="mixed")
-    else:
-        sigma, info = gmres_restart(op, b, restart=int(getattr(cfg, "gmres_restart", 256)),
-                                    tol=float(getattr(cfg, "gmres_tol", 5e-8)),
-                                    maxiter=int(getattr(cfg, "gmres_maxiter", 2000)),
-                                    precond="jacobi" if getattr(cfg, "use_precond", True) else None,
-                                    areas=A_dev.to(dtype), A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
+        if minfo["success"]:
+            sigma = x.to(dtype)
+            info = dict(iters=minfo["inner_iters"], resid=minfo["rel_resid"] * bn, success=True, code=0,
+                        tol_abs=mixed_rtol * bn, used_preconditioner=use_precond, outer=minfo["outer"],
+                        matvec64=minfo["matvec64"], history=minfo["history"], precision="mixed")
+    if sigma is None:
+        # the reference's chain (bem.py:2172-2302): preconditioned GMRES, a
+        # retry without the preconditioner, then damped Jacobi
+        precond = "jacobi" if use_precond else None
+        sigma, info = plain(precond)
+        ok, resid, code = _info_ok(info)
+        if precond is not None and (not ok or not math.isfinite(resid)):
+            sigma, info = plain(None)
+            ok, resid, code = _info_ok(info)
+        if not ok or not math.isfinite(resid):
+            if not bool(getattr(cfg, "allow_jacobi_fallback", True)):
+                return {"error": f"BEM linear solve failed: GMRES(code={code}, resid={resid})",
+                        "gmres_resid": resid, "gmres_code": code}
+            sj, ij = jacobi_fallback_solve(op, b, diag, maxiter=int(getattr(cfg, "jacobi_maxiter", 256)),
+                                           tol=float(getattr(cfg, "jacobi_tol", 1e-5)),
+                                           omega=float(getattr(cfg, "jacobi_omega", 0.8)))
+            rj = float(ij.get("resid", float("inf")))
+            if not (ij.get("success", False) and math.isfinite(rj)):
+                return {"error": f"BEM linear solve failed: GMRES(code={code}, resid={resid}) and Jacobi(resid={rj})",
+                        "gmres_resid": resid, "gmres_code": code, "jacobi_resid": rj, "jacobi_iters": ij.get("iters")}
+            sigma, info = sj, ij
+    if not bool(torch.isfinite(sigma).all()):
+        return {"error": "BEM sigma contains NaN/Inf after linear solve."}
     V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
     bc_resid = float(torch.max(torch.abs(V_tot - bc)))
+    energy = float(0.5 * torch.sum(V_tot.double() * torch.nan_to_num(sigma).double() * A_dev))
+    Nrm = torch.as_tensor(mesh.normals, dtype=dtype, device=dev)
+    return {"pass_payload": {"h": h, "dof": N, "bc_resid_linf": bc_resid, "energy_A": energy, "gmres_info": dict(info),
+                             "tile_size": int(getattr(cfg, "tile_size", 0) or 0),
+                             "artifacts": (spec, C_dev, A_dev.to(dtype), Nrm, sigma, V_tot, mesh)},
+            "operator": "fmm" if isinstance(op.base, FmmOperator) else "dense",
+            "near_pairs": 0 if near is None else near.n_pairs, "charges": charges, "PV": PV}
+
+
+def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] = None, differentiable: bool = False,
+              *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
+              use_graph: bool = True, self_integral: str = "auto", mixed: bool = False, mixed_rtol: float = 1e-6,
+              inner_restart: int = 40, inner_expansion_order: Optional[int] = None,
+              fp64_arithmetic: str = "two_float") -> Dict[str, Any]:
+    """The reference's bem_solve (bem.py:1550-2695) on the GPU operator.
+
+    h-refinement (bem.py:1667-2495): pass k meshes at h = initial_h *
+    refine_factor^k and solves; the loop stops once the pass's boundary
+    residual max |V_free + A sigma - bc| is at most ``target_bc_inf_norm``
+    (after ``min_refine_passes`` and ``min_panels``), on a plateau when
+    ``plateau_max`` is set, or after ``max_refine_passes``.  The best pass
+    (smallest boundary residual; a finer mesh wins within a band of 1e-3 of
+    the target) is returned.  Each solve is Jacobi-preconditioned restarted
+    GMRES from x0 = b / I_self; if it fails it is retried without the
+    preconditioner and then by damped Jacobi (``allow_jacobi_fallback``,
+    ``jacobi_maxiter``, ``jacobi_tol``, ``jacobi_omega``), as the reference
+    does.  Keys of the result are the reference's (``surface_charge_density``
+    as a host array, ``solution``, ``mesh_stats``, ``gmres_stats``,
+    ``refinement_history``, ``boundary_samples``, ``sample_points``) or
+    {"error": ...}.  Control-file polling, telemetry and manifests are not
+    part of this operator path; ``tile_size`` entries report 0 (no tiling).
+
+    Additions: ``mesh`` solves one pass on a given mesh; ``operator``
+    ("auto": dense below ``fmm_threshold`` panels, FMM above);
+    ``self_integral`` "auto" follows the reference (quadrature self terms only
+    when a near-quadrature option is on, else the equal-area disk value
+    2 pi K_E sqrt(A / pi), bem.py:1747-1816) or forces "quadrature" / "disk";
+    ``mixed=True`` builds the operator in FP64 and FP32 and solves with
+    :func:`solve_mixed` to an FP64 relative true residual of ``mixed_rtol``
+    (``cfg.fp64`` is then ignored; a failed mixed solve falls back to the
+    reference's chain in FP64); ``fp64_arithmetic`` ("two_float", the
+    default, or "native") is the arithmetic of that FP64 FMM operator's M2L
+    and near field (two-float: about 48 significant bits on the FP32 pipe,
+    within about 1e-13 of IEEE FP64).
+    """
+    if differentiable:
+        raise NotImplementedError("the differentiable (xitorch) path is not part of electrodrive_gb300")
+    cfg = cfg or BEMConfig()
+    if float(getattr(cfg, "near_alpha", 0.0) or 0.0) > 0.0:
+        raise NotImplementedError("near_alpha neighbour smoothing of the operator is not part of electrodrive_gb300")
+    _lib.load_library()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dtype = torch.float64 if (getattr(cfg, "fp64", False) or mixed) else torch.float32
+    t0 = time.perf_counter()
+    current_h = float(getattr(cfg, "initial_h", 0.3))
+    refine_factor = float(getattr(cfg, "refine_factor", 0.5))
+    target_bc = float(getattr(cfg, "target_bc_inf_norm", 1e-7))
+    tiny_band = max(target_bc * 1e-3, 1e-12)
+    max_passes = 1 if mesh is not None else int(getattr(cfg, "max_refine_passes", 3))
+    plateau_raw = getattr(cfg, "plateau_max", None)
+    try:
+        max_plateau = None if plateau_raw is None else int(plateau_raw)
+    except Exception:
+        max_plateau = None
+    plateau_rel = float(getattr(cfg, "plateau_rel_improvement", 0.05))
+    history: List[Dict[str, Any]] = []
+    best: Optional[Dict[str, Any]] = None
+    best_extra: Dict[str, Any] = {}
+    extras: List[Dict[str, Any]] = []
+    best_bc = float("inf")
+    plateau = 0
+
+    def error_result(msg: str, **extra: Any) -> Dict[str, Any]:
+        out: Dict[str, Any] = {"error": msg}
+        if history:
+            out["refinement_history"] = history
+        if best is not None:
+            out["best_bc_resid_linf"] = best.get("bc_resid_linf")
+            out["best_dof"] = best.get("dof")
+        out.update(extra)
+        return out
+
+    for rp in range(max_passes):
+        try:
+            m = mesh if mesh is not None else generate_mesh(spec, current_h)
+        except Exception:
+            break
+        if m.n_panels == 0:
+            break
+        res = _solve_pass(spec, cfg, m, current_h, dev=dev, dtype=dtype, mixed=mixed, mixed_rtol=mixed_rtol,
+                          inner_restart=inner_restart, inner_expansion_order=inner_expansion_order, operator=operator,
+                          fmm_threshold=fmm_threshold, use_graph=use_graph, self_integral=self_integral,
+                          logger=logger, fp64_arithmetic=fp64_arithmetic)
+        if "error" in res:
+            msg = res.pop("error")
+            return error_result(msg, **res)
+        payload = dict(res["pass_payload"], **{"pass": rp + 1})
+        history.append(payload)
+        extras.append(res)
+        bc_r, N = payload["bc_resid_linf"], payload["dof"]
+        if bc_r < best_bc:
+            improvement = best_bc - bc_r if math.isfinite(best_bc) else float("inf")
+            best, best_extra, best_bc = payload, res, bc_r
+            plateau = 0 if improvement > max(1e-16, plateau_rel * max(best_bc, 1e-16)) else plateau + 1
+        elif best is not None and abs(bc_r - best_bc) <= tiny_band and N > int(best.get("dof", 0)):
+            best, best_extra, best_bc = payload, res, bc_r
+            plateau = 0
+        else:
+            plateau += 1
+        have_min_panels = N >= int(getattr(cfg, "min_panels", 0))
+        have_min_passes = (rp + 1) >= int(getattr(cfg, "min_refine_passes", 1))
+        if bc_r <= target_bc and have_min_panels and have_min_passes:
+            break
+        if max_plateau is not None and plateau >= max_plateau and have_min_panels and have_min_passes:
+            break
+        current_h *= refine_factor
+    if best is None:
+        if not history:
+            return error_result("BEM solve failed (no passes)")
+        good = [p for p in history if _info_ok(p.get("gmres_info") or {})[0]
+                and math.isfinite(_info_ok(p.get("gmres_info") or {})[1])]
+        if not good:
+            return error_result("BEM solve failed (no successful linear solves)",
+                                gmres_last=history[-1].get("gmres_info", {}))
+        best = min(good, key=lambda p: p.get("bc_resid_linf", float("inf")))
+        best_extra = extras[history.index(best)]
+    spec_b, C_b, A_b, Nrm_b, sigma_b, Vtot_b, mesh_b = best["artifacts"]
+    N_b = int(best["dof"])
     torch.cuda.synchronize(dev)
     t_total = time.perf_counter() - t0
     # evaluation near quadrature as bem.py:2560-2600 configures it
@@ -256,20 +446,28 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
         eval_factor = max(eval_factor, 6.0)
     elif "plane" in ctypes_:
         eval_factor = max(eval_factor, 3.0)
-    use_near_eval = bool(getattr(cfg, "use_near_quadrature", False)) and N > 0
-    sol = BEMSolution(centroids=C_dev, areas=A_dev.to(dtype), sigma=sigma, charges=charges,
-                      panel_vertices=torch.as_tensor(PV, dtype=torch.float64, device=dev) if use_near_eval else None,
+    use_near_eval = bool(getattr(cfg, "use_near_quadrature", False)) and N_b > 0
+    sol = BEMSolution(centroids=C_b, areas=A_b, sigma=sigma_b, charges=best_extra["charges"],
+                      panel_vertices=torch.as_tensor(best_extra["PV"], dtype=torch.float64, device=dev)
+                      if use_near_eval else None,
                       near_quadrature=use_near_eval,
                       near_quad_order=int(getattr(cfg, "near_quadrature_order", 2)),
                       near_quad_dist_factor=eval_factor, near_quad_max_depth=quad_depths(spec)[0])
-    mesh_stats = dict(n_panels=N, total_area=float(mesh.areas.sum()), bc_residual_linf=bc_resid, h_final=h,
-                      operator="fmm" if isinstance(op.base, FmmOperator) else "dense",
-                      near_pairs=0 if near is None else near.n_pairs)
-    info = dict(info)
-    info.update(setup_seconds=t_setup, total_seconds=t_total)
-    return dict(solution=sol, surface_charge_density=sigma, mesh_stats=mesh_stats, gmres_stats=info,
-                refinement_history=[dict(pass_index=0, h=h, n_panels=N, bc_resid_linf=bc_resid,
-                                         gmres_iters=info["iters"])], boundary_samples=None, sample_points=None)
+    n_samples = min(1024, max(1, N_b))
+    step = max(1, N_b // n_samples)
+    idx = torch.arange(0, N_b, step, device=C_b.device)[:n_samples]
+    mesh_stats = dict(n_panels=N_b, total_area=float(A_b.sum()), bc_residual_linf=float(best["bc_resid_linf"]),
+                      h_final=float(best["h"]), tile_size_final=int(best["tile_size"]),
+                      operator=best_extra["operator"], near_pairs=best_extra["near_pairs"])
+    if any(_cget(c, "type") == "plane" for c in (_cget(spec, "conductors", []) or [])) and mesh_stats["total_area"] > 0:
+        mesh_stats["patch_L"] = math.sqrt(mesh_stats["total_area"])
+    gmres_stats = dict(best.get("gmres_info", {}))
+    gmres_stats.update(total_seconds=t_total)
+    sol.meta["energy_A"] = best["energy_A"]
+    return dict(solution=sol, surface_charge_density=sigma_b.detach().cpu().numpy(), mesh_stats=mesh_stats,
+                gmres_stats=gmres_stats, refinement_history=history,
+                boundary_samples=Vtot_b[idx].detach().cpu().numpy().tolist(),
+                sample_points=C_b[idx].detach().cpu().numpy().tolist())
 
 
 def assemble_system(mesh: TriMesh, spec: Any, *, kind: str = "dense", dtypes=(torch.float64,), near: bool = False,
@@ -454,5 +652,5 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
 
 
 __all__ = ["BEMOperator", "BEMSolution", "assemble_system", "autotune_inner_operator", "bem_solve", "build_operator",
-           "bc_vector", "point_charges",
+           "bc_vector", "jacobi_fallback_solve", "point_charges",
            "quad_depths", "segment_norms", "solve_mixed"]

@@ -127,6 +127,11 @@ def _graph_workspace(A: Any, key: tuple, make: Callable[[], Dict[str, Any]]) -> 
         per = _GRAPH_CACHE.setdefault(A, {})
     except TypeError:  # the operator cannot be weakly referenced: no reuse
         return make()
+    # graphs captured while the operator launched other kernels (an FP64
+    # plan switched between IEEE and two-float arithmetic) are not reused
+    state = getattr(A, "graph_state", None)
+    if state is not None:
+        key = key + (state(),)
     ws = per.get(key)
     if ws is None:
         ws = per[key] = make()

@@ -69,6 +69,11 @@ class FmmOperator:
         s = sigma if sigma.is_contiguous() else sigma.contiguous()
         return self.plan.matvec(s, self.a, self.si, k_e=self.k_e, out=o, flags=self.flags)
 
+    def graph_state(self) -> tuple:
+        """What a captured graph of this operator depends on besides its
+        buffers: the plan's arithmetic (two-float mode launches other kernels)."""
+        return (getattr(self.plan, "arithmetic", "native"),)
+
     def set_active_mask(self, flags: Optional[Tensor], stride: int = 1) -> bool:
         """Batched plans: later applications skip the far-field rows and
         near-field leaves of instances with flags[k * stride] == 0 (their

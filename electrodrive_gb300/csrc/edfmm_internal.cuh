@@ -206,6 +206,9 @@ struct DevTree {
     DevBuf leaves;     // int32 ids of leaf nodes (ascending)
     std::vector<int32_t> level_offsets;  // host: level l nodes = level_nodes[off[l], off[l+1])
     DevBuf level_nodes;                  // int32 node ids grouped by level
+    // FP64 trees in two-float mode: per point (x, y, z, charge) split into
+    // FP32 (hi, lo) pairs, 8 floats, refreshed with the charges
+    DevBuf pts_tf;
     // batched plans: instance k owns nodes inst_node_off[k] .. inst_node_off[k+1]-1
     int n_inst = 0;
     DevBuf inst_node_off;  // int32 x (n_inst + 1)
@@ -279,6 +282,9 @@ struct FmmBuffers {
     DevBuf translated;  // complex T, n_nodes x nc_pad: each node's multipole moved to its parent's centre
     ExtremeRows extreme, extreme_swapped;
     InstMask mask;  // set around the steps of a batched solve
+    // FP64 plans: EDFMM_ARITH_TWO_FLOAT runs M2L and the near field in
+    // two-float arithmetic on the FP32 pipe (twofloat.cuh)
+    int arith = EDFMM_ARITH_NATIVE;
 };
 
 int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaStream_t s);
@@ -289,9 +295,16 @@ int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool sw
 int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s);
+// the same in two-float arithmetic for FP64 plans, orders 6..8
+// (EDFMM_ERR_UNSUPPORTED for other orders, launching nothing)
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
+                      const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+                      cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
                 FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
+// the same-tree extreme-pair rows of buf (built once; synchronises s)
+int prepare_extreme_rows(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, cudaStream_t s);
 
 struct NearArgs {
     const void *sigma = nullptr;      // original order (nullable)

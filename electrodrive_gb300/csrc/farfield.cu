@@ -24,6 +24,7 @@
 
 #include "edfmm_internal.cuh"
 #include "harmonics.cuh"
+#include "twofloat.cuh"
 
 namespace edfmm {
 
@@ -50,6 +51,24 @@ __global__ void k_set_charges(typename Vec4<T>::type *pts, const int32_t *__rest
     if (i >= n) return;
     int o = idx[i];
     pts[i].w = b ? a[o] * b[o] : a[o];
+}
+
+// FP64 trees in two-float mode: the charges as above (a == NULL keeps them)
+// and every point split into (hi, lo) FP32 pairs, 8 floats per point
+__global__ void k_set_charges_split(double4 *pts, float4 *pts_tf, const int32_t *__restrict__ idx, int64_t n,
+                                    const double *__restrict__ a, const double *__restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 x = pts[i];
+    if (a) {
+        const int o = idx[i];
+        x.w = b ? a[o] * b[o] : a[o];
+        pts[i].w = x.w;
+    }
+    const tf32x2 sx = tf_from_double(x.x), sy = tf_from_double(x.y), sz = tf_from_double(x.z),
+                 sq = tf_from_double(x.w);
+    pts_tf[2 * i] = make_float4(sx.hi, sx.lo, sy.hi, sy.lo);
+    pts_tf[2 * i + 1] = make_float4(sz.hi, sz.lo, sq.hi, sq.lo);
 }
 
 // ---------------------------------------------------------------------------
@@ -631,26 +650,30 @@ __global__ void __launch_bounds__(128) k_m2l_generic(int64_t n_rows, const int32
 }
 
 // extreme pairs (source radius > 256x target radius) as a CSR by target
-__global__ void k_extreme_flags(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *thalf,
-                                const float4 *half, int32_t *row_cnt) {
+template <typename T4>
+__global__ void k_extreme_flags(int64_t n_nodes, const int32_t *off, const int32_t *src, const T4 *thalf,
+                                const T4 *half, int32_t *row_cnt) {
+    using T = decltype(thalf->w);
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= n_nodes) return;
-    const float iaL = 1.0f / thalf[t].w;
+    const T iaL = (T)1 / thalf[t].w;
     int c = 0;
-    for (int k = off[t] + lane; k < off[t + 1]; k += 32) c += (half[src[k]].w * iaL > kExtremeRatio) ? 1 : 0;
+    for (int k = off[t] + lane; k < off[t + 1]; k += 32) c += (half[src[k]].w * iaL > (T)kExtremeRatio) ? 1 : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (lane == 0) row_cnt[t] = c;
 }
-__global__ void k_extreme_fill(int64_t n_nodes, const int32_t *off, const int32_t *src, const float4 *thalf,
-                               const float4 *half, const int32_t *eoff, int32_t *esrc) {
+template <typename T4>
+__global__ void k_extreme_fill(int64_t n_nodes, const int32_t *off, const int32_t *src, const T4 *thalf,
+                               const T4 *half, const int32_t *eoff, int32_t *esrc) {
+    using T = decltype(thalf->w);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_nodes) return;
-    const float iaL = 1.0f / thalf[t].w;
+    const T iaL = (T)1 / thalf[t].w;
     int j = eoff[t];
     for (int k = off[t]; k < off[t + 1]; ++k)
-        if (half[src[k]].w * iaL > kExtremeRatio) esrc[j++] = src[k];
+        if (half[src[k]].w * iaL > (T)kExtremeRatio) esrc[j++] = src[k];
 }
 __global__ void k_set_last(int32_t *off, int64_t rows, const int64_t *total) { off[rows] = (int32_t)*total; }
 __global__ void k_nonempty_rows(int64_t n_nodes, const int32_t *cnt, const int32_t *pos, int32_t *rows) {
@@ -836,6 +859,7 @@ template <typename T> int l2l_impl(const DevTree &tree, FmmBuffers &buf, cudaStr
 }
 
 // extreme-pair CSR for one orientation (float plans only)
+template <typename T4>
 int build_extreme(const DevTree &tree, const DevTree &stree, const int32_t *off, const int32_t *src, ExtremeRows &ext,
                   cudaStream_t s) {
     int rc;
@@ -844,7 +868,7 @@ int build_extreme(const DevTree &tree, const DevTree &stree, const int32_t *off,
     if ((rc = cnt.reserve(sizeof(int32_t) * M)) || (rc = ext.off.reserve(sizeof(int32_t) * (M + 1))) ||
         (rc = tmp.reserve(scan_tmp_bytes(M))) || (rc = total.reserve(sizeof(int64_t))))
         return rc;
-    k_extreme_flags<<<nblk(M * 32, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<float4>(stree.half),
+    k_extreme_flags<T4><<<nblk(M * 32, 128), 128, 0, s>>>(M, off, src, dptr<T4>(tree.half), dptr<T4>(stree.half),
                                                       dptr<int32_t>(cnt));
     EDFMM_LAUNCH_CHECK("k_extreme_flags");
     if ((rc = scan_exclusive(dptr<int32_t>(cnt), dptr<int32_t>(ext.off), M, dptr<int64_t>(total), tmp.p, s))) return rc;
@@ -860,7 +884,7 @@ int build_extreme(const DevTree &tree, const DevTree &stree, const int32_t *off,
     if ((rc = ext.src.reserve(sizeof(int32_t) * n_ext)) || (rc = flag.reserve(sizeof(int32_t) * M)) ||
         (rc = pos.reserve(sizeof(int32_t) * M)) || (rc = ext.rows.reserve(sizeof(int32_t) * M)))
         return rc;
-    k_extreme_fill<<<nblk(M, 128), 128, 0, s>>>(M, off, src, dptr<float4>(tree.half), dptr<float4>(stree.half),
+    k_extreme_fill<T4><<<nblk(M, 128), 128, 0, s>>>(M, off, src, dptr<T4>(tree.half), dptr<T4>(stree.half),
                                                  dptr<int32_t>(ext.off), dptr<int32_t>(ext.src));
     EDFMM_LAUNCH_CHECK("k_extreme_fill");
     k_flag_nonzero<<<nblk(M, 256), 256, 0, s>>>(M, dptr<int32_t>(cnt), dptr<int32_t>(flag));
@@ -894,23 +918,34 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
         EDFMM_LAUNCH_CHECK("k_m2l_generic");
         return EDFMM_OK;
     }
-    if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, tree.center.p,
-                                tree.half.p, stree.center.p, stree.half.p, sbuf.multipoles.p, buf.locals.p,
-                                buf.nc_pad, buf.mask, s))
-        return rc;
-    if (sizeof(T) == 8) return EDFMM_OK;  // FP64 has the range for any scale ratio the tree produces
-    // FP32: pairs whose source scale exceeds 256x the target's, skipped above
-    const float4 *tc = dptr<float4>(tree.center), *th = dptr<float4>(tree.half);
-    const float4 *cen = dptr<float4>(stree.center), *hal = dptr<float4>(stree.half);
+    // FP64 plans in two-float mode: the rotation kernel on the FP32 pipe
+    // (orders 6..8), which leaves extreme pairs like the FP32 kernel does
+    bool two_float = false;
+    if (sizeof(T) == 8 && buf.arith == EDFMM_ARITH_TWO_FLOAT) {
+        int rc = launch_m2l_rot_tf(buf.p, M, off, src, tree.center.p, tree.half.p, stree.center.p, stree.half.p,
+                                   sbuf.multipoles.p, buf.locals.p, buf.nc_pad, buf.mask, s);
+        if (rc == EDFMM_OK) two_float = true;
+        else if (rc != EDFMM_ERR_UNSUPPORTED) return rc;
+    }
+    if (!two_float) {
+        if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, tree.center.p,
+                                    tree.half.p, stree.center.p, stree.half.p, sbuf.multipoles.p, buf.locals.p,
+                                    buf.nc_pad, buf.mask, s))
+            return rc;
+        if (sizeof(T) == 8) return EDFMM_OK;  // FP64 has the range for any scale ratio the tree produces
+    }
+    // FP32 and two-float: pairs whose source scale exceeds 256x the target's, skipped above
+    const T4 *tc = dptr<T4>(tree.center), *th = dptr<T4>(tree.half);
+    const T4 *cen = dptr<T4>(stree.center), *hal = dptr<T4>(stree.half);
     ExtremeRows &ext = swapped ? buf.extreme_swapped : buf.extreme;
     if (!ext.built) {
-        int rc = build_extreme(tree, stree, off, src, ext, s);
+        int rc = build_extreme<T4>(tree, stree, off, src, ext, s);
         if (rc) return rc;
     }
     if (ext.n_pairs > 0) {
-        k_m2l_generic<float><<<nblk(ext.n_rows, 4), 128, 0, s>>>(
+        k_m2l_generic<T><<<nblk(ext.n_rows, 4), 128, 0, s>>>(
             ext.n_rows, dptr<int32_t>(ext.rows), dptr<int32_t>(ext.off), dptr<int32_t>(ext.src), tc, th, cen, hal,
-            dptr<Cplx<float>>(sbuf.multipoles), dptr<Cplx<float>>(buf.locals), buf.p, buf.nc_pad, 1);
+            dptr<Cplx<T>>(sbuf.multipoles), dptr<Cplx<T>>(buf.locals), buf.p, buf.nc_pad, 1);
         EDFMM_LAUNCH_CHECK("k_m2l_generic");
     }
     return EDFMM_OK;
@@ -920,6 +955,13 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
 
 int set_charges(const DevTree &tree, const void *a, const void *b, cudaStream_t s) {
     if (tree.n_points == 0) return EDFMM_OK;
+    if (tree.dtype == EDFMM_F64 && tree.pts_tf.p) {
+        k_set_charges_split<<<nblk(tree.n_points, 256), 256, 0, s>>>(
+            dptr<double4>(tree.pts), dptr<float4>(tree.pts_tf), dptr<int32_t>(tree.index_map), tree.n_points,
+            static_cast<const double *>(a), static_cast<const double *>(b));
+        EDFMM_LAUNCH_CHECK("k_set_charges_split");
+        return EDFMM_OK;
+    }
     if (tree.dtype == EDFMM_F64)
         k_set_charges<double><<<nblk(tree.n_points, 256), 256, 0, s>>>(dptr<double4>(tree.pts), dptr<int32_t>(tree.index_map),
                                                                       tree.n_points, static_cast<const double *>(a),
@@ -946,6 +988,12 @@ int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists
                 FmmBuffers &tgt_buf, cudaStream_t s) {
     return tgt_tree.dtype == EDFMM_F64 ? m2l_impl<double>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s)
                                        : m2l_impl<float>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s);
+}
+int prepare_extreme_rows(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, cudaStream_t s) {
+    if (buf.extreme.built || tree.n_nodes == 0) return EDFMM_OK;
+    const int32_t *off = dptr<int32_t>(lists.m2l_off), *src = dptr<int32_t>(lists.m2l_src);
+    return tree.dtype == EDFMM_F64 ? build_extreme<double4>(tree, tree, off, src, buf.extreme, s)
+                                   : build_extreme<float4>(tree, tree, off, src, buf.extreme, s);
 }
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
     return tree.dtype == EDFMM_F64 ? l2l_impl<double>(tree, buf, s) : l2l_impl<float>(tree, buf, s);

@@ -16,9 +16,12 @@
 // azimuth-factored contraction.  One lane per (target, source) pair, one
 // warp per target row; each lane accumulates its translated locals in
 // private shared-memory slots, reduced over the warp at the end (fixed order).
+#include <type_traits>
+
 #include "edfmm_internal.cuh"
 #include "harmonics.cuh"
 #include "rotation_tables.h"
+#include "twofloat.cuh"
 
 namespace edfmm {
 namespace {
@@ -34,7 +37,16 @@ template <int TAB> __host__ __device__ constexpr double rot_entry(int i) {
 template <typename T, int TAB, int N, int OFF, int I, int J>
 __device__ __forceinline__ void rot_dot(const T (&x)[N], T &acc) {
     constexpr double g = rot_entry<TAB>(OFF + I * N + J);
-    if constexpr (g != 0.0) acc = fma((T)g, x[J], acc);
+    if constexpr (g != 0.0) {
+        if constexpr (std::is_same<T, tf32x2>::value) {
+            // the table entries are dyadic rationals: nearly all exact in FP32
+            constexpr float ghi = (float)g;
+            constexpr float glo = (float)(g - (double)ghi);
+            acc = tf_fma_const<glo == 0.0f>(ghi, glo, x[J], acc);
+        } else {
+            acc = fma((T)g, x[J], acc);
+        }
+    }
     if constexpr (J + 1 < N) rot_dot<T, TAB, N, OFF, I, J + 1>(x, acc);
 }
 template <typename T, int TAB, int N, int OFF, int I>
@@ -98,6 +110,17 @@ __device__ __forceinline__ void sts_keep(float *p, float v) {
 }
 __device__ __forceinline__ void sts_keep(double *p, double v) {
     asm volatile("st.volatile.shared.f64 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "d"(v));
+}
+__device__ __forceinline__ tf32x2 lds_keep(const tf32x2 *p) {
+    tf32x2 v;
+    asm volatile("ld.volatile.shared.v2.f32 {%0, %1}, [%2];"
+                 : "=f"(v.hi), "=f"(v.lo)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ void sts_keep(tf32x2 *p, tf32x2 v) {
+    asm volatile("st.volatile.shared.v2.f32 [%0], {%1, %2};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v.hi),
+                 "f"(v.lo));
 }
 template <typename T, int STRIDE> struct SmemV {
     T *base;  // this lane's slot 0; slot i at base[i * STRIDE]
@@ -363,7 +386,178 @@ __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? 3 : 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Two-float M2L for FP64 plans.  The same rotation algorithm on the FP32 pipe
+// in two-float arithmetic (about 48 significant bits; twofloat.cuh): the
+// multipoles are read as FP64 and split, the pair geometry is formed in FP64
+// and split, and the locals are written back as FP64.  Each lane's
+// translated locals go back into its own coefficient slots (81 two-float
+// values at p = 8), and after every round of 32 pairs the warp adds the
+// slots of its lanes, lane i owning coefficients i, i + 32, i + 64 in
+// registers; so a block needs 81 KB of shared memory and two blocks share an
+// SM (the FP64 kernel's per-lane accumulators allow one).  Pairs whose source
+// scale exceeds 256x the target's are left to the caller (FP32 exponent
+// range), as in the FP32 kernel.
+// ---------------------------------------------------------------------------
+template <int P, int n, typename V>
+__device__ __forceinline__ void backward_tf(V &v, const Frame<tf32x2, P> &F) {
+    constexpr int N = 2 * n + 1, OV = n * n, OFF = kRotOff[n];
+    tf32x2 b[N], o[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) b[i] = v.get(OV + i);
+    rot_apply<tf32x2, 3, N, OFF, 0>(b, o);
+    zrot<tf32x2, N, P>(o, F.ct, F.st, tf32x2(-1));
+    rot_apply<tf32x2, 2, N, OFF, 0>(o, b);
+    zrot<tf32x2, N, P>(b, F.cp, F.sp, tf32x2(-1));
+#pragma unroll
+    for (int i = 0; i < N; ++i) v.set(OV + i, b[i]);
+    if constexpr (n < P) backward_tf<P, n + 1>(v, F);
+}
+
+// One pair: v <- the translated locals (real block basis) of source row Mrow.
+template <int P, typename V>
+__device__ __forceinline__ void rot_pair_tf(V &v, const double2 *__restrict__ Mrow, tf32x2 c, tf32x2 dx, tf32x2 dy,
+                                            tf32x2 dz) {
+    using T = tf32x2;
+#pragma unroll
+    for (int n = 0; n <= P; ++n) {
+#pragma unroll
+        for (int m = 0; m <= n; ++m) {
+            const double2 x = Mrow[tri(n, m)];
+            if (m == 0) {
+                v.set(n * n, tf_from_double(x.x));
+            } else {
+                v.set(n * n + 2 * m - 1, tf_from_double(x.x));
+                v.set(n * n + 2 * m, tf_from_double(x.y));
+            }
+        }
+    }
+    const T s2 = fma(dy, dy, dx * dx), r2 = fma(dz, dz, s2);
+    const T s = sqrt(s2), rho = sqrt(r2), irho = tf_recip(rho);
+    Frame<T, P> F;
+    T cphi = T(1), sphi = T(0);
+    if (s2.hi > 0.0f) {
+        const T is = tf_recip(s);
+        cphi = dx * is;
+        sphi = dy * is;
+    }
+    powers<T, P>(cphi, sphi, F.cp, F.sp);
+    powers<T, P>(dz * irho, s * irho, F.ct, F.st);
+    forward<T, P, 0>(v, c, T(1), F);
+    T f[2 * P + 1];
+    f[0] = irho;
+#pragma unroll
+    for (int j = 1; j <= 2 * P; ++j) f[j] = f[j - 1] * T(j) * irho;
+    float2 f2[2 * P + 1];
+    axial<T, P, 0>(v, f, f2);
+    backward_tf<P, 0>(v, F);
+}
+
+template <int P>
+__global__ void __launch_bounds__(kRotThreads, 2)
+    k_m2l_rot_tf(int64_t n_nodes, const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+                 const double4 *__restrict__ tcenter, const double4 *__restrict__ thalf,
+                 const double4 *__restrict__ center, const double4 *__restrict__ half,
+                 const double2 *__restrict__ Mexp, double2 *__restrict__ Lexp, int nc_pad, const InstMask mask) {
+    using T = tf32x2;
+    constexpr int NV = (P + 1) * (P + 1), NT = kRotThreads, NR = (NV + 31) / 32;
+    extern __shared__ __align__(16) unsigned char rot_smem[];
+    __shared__ int max_rounds;
+    T *slots = reinterpret_cast<T *>(rot_smem);  // slot i of thread u at slots[i * NT + u]
+    SmemV<T, NT> v{slots + threadIdx.x};
+    const int64_t t = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int wbase = threadIdx.x & ~31;
+    const bool live = t < n_nodes && inst_active(mask, (int)t);
+    double4 ct{};
+    double iaL = 1.0;
+    int b = 0, e = 0;
+    if (live) {
+        ct = tcenter[t];
+        iaL = 1.0 / thalf[t].w;
+        b = off[t];
+        e = off[t + 1];
+    }
+    T acc[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = T(0);
+    if (threadIdx.x == 0) max_rounds = 0;
+    __syncthreads();
+    if (lane == 0) atomicMax(&max_rounds, (e - b + 31) >> 5);
+    __syncthreads();
+    const int rounds = max_rounds;
+    for (int r = 0; r < rounds; ++r) {
+        const int k = b + r * 32 + lane;
+        bool have = false;
+        if (k < e) {
+            const int s = __ldg(src + k);
+            const double4 cs = center[s];
+            const double c = half[s].w * iaL;
+            if (!(c > (double)kRotExtremeRatio)) {
+                have = true;
+                rot_pair_tf<P>(v, Mexp + (int64_t)s * nc_pad, tf_from_double(c), tf_from_double((ct.x - cs.x) * iaL),
+                               tf_from_double((ct.y - cs.y) * iaL), tf_from_double((ct.z - cs.z) * iaL));
+            }
+        }
+        if (!have) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) v.set(i, T(0));
+        }
+        __syncwarp();
+        // coefficient i = lane + 32 j summed over the warp's lanes, starting at
+        // this lane (conflict-free shared-memory reads; a fixed order per i)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+            const int i = lane + 32 * j;
+            if (i < NV) {
+                T sum = acc[j];
+                const T *row = slots + i * NT + wbase;
+#pragma unroll 8
+                for (int l = 0; l < 32; ++l) sum = sum + lds_keep(row + ((l + lane) & 31));
+                acc[j] = sum;
+            }
+        }
+        __syncwarp();
+    }
+    if (!live) return;
+    double *out = reinterpret_cast<double *>(Lexp + t * nc_pad);
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+        const int i = lane + 32 * j;
+        if (i < NV) {
+            int n = 0;
+            while ((n + 1) * (n + 1) <= i) ++n;
+            const int q = i - n * n;  // 0: Re X0; 2m - 1: Re Xm; 2m: Im Xm
+            const double val = tf_to_double(acc[j]) * iaL;
+            if (q == 0) {
+                out[2 * tri(n, 0)] = val;
+                out[2 * tri(n, 0) + 1] = 0.0;
+            } else {
+                out[2 * tri(n, (q + 1) >> 1) + ((q & 1) ? 0 : 1)] = val;
+            }
+        }
+    }
+}
+
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <int P>
+int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
+                  const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+                  cudaStream_t s) {
+    constexpr int NV = (P + 1) * (P + 1), NT = kRotThreads;
+    constexpr size_t smem = (size_t)NV * NT * sizeof(tf32x2);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_m2l_rot_tf<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess)
+        return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot_tf shared memory attribute: ") + cudaGetErrorString(attr));
+    k_m2l_rot_tf<P><<<nblk(M * 32, NT), NT, smem, s>>>(
+        M, off, src, static_cast<const double4 *>(tcen), static_cast<const double4 *>(thal),
+        static_cast<const double4 *>(cen), static_cast<const double4 *>(hal), static_cast<const double2 *>(Mx),
+        static_cast<double2 *>(Lx), nc_pad, mask);
+    EDFMM_LAUNCH_CHECK("k_m2l_rot_tf");
+    return EDFMM_OK;
+}
 
 template <typename T, int P, bool V_IN_SMEM>
 int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal, const void *cen,
@@ -411,6 +605,20 @@ int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_
             return fail(EDFMM_ERR_UNSUPPORTED, "rotation M2L supports orders 1..8");
     }
 #undef EDFMM_ROT_CASE
+}
+
+// Two-float M2L of an FP64 plan (orders 6..8); returns EDFMM_ERR_UNSUPPORTED
+// for other orders (the caller then runs the FP64 kernel).
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
+                      const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+                      cudaStream_t s) {
+    if (M <= 0) return EDFMM_OK;
+    switch (p) {
+        case 6: return launch_rot_tf<6>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
+        case 7: return launch_rot_tf<7>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
+        case 8: return launch_rot_tf<8>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
+        default: return EDFMM_ERR_UNSUPPORTED;
+    }
 }
 
 }  // namespace edfmm

@@ -15,9 +15,11 @@
 // bem_fmm.py:718-749 (K_E, original order, self term, non-finite -> 0), so
 // each output is written exactly once.
 #include <cfloat>
+#include <type_traits>
 
 #include "edfmm_internal.cuh"
 #include "harmonics.cuh"
+#include "twofloat.cuh"
 
 namespace edfmm {
 
@@ -25,6 +27,7 @@ namespace {
 
 __constant__ float c_rdiv_f[kPMax + 1][kPMax + 1];
 __constant__ double c_rdiv_d[kPMax + 1][kPMax + 1];
+__constant__ float2 c_rdiv_tf[kPMax + 1][kPMax + 1];  // (hi, lo) of the FP64 table
 
 template <typename T> __device__ __forceinline__ T rdiv(int n, int m);
 template <> __device__ __forceinline__ float rdiv<float>(int n, int m) { return c_rdiv_f[n][m]; }
@@ -65,6 +68,39 @@ __device__ __forceinline__ T l2p_point(const Cplx<T> *L, int p, T x, T y, T z) {
     return acc;
 }
 
+// l2p_point in two-float arithmetic, on two-float locals
+__device__ __forceinline__ tf32x2 l2p_point_tf(const tf32x2c *L, int p, tf32x2 x, tf32x2 y, tf32x2 z) {
+    using T = tf32x2;
+    const T r2 = fma(z, z, fma(y, y, x * x));
+    T acc = T(0), dr = T(1), di = T(0);
+    for (int m = 0; m <= p; ++m) {
+        if (m > 0) {
+            const float2 rd = c_rdiv_tf[m][0];
+            const T sc = T(rd.x, rd.y) * T(-m) * T(0.5);  // -1 / (2m)
+            const T nr = sc * (x * dr - y * di), ni = sc * (x * di + y * dr);
+            dr = nr;
+            di = ni;
+        }
+        T pr = dr, pi = di, qr = T(0), qi = T(0);
+        tf32x2c lv = L[tri(m, m)];
+        T col = lv.x * pr - lv.y * pi;
+        for (int n = m + 1; n <= p; ++n) {
+            const float2 rd = c_rdiv_tf[n][m];
+            const T d(rd.x, rd.y);
+            const T c1 = T(2 * n - 1) * z;
+            const T nr = (c1 * pr - r2 * qr) * d, ni = (c1 * pi - r2 * qi) * d;
+            lv = L[tri(n, m)];
+            col = col + (lv.x * nr - lv.y * ni);
+            qr = pr;
+            qi = pi;
+            pr = nr;
+            pi = ni;
+        }
+        acc = m == 0 ? acc + col : acc + T(2) * col;
+    }
+    return acc;
+}
+
 template <typename T> struct NearParams {
     const int32_t *leaves;
     int64_t n_leaves;
@@ -73,6 +109,7 @@ template <typename T> struct NearParams {
     const typename Vec4<T>::type *pts;   // targets
     const int2 *range;                   // target leaves' point ranges
     const typename Vec4<T>::type *spts;  // sources (== pts for one tree)
+    const float4 *spts_tf;               // two-float mode: sources as (xh, xl, yh, yl), (zh, zl, qh, ql)
     const int2 *srange;
     int same;                            // one tree: drop i == j in self pairs
     const typename Vec4<T>::type *center;
@@ -110,6 +147,11 @@ template <> struct Slot<float> {
 template <> struct Slot<double> {
     double x, y, z;
     double ps;
+    int ti;
+};
+template <> struct Slot<tf32x2> {
+    tf32x2 x, y, z;
+    tf32x2 ps;
     int ti;
 };
 
@@ -156,6 +198,28 @@ __device__ __forceinline__ void accumulate_slot(const double4 *sp, int cnt, int 
     S.ps += ps;  // per-chunk partial, then one add: two-level summation
 }
 
+// Two-float: one source per step from the staged split arrays
+// (xh, xl, yh, yl, zh, zl, qh, ql; 64 each).  The coordinate differences
+// are formed from the split parts, so the cancellation of nearby points
+// loses nothing; 1 / r takes one Newton step from the FP32 estimate.
+template <int G, bool SELF>
+__device__ __forceinline__ void accumulate_slot(const float *s8, int cnt, int sbase, int part, Slot<tf32x2> &S,
+                                                float eps2) {
+    tf32x2 ps = tf32x2(0);
+#pragma unroll 2
+    for (int j = part; j < cnt; j += G) {
+        const tf32x2 dx = S.x - tf32x2(s8[j], s8[64 + j]);
+        const tf32x2 dy = S.y - tf32x2(s8[128 + j], s8[192 + j]);
+        const tf32x2 dz = S.z - tf32x2(s8[256 + j], s8[320 + j]);
+        tf32x2 r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+        if (!(r2.hi >= eps2)) r2 = tf32x2(eps2, 0.0f);
+        tf32x2 inv = tf_rsqrt(r2, rsqrt_normal(r2.hi));
+        if (SELF && sbase + j == S.ti) inv = tf32x2(0);
+        ps = fma(tf32x2(s8[384 + j], s8[448 + j]), inv, ps);
+    }
+    S.ps = S.ps + ps;  // per-chunk partial, then one add: two-level summation
+}
+
 template <typename T, int G>
 __device__ __forceinline__ void slot_init(const NearParams<T> &P, int tb, int te, int base, int lane, Slot<T> &S) {
     const int ti = tb + base + lane / G;
@@ -174,6 +238,26 @@ __device__ __forceinline__ void slot_init(const NearParams<T> &P, int tb, int te
     }
 }
 
+template <int G>
+__device__ __forceinline__ void slot_init(const NearParams<double> &P, int tb, int te, int base, int lane,
+                                          Slot<tf32x2> &S) {
+    const int ti = tb + base + lane / G;
+    S.ti = ti < te ? ti : -1;
+    const double4 x = P.pts[ti < te ? ti : tb];
+    S.x = tf_from_double(x.x);
+    S.y = tf_from_double(x.y);
+    S.z = tf_from_double(x.z);
+    S.ps = tf32x2(0);
+}
+
+template <int G>
+__device__ __forceinline__ void slot_finish(Slot<tf32x2> &S, int lane, int tb, double *pot) {
+    tf32x2 a = S.ps;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) a = a + tf_shfl_xor(a, o);
+    if (lane % G == 0 && S.ti >= 0) pot[S.ti - tb] = tf_to_double(a);
+}
+
 template <typename T, int G>
 __device__ __forceinline__ void slot_finish(Slot<T> &S, int lane, int tb, T *pot) {
     T a;
@@ -186,9 +270,9 @@ __device__ __forceinline__ void slot_finish(Slot<T> &S, int lane, int tb, T *pot
     if (lane % G == 0 && S.ti >= 0) pot[S.ti - tb] = a;
 }
 
-template <typename T, bool SELF, typename C>
+template <typename T, bool SELF, typename C, typename E>
 __device__ __forceinline__ void accumulate_slots(const C *chunk, int cnt, int sb, int lane, const bool (&on)[5],
-                                                 Slot<T> (&S)[5], T eps2) {
+                                                 Slot<T> (&S)[5], E eps2) {
     if (on[0]) accumulate_slot<1, SELF>(chunk, cnt, sb, 0, S[0], eps2);
     if (on[1]) accumulate_slot<1, SELF>(chunk, cnt, sb, 0, S[1], eps2);
     if (on[2]) accumulate_slot<2, SELF>(chunk, cnt, sb, lane % 2, S[2], eps2);
@@ -204,10 +288,16 @@ __device__ __forceinline__ void accumulate_slots(const C *chunk, int cnt, int sb
 // lane) and broadcast by shuffles, and the next chunk's points are loaded
 // before the current chunk is computed, so the dependent global loads
 // overlap the arithmetic.
-template <typename T>
+struct SplitPt {  // two-float source point: (xh, xl, yh, yl), (zh, zl, qh, ql)
+    float4 a, b;
+};
+
+template <typename T, bool TF>
 __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb, int te,
                                            typename Vec4<T>::type *sp, T *pot, const Cplx<T> *sL) {
     using T4 = typename Vec4<T>::type;
+    using ST = std::conditional_t<TF, tf32x2, T>;      // slot arithmetic
+    using Pre = std::conditional_t<TF, SplitPt, T4>;  // prefetched source point
     const int lane = threadIdx.x & 31;
     const int nt = te - tb;
     bool on[5];
@@ -229,12 +319,20 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
         on[4] = (rem & 4) != 0;
         base[4] = o;
     }
-    Slot<T> S[5];
-    slot_init<T, 1>(P, tb, te, base[0], lane, S[0]);
-    slot_init<T, 1>(P, tb, te, base[1], lane, S[1]);
-    slot_init<T, 2>(P, tb, te, base[2], lane, S[2]);
-    slot_init<T, 4>(P, tb, te, base[3], lane, S[3]);
-    slot_init<T, 8>(P, tb, te, base[4], lane, S[4]);
+    Slot<ST> S[5];
+    if constexpr (TF) {
+        slot_init<1>(P, tb, te, base[0], lane, S[0]);
+        slot_init<1>(P, tb, te, base[1], lane, S[1]);
+        slot_init<2>(P, tb, te, base[2], lane, S[2]);
+        slot_init<4>(P, tb, te, base[3], lane, S[3]);
+        slot_init<8>(P, tb, te, base[4], lane, S[4]);
+    } else {
+        slot_init<T, 1>(P, tb, te, base[0], lane, S[0]);
+        slot_init<T, 1>(P, tb, te, base[1], lane, S[1]);
+        slot_init<T, 2>(P, tb, te, base[2], lane, S[2]);
+        slot_init<T, 4>(P, tb, te, base[3], lane, S[3]);
+        slot_init<T, 8>(P, tb, te, base[4], lane, S[4]);
+    }
     if (P.near) {
         const T eps2 = P.eps2;
         const int kbeg = P.off[t], kend = P.off[t + 1];
@@ -247,17 +345,40 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
             sa_l = r.x;
             se_l = r.y;
         };
-        auto fetch = [&](int sb, int se, int i) { return i < se - sb ? P.spts[sb + i] : T4{0, 0, 0, 0}; };
+        auto fetch = [&](int sb, int se, int i) -> Pre {
+            if constexpr (TF) {
+                if (i < se - sb) return SplitPt{P.spts_tf[2 * (sb + i)], P.spts_tf[2 * (sb + i) + 1]};
+                return SplitPt{make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+            } else {
+                return i < se - sb ? P.spts[sb + i] : T4{0, 0, 0, 0};
+            }
+        };
         if (kbeg < kend) {
             load_batch(kbeg);
             int k = kbeg;
             int s = __shfl_sync(0xffffffffu, s_l, 0), sb = __shfl_sync(0xffffffffu, sa_l, 0),
                 se = __shfl_sync(0xffffffffu, se_l, 0);
-            T4 qa = fetch(sb, se, lane), qb = fetch(sb, se, lane + 32);
+            Pre qa = fetch(sb, se, lane), qb = fetch(sb, se, lane + 32);
             while (true) {
                 const int cs = s, csb = sb, cnt = min(64, se - sb);
                 __syncwarp();
-                if constexpr (sizeof(T) == 4) {
+                if constexpr (TF) {
+                    float *s8 = reinterpret_cast<float *>(sp);
+                    const float4 qs[4] = {qa.a, qa.b, qb.a, qb.b};
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float4 u = qs[2 * h], w = qs[2 * h + 1];
+                        const int o = lane + 32 * h;
+                        s8[o] = u.x;
+                        s8[64 + o] = u.y;
+                        s8[128 + o] = u.z;
+                        s8[192 + o] = u.w;
+                        s8[256 + o] = w.x;
+                        s8[320 + o] = w.y;
+                        s8[384 + o] = w.z;
+                        s8[448 + o] = w.w;
+                    }
+                } else if constexpr (sizeof(T) == 4) {
                     float *sx = reinterpret_cast<float *>(sp);
                     sx[lane] = qa.x;
                     sx[64 + lane] = qa.y;
@@ -287,7 +408,13 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
                     qa = fetch(sb, se, lane);
                     qb = fetch(sb, se, lane + 32);
                 }
-                if constexpr (sizeof(T) == 4) {
+                if constexpr (TF) {
+                    const float *s8 = reinterpret_cast<const float *>(sp);
+                    if (P.same && cs == t)
+                        accumulate_slots<tf32x2, true>(s8, cnt, csb, lane, on, S, (float)eps2);
+                    else
+                        accumulate_slots<tf32x2, false>(s8, cnt, csb, lane, on, S, (float)eps2);
+                } else if constexpr (sizeof(T) == 4) {
                     const float *sx = reinterpret_cast<const float *>(sp);
                     if (P.same && cs == t)
                         accumulate_slots<T, true>(sx, cnt, csb, lane, on, S, eps2);
@@ -303,11 +430,19 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
             }
         }
     }
-    slot_finish<T, 1>(S[0], lane, tb, pot);
-    slot_finish<T, 1>(S[1], lane, tb, pot);
-    slot_finish<T, 2>(S[2], lane, tb, pot);
-    slot_finish<T, 4>(S[3], lane, tb, pot);
-    slot_finish<T, 8>(S[4], lane, tb, pot);
+    if constexpr (TF) {
+        slot_finish<1>(S[0], lane, tb, pot);
+        slot_finish<1>(S[1], lane, tb, pot);
+        slot_finish<2>(S[2], lane, tb, pot);
+        slot_finish<4>(S[3], lane, tb, pot);
+        slot_finish<8>(S[4], lane, tb, pot);
+    } else {
+        slot_finish<T, 1>(S[0], lane, tb, pot);
+        slot_finish<T, 1>(S[1], lane, tb, pot);
+        slot_finish<T, 2>(S[2], lane, tb, pot);
+        slot_finish<T, 4>(S[3], lane, tb, pot);
+        slot_finish<T, 8>(S[4], lane, tb, pot);
+    }
     __syncwarp();
     T4 c;
     T ia = (T)1;
@@ -320,7 +455,14 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
         const T4 x = P.pts[ti];
         T v = P.near ? pot[i] : (T)0;
         if (P.add_in) v += P.add_in[ti];
-        if (P.far) v += l2p_point<T>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
+        if (P.far) {
+            if constexpr (TF)
+                v += tf_to_double(l2p_point_tf(reinterpret_cast<const tf32x2c *>(sL), P.p,
+                                               tf_from_double((x.x - c.x) * ia), tf_from_double((x.y - c.y) * ia),
+                                               tf_from_double((x.z - c.z) * ia)));
+            else
+                v += l2p_point<T>(sL, P.p, (x.x - c.x) * ia, (x.y - c.y) * ia, (x.z - c.z) * ia);
+        }
         if (P.scatter) {
             const int o = P.index_map[ti];
             v = v * P.k_e;
@@ -334,7 +476,8 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
     __syncwarp();
 }
 
-template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 4) k_p2p_l2p(const NearParams<T> P) {
+template <typename T, bool TF>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 4) k_p2p_l2p(const NearParams<T> P) {
     using T4 = typename Vec4<T>::type;
     __shared__ T4 sp[4][64];  // a staged chunk of up to 64 sources
     __shared__ Cplx<T> sL[4][ncoef(kPMax)];
@@ -346,11 +489,18 @@ template <typename T> __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 
     if (!inst_active(P.mask, t)) return;  // uniform over the warp; the kernel has no block barrier
     if (P.far) {
         const int nc = ncoef(P.p);
-        for (int k = lane; k < nc; k += 32) sL[wl][k] = P.Lexp[(int64_t)t * P.nc_pad + k];
+        for (int k = lane; k < nc; k += 32) {
+            const Cplx<T> c = P.Lexp[(int64_t)t * P.nc_pad + k];
+            if constexpr (TF)  // staged as two-float (the same 16 bytes per coefficient)
+                reinterpret_cast<tf32x2c *>(sL[wl])[k] = tf32x2c{tf_from_double(c.re), tf_from_double(c.im)};
+            else
+                sL[wl][k] = c;
+        }
         __syncwarp();
     }
     const int2 rg = P.range[t];
-    for (int tb = rg.x; tb < rg.y; tb += 64) leaf_slots<T>(P, t, tb, min(rg.y, tb + 64), sp[wl], spot[wl], sL[wl]);
+    for (int tb = rg.x; tb < rg.y; tb += 64)
+        leaf_slots<T, TF>(P, t, tb, min(rg.y, tb + 64), sp[wl], spot[wl], sL[wl]);
 }
 
 }  // namespace
@@ -367,8 +517,15 @@ int upload_tables() {
             hd[n][m] = d != 0 ? 1.0 / d : 0.0;
             hf[n][m] = (float)hd[n][m];
         }
+    float2 ht[kPMax + 1][kPMax + 1];
+    for (int n = 0; n <= kPMax; ++n)
+        for (int m = 0; m <= kPMax; ++m) {
+            ht[n][m].x = (float)hd[n][m];
+            ht[n][m].y = (float)(hd[n][m] - (double)ht[n][m].x);
+        }
     EDFMM_CUDA_TRY(cudaMemcpyToSymbol(c_rdiv_f, hf, sizeof(hf)));
     EDFMM_CUDA_TRY(cudaMemcpyToSymbol(c_rdiv_d, hd, sizeof(hd)));
+    EDFMM_CUDA_TRY(cudaMemcpyToSymbol(c_rdiv_tf, ht, sizeof(ht)));
     return EDFMM_OK;
 }
 
@@ -386,6 +543,9 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     P.pts = dptr<T4>(tree.pts);
     P.range = dptr<int2>(tree.range);
     P.spts = a.src_tree ? dptr<T4>(a.src_tree->pts) : P.pts;
+    // two-float near field: an FP64 plan (one tree) whose split points exist
+    const bool tf = sizeof(T) == 8 && !a.src_tree && buf.arith == EDFMM_ARITH_TWO_FLOAT && tree.pts_tf.p;
+    P.spts_tf = tf ? dptr<float4>(tree.pts_tf) : nullptr;
     P.srange = a.src_tree ? dptr<int2>(a.src_tree->range) : P.range;
     P.same = a.src_tree ? 0 : 1;
     P.center = dptr<T4>(tree.center);
@@ -406,7 +566,14 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     P.self_int = static_cast<const T *>(a.self_int);
     P.k_e = (T)a.k_e;
     P.out = static_cast<T *>(a.out);
-    k_p2p_l2p<T><<<(unsigned)((tree.n_leaves + 3) / 4), 128, 0, s>>>(P);
+    if constexpr (sizeof(T) == 8) {
+        if (tf) {
+            k_p2p_l2p<T, true><<<(unsigned)((tree.n_leaves + 3) / 4), 128, 0, s>>>(P);
+            EDFMM_LAUNCH_CHECK("k_p2p_l2p (two-float)");
+            return EDFMM_OK;
+        }
+    }
+    k_p2p_l2p<T, false><<<(unsigned)((tree.n_leaves + 3) / 4), 128, 0, s>>>(P);
     EDFMM_LAUNCH_CHECK("k_p2p_l2p");
     return EDFMM_OK;
 }

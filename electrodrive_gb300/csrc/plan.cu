@@ -398,6 +398,28 @@ int edfmm_plan_destroy(edfmm_plan *plan) {
     return EDFMM_OK;
 }
 
+int edfmm_plan_set_arithmetic(edfmm_plan *p, int mode, void *stream) {
+    if (int rc = check_plan(p)) return rc;
+    if (mode != EDFMM_ARITH_NATIVE && mode != EDFMM_ARITH_TWO_FLOAT)
+        return fail(EDFMM_ERR_ARG, "mode must be EDFMM_ARITH_NATIVE or EDFMM_ARITH_TWO_FLOAT");
+    cudaStream_t s = S(stream);
+    if (mode == EDFMM_ARITH_NATIVE) {
+        p->tree.pts_tf.release();
+        p->fmm.arith = EDFMM_ARITH_NATIVE;
+        return EDFMM_OK;
+    }
+    if (p->tree.dtype != EDFMM_F64) return fail(EDFMM_ERR_UNSUPPORTED, "two-float arithmetic applies to FP64 plans");
+    if (p->tree.n_points > 0) {
+        if (int rc = p->tree.pts_tf.reserve(sizeof(float) * 8 * (size_t)p->tree.n_points)) return rc;
+        if (int rc = set_charges(p->tree, nullptr, nullptr, s)) return rc;  // splits the points and charges
+    }
+    // the pairs the two-float M2L leaves to the FP64 kernel, built now (it
+    // synchronises the stream) rather than inside a later matvec
+    if (int rc = prepare_extreme_rows(p->tree, p->lists, p->fmm, s)) return rc;
+    p->fmm.arith = EDFMM_ARITH_TWO_FLOAT;
+    return EDFMM_OK;
+}
+
 int edfmm_plan_rebuild_lists(edfmm_plan *p, double mac_theta, void *stream) {
     if (int rc = check_plan(p)) return rc;
     if (!(mac_theta > 0.0 && mac_theta < 1.0)) return fail(EDFMM_ERR_ARG, "mac_theta must be in (0, 1)");
@@ -406,6 +428,9 @@ int edfmm_plan_rebuild_lists(edfmm_plan *p, double mac_theta, void *stream) {
     p->mac_theta = mac_theta;
     p->fmm.extreme = ExtremeRows();
     p->fmm.extreme_swapped = ExtremeRows();
+    if (p->fmm.arith == EDFMM_ARITH_TWO_FLOAT) {
+        if (int rc = prepare_extreme_rows(p->tree, p->lists, p->fmm, S(stream))) return rc;
+    }
     return EDFMM_OK;
 }
 

@@ -49,6 +49,10 @@ extern "C" {
 #define EDFMM_NO_FARFIELD 2          /* near field only (P2P) */
 #define EDFMM_NO_NEARFIELD 4         /* far field only (P2M..L2P) */
 
+/* arithmetic of an FP64 plan's M2L and near field (edfmm_plan_set_arithmetic) */
+#define EDFMM_ARITH_NATIVE 0         /* IEEE FP64 */
+#define EDFMM_ARITH_TWO_FLOAT 1      /* two-float (hi + lo FP32 pairs, about 48 bits) on the FP32 pipe */
+
 typedef struct edfmm_plan edfmm_plan;
 
 typedef struct {
@@ -124,6 +128,20 @@ EDFMM_API int edfmm_plan_destroy(edfmm_plan *plan);
  * electrodrive/fmm3d/interaction_lists.py:531-577).
  */
 EDFMM_API int edfmm_plan_rebuild_lists(edfmm_plan *plan, double mac_theta, void *stream);
+
+/*
+ * Arithmetic of an FP64 plan's M2L (orders 6..8) and near field (no
+ * counterpart in the reference, whose FP64 path is IEEE FP64 throughout):
+ * EDFMM_ARITH_TWO_FLOAT evaluates them on the FP32 pipe in two-float
+ * arithmetic (each value an unevaluated sum of two floats, about 48
+ * significant bits; within about 1e-13 of the FP64 result, far inside the
+ * expansion's truncation error), which on this GPU runs several times faster
+ * than FP64; the expansions, P2M, M2M, L2L and every input and output stay
+ * FP64.  EDFMM_ARITH_NATIVE (the default) restores IEEE FP64.  Two-float mode
+ * keeps a split copy of the points (32 bytes per point) and synchronises
+ * `stream` once while it prepares.  FP32 plans accept only EDFMM_ARITH_NATIVE.
+ */
+EDFMM_API int edfmm_plan_set_arithmetic(edfmm_plan *plan, int mode, void *stream);
 
 /*
  * Change the expansion order p (FmmConfig.expansion_order,

@@ -263,6 +263,70 @@ def save_solve_cases():
     np.savez_compressed(os.path.join(HERE, "solve_cases.npz"), **out)
 
 
+def save_refine_cases():
+    """electrodrive/core/bem.py:1550 bem_solve with more than one pass
+    (h-refinement and best-pass selection, :1667-2495) and with a GMRES that
+    cannot meet its tolerance (retry without the preconditioner, then the
+    damped-Jacobi fallback, :2172-2302), FP64, CPU."""
+    import tempfile
+
+    from electrodrive.core.bem import bem_solve
+    from electrodrive.utils.config import BEMConfig
+    from electrodrive.utils.logging import JsonlLogger
+
+    sphere = ([dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=0.0)],
+              [dict(type="point", q=1.0, pos=[0.0, 0.0, 2.0])])
+    sphere1 = ([dict(type="sphere", radius=1.0, center=[0.0, 0.0, 0.0], potential=1.0)],
+               [dict(type="point", q=1.0, pos=[0.0, 0.0, 2.0])])
+    torus = ([dict(type="torus", major_radius=1.0, minor_radius=0.35, potential=1.0)],
+             [dict(type="point", q=1.0, pos=[1.6, 0.3, 0.2])])
+    # name: (spec, cfg overrides)
+    cases = {
+        # the first pass meets the target: the loop stops before max_refine_passes
+        "sphere_stop_on_bc": (sphere, dict(initial_h=0.8, max_refine_passes=3, target_bc_inf_norm=1e-2)),
+        # short cycles and a loose tolerance: each pass stops at a boundary
+        # residual far above rounding, so the best-pass choice is reproducible
+        # (full 256-step cycles end every pass at rounding level, where the
+        # choice between passes is decided by rounding)
+        "sphere_refine3_v1": (sphere1, dict(initial_h=0.8, max_refine_passes=3, target_bc_inf_norm=1e-12,
+                                            gmres_restart=10, gmres_tol=1e-4)),
+        "torus_refine2_near": (torus, dict(initial_h=0.25, max_refine_passes=2, target_bc_inf_norm=1e-12,
+                                           use_near_quadrature_matvec=True, gmres_restart=10, gmres_tol=1e-4)),
+        "sphere_fallback": (sphere, dict(initial_h=0.8, max_refine_passes=1, gmres_tol=1e-30, gmres_restart=20,
+                                         gmres_maxiter=20)),
+    }
+    out = {}
+    for name, ((conds, charges), over) in cases.items():
+        cfg = BEMConfig()
+        cfg.fp64 = True
+        cfg.use_gpu = False
+        for k, v in over.items():
+            setattr(cfg, k, v)
+        t0 = time.time()
+        res = bem_solve(_spec(conds, charges), cfg, JsonlLogger(tempfile.mkdtemp()))
+        dt = time.time() - t0
+        if "error" in res:
+            out[f"{name}__error"] = np.array(str(res["error"]))
+            print(f"refine {name}: error {res['error']}")
+            continue
+        st = res["gmres_stats"]
+        ms = res["mesh_stats"]
+        hist = res["refinement_history"]
+        out[f"{name}__sigma"] = np.asarray(res["surface_charge_density"], dtype=np.float64)
+        out[f"{name}__passes"] = np.array([[p["pass"], p["h"], p["dof"], p["bc_resid_linf"], p["energy_A"],
+                                            p["gmres_info"].get("iters", -1), p["gmres_info"].get("code", -1)]
+                                           for p in hist], dtype=np.float64)
+        out[f"{name}__best"] = np.array([ms["n_panels"], ms["h_final"], ms["bc_residual_linf"],
+                                         res["solution"].meta.get("energy_A", np.nan), st.get("iters", -1),
+                                         float(bool(st.get("success", True))), float(st.get("resid", np.nan)), dt])
+        out[f"{name}__solver"] = np.array(str(st.get("solver", "gmres")))
+        out[f"{name}__boundary_samples"] = np.asarray(res["boundary_samples"], dtype=np.float64)
+        out[f"{name}__sample_points"] = np.asarray(res["sample_points"], dtype=np.float64)
+        print(f"refine {name}: passes {[(p['dof'], p['bc_resid_linf']) for p in hist]} -> {ms['n_panels']} "
+              f"solver {st.get('solver', 'gmres')} {dt:.1f}s")
+    np.savez_compressed(os.path.join(HERE, "refine_cases.npz"), **out)
+
+
 def save_icosphere_solve():
     """The sphere workload (5,120 icosphere panels, unit charge at (0,0,2),
     grounded, FP64, dense operator, GMRES(50) tol 1e-8) run through the
@@ -387,7 +451,8 @@ def save_efield_cases():
 
 
 def main():
-    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "ico", "targets", "efield", "nearpot"]
+    which = sys.argv[1:] or ["trees", "fmm", "gmres", "near", "solve", "refine", "ico", "targets", "efield",
+                             "nearpot"]
     if "nearpot" in which:
         save_nearpot_cases()
     if "efield" in which:
@@ -398,6 +463,8 @@ def main():
         save_near_cases()
     if "solve" in which:
         save_solve_cases()
+    if "refine" in which:
+        save_refine_cases()
     if "ico" in which:
         save_icosphere_solve()
     if "gmres" in which:

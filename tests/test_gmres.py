@@ -119,3 +119,27 @@ def test_device_gmres_early_exit(cuda_lib, graph):
     x = x.cpu().numpy()
     assert np.linalg.norm(A @ x - b) <= info["tol_abs"] * (1 + 1e-9)
     assert np.linalg.norm(x - x_ref) <= 1e-6 * np.linalg.norm(x_ref)
+
+
+def test_jacobi_fallback_converges_or_reports_failure():
+    """core.bem.jacobi_fallback_solve, the reference's damped-Jacobi last
+    resort (electrodrive/core/bem.py:1156-1251), on CPU tensors: a diagonally
+    dominant system converges to tol * max(|b|, 1); a system whose Jacobi
+    iteration diverges ends with a non-finite residual and success False."""
+    import torch
+
+    from electrodrive_gb300.core.bem import jacobi_fallback_solve
+
+    g = torch.Generator().manual_seed(0)
+    n = 60
+    M = torch.rand(n, n, generator=g, dtype=torch.float64) * 0.01
+    M += torch.diag(torch.full((n,), 2.0, dtype=torch.float64))
+    b = torch.rand(n, generator=g, dtype=torch.float64)
+    x, info = jacobi_fallback_solve(lambda v: M @ v, b, torch.diagonal(M).clone(), maxiter=256, tol=1e-10,
+                                    omega=0.8)
+    assert info["success"] and info["solver"] == "jacobi_fallback"
+    assert float(torch.linalg.norm(b - M @ x)) <= 1e-10 * max(float(torch.linalg.norm(b)), 1.0)
+    D = torch.ones(n, n, dtype=torch.float64) + torch.eye(n, dtype=torch.float64)
+    x, info = jacobi_fallback_solve(lambda v: D @ v, b, torch.diagonal(D).clone(), maxiter=2000, tol=1e-10,
+                                    omega=0.8)
+    assert not info["success"] and not np.isfinite(info["resid"])
