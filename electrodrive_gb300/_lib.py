@@ -31,6 +31,11 @@ EDFMM_NO_FARFIELD = 2
 EDFMM_NO_NEARFIELD = 4
 EDFMM_ARITH_NATIVE = 0
 EDFMM_ARITH_TWO_FLOAT = 1
+EDFMM_LAUNCH_M2L_TF_BLOCK = 1
+EDFMM_LAUNCH_NEAR_OVERLAP = 2
+EDFMM_MESH_SPHERE = 1
+EDFMM_MESH_TORUS = 2
+EDFMM_MESH_PLANE = 3
 EDFMM_TARGETS_M2L = 1
 EDFMM_TARGETS_L2L = 2
 EDFMM_TARGETS_L2P = 3
@@ -91,6 +96,8 @@ def _declare(L):
         "edfmm_plan_rebuild_lists": (i32, [_vp, dbl, _vp]),
         "edfmm_plan_set_order": (i32, [_vp, i32, _vp]),
         "edfmm_plan_set_arithmetic": (i32, [_vp, i32, _vp]),
+        "edfmm_plan_set_launch": (i32, [_vp, i32, i32]),
+        "edfmm_plan_get_launch": (i32, [_vp, i32, C.POINTER(i32)]),
         "edfmm_plan_set_instance_mask": (i32, [_vp, _vp, i32]),
         "edfmm_plan_get_info": (i32, [_vp, C.POINTER(PlanInfo)]),
         "edfmm_plan_export_tree": (i32, [_vp] * 11),
@@ -106,6 +113,8 @@ def _declare(L):
         "edfmm_plan_get_expansions": (i32, [_vp, _vp, _vp, _vp]),
         "edfmm_measure_fp32_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
         "edfmm_measure_fp64_peak": (i32, [i32, _vp, C.POINTER(C.c_double)]),
+        "edfmm_mesh_grid": (i32, [i32, C.POINTER(C.c_double), _vp, i64, _vp, i64, i64, C.c_int32, _vp, _vp, _vp, _vp]),
+        "edfmm_mesh_finish": (i32, [_vp, i64, _vp, _vp, i64, _vp, _vp, _vp, _vp, _vp, C.POINTER(i64), _vp]),
         "edfmm_pcn_num_params": (i64, []),
         "edfmm_pcn_workspace_bytes": (C.c_size_t, [i64]),
         "edfmm_pcn_features": (i32, [_vp, _vp, _vp, _vp, i64, _vp, _vp, C.c_size_t, _vp]),
@@ -336,6 +345,23 @@ class Plan:
             check(self._lib.edfmm_plan_set_arithmetic(self._h, code, stream_handle(self.device)),
                   "edfmm_plan_set_arithmetic")
         self.arithmetic = mode
+
+    _KNOBS = {"m2l_tf_block": EDFMM_LAUNCH_M2L_TF_BLOCK, "near_overlap": EDFMM_LAUNCH_NEAR_OVERLAP}
+
+    def set_launch(self, **knobs):
+        """Launch shapes: m2l_tf_block (128 or 256), near_overlap (0 or 1)."""
+        for k, v in knobs.items():
+            if k not in self._KNOBS:
+                raise ValueError(f"unknown launch knob {k!r}")
+            check(self._lib.edfmm_plan_set_launch(self._h, self._KNOBS[k], int(v)), "edfmm_plan_set_launch")
+
+    def get_launch(self) -> dict:
+        out = {}
+        for k, code in self._KNOBS.items():
+            v = C.c_int()
+            check(self._lib.edfmm_plan_get_launch(self._h, code, C.byref(v)), "edfmm_plan_get_launch")
+            out[k] = int(v.value)
+        return out
 
     def set_order(self, p: int):
         with torch.cuda.device(self.device):

@@ -38,10 +38,16 @@ from .bem_near import point_charge_potential, self_integrals
 from .operators import FmmOperator
 
 
+def _uv_sphere_shape(n_panels: int) -> Tuple[int, int]:
+    """(n_theta, n_phi) of the tensor-grid sphere with about n_panels panels (n_phi = 2 n_theta)."""
+    nt = max(4, int(round(1.0 + math.sqrt(1.0 + n_panels / 4.0))))
+    return nt, 2 * nt
+
+
 def _uv_sphere(center, radius: float, n_panels: int, cid: int) -> TriMesh:
     """The reference's tensor-grid sphere with about n_panels panels (n_phi = 2 n_theta)."""
-    nt = max(4, int(round(1.0 + math.sqrt(1.0 + n_panels / 4.0))))
-    v, t = _mesh_sphere(np.asarray(center, float), float(radius), nt, 2 * nt)
+    nt, nph = _uv_sphere_shape(n_panels)
+    v, t = _mesh_sphere(np.asarray(center, float), float(radius), nt, nph)
     return _finish(v, t, np.full(t.shape[0], cid, np.int32))
 
 
@@ -51,7 +57,9 @@ def _join(a: TriMesh, b: TriMesh) -> TriMesh:
     return _finish(v, t, np.concatenate([a.conductor_ids, b.conductor_ids]))
 
 
-def dimer_case(seed: int, n_panels: Optional[int] = None) -> Tuple[TriMesh, Dict[str, Any]]:
+def _dimer_recipe(seed: int, n_panels: Optional[int]):
+    """The random draws of one dimer instance: the two spheres (center,
+    radius, panels) and the conductor spec with its point charge."""
     rng = np.random.default_rng(seed)
     if n_panels is None:
         n_panels = int(rng.integers(2000, 40001))
@@ -61,7 +69,6 @@ def dimer_case(seed: int, n_panels: Optional[int] = None) -> Tuple[TriMesh, Dict
     u /= np.linalg.norm(u)
     c1, c2 = -u * (r1 + gap / 2), u * (r2 + gap / 2)
     n1 = int(round(n_panels * r1 * r1 / (r1 * r1 + r2 * r2)))
-    mesh = _join(_uv_sphere(c1, r1, n1, 0), _uv_sphere(c2, r2, n_panels - n1, 1))
     near, rn, far, rf = (c1, r1, c2, r2) if rng.random() < 0.5 else (c2, r2, c1, r1)
     d = rng.uniform(0.3, 2.0)
     for _ in range(100):
@@ -72,7 +79,22 @@ def dimer_case(seed: int, n_panels: Optional[int] = None) -> Tuple[TriMesh, Dict
             break
     spec = dict(conductors=[dict(type="sphere", potential=0.0, id=0), dict(type="sphere", potential=0.0, id=1)],
                 charges=[dict(type="point", q=float(rng.uniform(-1, 1)), pos=pos.tolist())])
-    return mesh, spec
+    return (c1, float(r1), n1), (c2, float(r2), n_panels - n1), spec
+
+
+def dimer_case(seed: int, n_panels: Optional[int] = None) -> Tuple[TriMesh, Dict[str, Any]]:
+    (c1, r1, n1), (c2, r2, n2), spec = _dimer_recipe(seed, n_panels)
+    return _join(_uv_sphere(c1, r1, n1, 0), _uv_sphere(c2, r2, n2, 1)), spec
+
+
+def dimer_case_device(seed: int, n_panels: Optional[int] = None, device=None):
+    """dimer_case with the mesh generated on the GPU (bit-identical arrays)."""
+    from .mesh_device import mesh_grids
+
+    (c1, r1, n1), (c2, r2, n2), spec = _dimer_recipe(seed, n_panels)
+    grids = [("sphere", (np.asarray(c1, float), r1) + _uv_sphere_shape(n1), 0),
+             ("sphere", (np.asarray(c2, float), r2) + _uv_sphere_shape(n2), 1)]
+    return mesh_grids(grids, device), spec
 
 
 class BatchSystem:
@@ -181,44 +203,82 @@ class BatchSystem:
         return segment_norms(r, self.offsets) / segment_norms(self.b, self.offsets).clamp_min(1e-300)
 
 
+def _time_op(op, x: Tensor, reps: int) -> Tuple[float, Tensor]:
+    dev = x.device
+    stream = torch.cuda.current_stream(dev)
+    op(x)
+    times = []
+    y = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        y = op(x)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1))
+    return statistics.median(times), y
+
+
 def autotune_inner(system: BatchSystem, leaf_sizes=(32, 64, 128), orders=(6, 7, 8), max_rel_error: float = 3e-7,
-                   reps: int = 3) -> Dict[str, Any]:
-    """Pick the FP32 inner operator (leaf size, expansion order) with the
+                   reps: int = 3, use_cache: bool = True) -> Dict[str, Any]:
+    """Pick the FP32 inner operator (leaf size, expansion order and launch
+    shape: near field beside the far field or fused after it) with the
     shortest matvec whose output is within ``max_rel_error`` of the FP64
     operator's on a fixed random density; installs it as system.op32.  The
     bound matches the inner tolerance floor of the batched solve (3e-7), so
-    that one refinement step can reach 1e-6."""
+    that one refinement step can reach 1e-6.  The choice is kept in the
+    autotune cache (electrodrive_gb300.fmm3d.autotune) under this machine,
+    the panel-count bucket and the batch's signature; a cached choice is
+    rebuilt and its accuracy checked once instead of searching again."""
+    from ..fmm3d import autotune as at
+
     dev = system.device
     g = torch.Generator(device="cpu").manual_seed(0)
     probe = torch.rand(system.n, generator=g, dtype=torch.float64).to(dev)
     ref = system.op64(probe).to(torch.float64).clone()
-    stream = torch.cuda.current_stream(dev)
+    x = probe.float()
+    fingerprint = at.hardware_fingerprint(dev)
+    bucket = at.bucket_problem_size(system.n)
+    signature = f"batch:{len(system.offsets) - 1}:{system.n}"
+    if use_cache:
+        rec = at.load_best(fingerprint, bucket, max_rel_error, kind="inner_fp32", signature=signature)
+        if rec is not None:
+            c = rec["config"]
+            op = system.make_operator(torch.float32, int(c["leaf_size"]), int(c["expansion_order"]))
+            at.apply_launch(op.plan, rec.get("launch", {}))
+            t, y = _time_op(op, x, reps)
+            err = float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
+            if err <= max_rel_error:
+                system.op32 = op
+                return dict(leaf_size=int(c["leaf_size"]), expansion_order=int(c["expansion_order"]), ms=t,
+                            launch=dict(rec.get("launch", {})), trials=[], from_cache=True)
     trials = []
     best = None
     for leaf in leaf_sizes:
         for p in orders:
             op = system.make_operator(torch.float32, leaf, p)
-            x = probe.float()
-            op(x)
-            times = []
-            for _ in range(reps):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                y = op(x)
-                e1.record(stream)
-                torch.cuda.synchronize(dev)
-                times.append(e0.elapsed_time(e1))
-            err = float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
-            t = statistics.median(times)
-            trials.append(dict(leaf_size=leaf, expansion_order=p, ms=t, rel_error=err))
-            if err <= max_rel_error and (best is None or t < best[0]):
-                best = (t, leaf, p, op)
-            else:
+            for launch in at.LAUNCH_CHOICES:
+                op.plan.set_launch(**launch)
+                t, y = _time_op(op, x, reps)
+                err = float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
+                trials.append(dict(leaf_size=leaf, expansion_order=p, launch=dict(launch), ms=t, rel_error=err))
+                if err <= max_rel_error and (best is None or t < best[0]):
+                    best = (t, leaf, p, op, dict(launch))
+            if best is None or best[3] is not op:
                 del op
     if best is None:
         raise RuntimeError("no inner operator met the accuracy bound")
-    system.op32 = best[3]
-    return dict(leaf_size=best[1], expansion_order=best[2], ms=best[0], trials=trials)
+    t, leaf, p, op, launch = best
+    at.apply_launch(op.plan, launch)
+    system.op32 = op
+    if use_cache:
+        at.append_record({"fingerprint": fingerprint, "problem_size_bucket": bucket, "kind": "inner_fp32",
+                          "signature": signature, "config": {"leaf_size": leaf, "expansion_order": p,
+                                                             "precision": "single"},
+                          "launch": launch, "metrics": {"wall_time_s": t * 1e-3, "rel_l2_error": min(
+                              tr["rel_error"] for tr in trials if tr["leaf_size"] == leaf and
+                              tr["expansion_order"] == p)}})
+    return dict(leaf_size=leaf, expansion_order=p, ms=t, launch=launch, trials=trials, from_cache=False)
 
 
 def plain_fp64_solve(mesh: TriMesh, spec: Dict[str, Any], *, rtol: float = 1e-6, restart: int = 256,
@@ -246,4 +306,4 @@ def plain_fp64_solve(mesh: TriMesh, spec: Dict[str, Any], *, rtol: float = 1e-6,
     return dict(seconds=dt, iters=info["iters"], code=info["code"], rel_resid=rel, n=mesh.n_panels)
 
 
-__all__ = ["BatchSystem", "autotune_inner", "dimer_case", "plain_fp64_solve"]
+__all__ = ["BatchSystem", "autotune_inner", "dimer_case", "dimer_case_device", "plain_fp64_solve"]

@@ -511,47 +511,84 @@ def assemble_system(mesh: TriMesh, spec: Any, *, kind: str = "dense", dtypes=(to
 
 def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: Tensor, near=None, *,
                             orders=(8, 7, 6), leaf_sizes=(64,), max_rel_error: float = 3e-7, reps: int = 5,
-                            device=None) -> Tuple[Any, List[Dict[str, Any]]]:
+                            device=None, use_cache: bool = True,
+                            signature: Optional[str] = None) -> Tuple[Any, List[Dict[str, Any]]]:
     """The FP32 FMM operator for the inner solves of iterative refinement:
-    among expansion orders and leaf sizes, the fastest whose output on a
-    fixed random density is within ``max_rel_error`` of ``op64``'s (the FP32
+    among expansion orders, leaf sizes and launch shapes (near field beside
+    the far field or fused after it), the fastest whose output on a fixed
+    random density is within ``max_rel_error`` of ``op64``'s (the FP32
     operator at p = 8 is about 2e-7 away; looser operators make the first
     refinement step fall short of 1e-6).  ``near`` is the FP32 near
-    correction the operator adds.  Returns (operator, trials)."""
+    correction the operator adds.  The choice is kept in the autotune cache
+    (electrodrive_gb300.fmm3d.autotune) under this machine, the panel-count
+    bucket and ``signature`` (default: the panel count); a cached choice is
+    rebuilt and checked once instead of searching again.  Returns
+    (operator, trials)."""
+    from ..fmm3d import autotune as at
+
     dev = torch.device(device) if device is not None else op64.device if hasattr(op64, "device") else \
         torch.device("cuda", torch.cuda.current_device())
     g = torch.Generator(device="cpu").manual_seed(0)
     probe = torch.rand(int(areas.shape[0]), generator=g, dtype=torch.float64).to(dev)
     ref = op64(probe).to(torch.float64).clone()
     stream = torch.cuda.current_stream(dev)
-    trials, best = [], None
     base64 = getattr(op64, "base", op64)
     leaf64 = int(base64.plan.info.leaf_size) if isinstance(base64, FmmOperator) else None
+
+    def make(leaf, p):
+        op = (converted_operator(op64, areas, self_corr, dtype=torch.float32, expansion_order=p, near=near)
+              if leaf == leaf64 else None)
+        if op is None:
+            op = build_operator(centroids, areas, self_corr.to(torch.float32), dtype=torch.float32, kind="fmm",
+                                near=near, leaf_size=leaf, expansion_order=p, device=dev)
+        return op
+
+    def timed(op):
+        x = probe.float()
+        op(x)
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            y = op(x)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1))
+        return sorted(times)[len(times) // 2], float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
+
+    n = int(areas.shape[0])
+    fingerprint = at.hardware_fingerprint(dev)
+    bucket = at.bucket_problem_size(n)
+    sig = signature or f"single:{n}"
+    if use_cache:
+        rec = at.load_best(fingerprint, bucket, max_rel_error, kind="inner_fp32", signature=sig)
+        if rec is not None:
+            c = rec["config"]
+            op = make(int(c["leaf_size"]), int(c["expansion_order"]))
+            at.apply_launch(op.base.plan, rec.get("launch", {}))
+            t, err = timed(op)
+            if err <= max_rel_error:
+                return op, [dict(leaf_size=int(c["leaf_size"]), expansion_order=int(c["expansion_order"]),
+                                 launch=dict(rec.get("launch", {})), ms=t, rel_error=err, from_cache=True)]
+    trials, best = [], None
     for leaf in leaf_sizes:
         for p in orders:
-            op = (converted_operator(op64, areas, self_corr, dtype=torch.float32, expansion_order=p, near=near)
-                  if leaf == leaf64 else None)
-            if op is None:
-                op = build_operator(centroids, areas, self_corr.to(torch.float32), dtype=torch.float32, kind="fmm",
-                                    near=near, leaf_size=leaf, expansion_order=p, device=dev)
-            x = probe.float()
-            op(x)
-            times = []
-            for _ in range(reps):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                y = op(x)
-                e1.record(stream)
-                torch.cuda.synchronize(dev)
-                times.append(e0.elapsed_time(e1))
-            err = float(torch.linalg.norm(y.double() - ref) / torch.linalg.norm(ref))
-            t = sorted(times)[len(times) // 2]
-            trials.append(dict(leaf_size=leaf, expansion_order=p, ms=t, rel_error=err))
-            if err <= max_rel_error and (best is None or t < best[0]):
-                best = (t, op)
+            op = make(leaf, p)
+            for launch in at.LAUNCH_CHOICES:
+                op.base.plan.set_launch(**launch)
+                t, err = timed(op)
+                trials.append(dict(leaf_size=leaf, expansion_order=p, launch=dict(launch), ms=t, rel_error=err))
+                if err <= max_rel_error and (best is None or t < best[0]):
+                    best = (t, op, leaf, p, dict(launch), err)
     if best is None:
         raise RuntimeError("no inner operator met the accuracy bound")
-    return best[1], trials
+    t, op, leaf, p, launch, err = best
+    at.apply_launch(op.base.plan, launch)
+    if use_cache:
+        at.append_record({"fingerprint": fingerprint, "problem_size_bucket": bucket, "kind": "inner_fp32",
+                          "signature": sig, "config": {"leaf_size": leaf, "expansion_order": p, "precision": "single"},
+                          "launch": launch, "metrics": {"wall_time_s": t * 1e-3, "rel_l2_error": err}})
+    return op, trials
 
 
 def segment_norms(v: Tensor, offsets: Optional[List[int]]) -> Tensor:

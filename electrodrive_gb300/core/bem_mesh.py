@@ -130,14 +130,14 @@ def _cget(c: Any, key: str, default=None):
     return c.get(key, default) if isinstance(c, dict) else getattr(c, key, default)
 
 
-def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None) -> TriMesh:
-    """Mesh every conductor of ``spec`` (same rules as bem_mesh.py:27-136)."""
+def conductor_grids(spec: Any, target_h: float = 0.1) -> List[Tuple[str, tuple, int]]:
+    """The tensor grid of every conductor of ``spec`` at ``target_h``, as
+    (kind, generator arguments, conductor id) with the sizing rules of
+    bem_mesh.py:27-136; kind is "plane" (z, L, n), "sphere" (center, radius,
+    n_theta, n_phi) or "torus" (center, R, a, n_u, n_v)."""
     conductors = list(_cget(spec, "conductors", []) or [])
     charges = list(_cget(spec, "charges", []) or [])
-    V_list: List[np.ndarray] = []
-    T_list: List[np.ndarray] = []
-    C_list: List[np.ndarray] = []
-    offset = 0
+    out: List[Tuple[str, tuple, int]] = []
     for idx, c in enumerate(conductors):
         typ = _cget(c, "type")
         cid = int(_cget(c, "id", idx))
@@ -149,7 +149,7 @@ def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None
                     dmin = max(dmin, abs(float(_cget(ch, "pos")[2] - z)))
             scale = float(os.getenv("EDE_BEM_PLANE_PATCH_SCALE", "1.0"))
             L = scale * max(8.0, 16.0 * dmin)
-            v, t = _mesh_plane_patch(z, L, max(8, int(L / max(1e-3, target_h))))
+            out.append(("plane", (z, L, max(8, int(L / max(1e-3, target_h)))), cid))
         elif typ == "sphere":
             center = np.asarray(_cget(c, "center", [0.0, 0.0, 0.0]), float)
             radius = float(_cget(c, "radius", 1.0))
@@ -157,7 +157,7 @@ def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None
             ds = max(1.0, float(os.getenv("EDE_BEM_SPHERE_DENSITY_SCALE", "1.5")))
             n_theta = max(10, int(np.ceil(ds * np.pi * radius / base)))
             n_phi = max(20, int(np.ceil(ds * 2.0 * np.pi * radius / base)))
-            v, t = _mesh_sphere(center, radius, n_theta, n_phi)
+            out.append(("sphere", (center, radius, n_theta, n_phi), cid))
         elif typ in ("torus", "toroid"):
             center = np.asarray(_cget(c, "center", [0.0, 0.0, 0.0]), float)
             R = float(_cget(c, "major_radius", _cget(c, "radius", 1.0)))
@@ -165,10 +165,24 @@ def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None
             base = max(1e-3, target_h)
             ms = float(os.getenv("EDE_BEM_TORUS_MAJOR_SCALE", "1.0"))
             ns = float(os.getenv("EDE_BEM_TORUS_MINOR_SCALE", "1.0"))
-            v, t = _mesh_torus(center, R, a, max(24, int(np.ceil(ms * 2.0 * np.pi * R / base))),
-                               max(16, int(np.ceil(ns * 2.0 * np.pi * a / base))))
+            out.append(("torus", (center, R, a, max(24, int(np.ceil(ms * 2.0 * np.pi * R / base))),
+                                  max(16, int(np.ceil(ns * 2.0 * np.pi * a / base)))), cid))
         else:
             raise NotImplementedError(f"Unsupported conductor type: {typ}")
+    return out
+
+
+_GENERATORS = {"plane": _mesh_plane_patch, "sphere": _mesh_sphere, "torus": _mesh_torus}
+
+
+def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None) -> TriMesh:
+    """Mesh every conductor of ``spec`` (same rules as bem_mesh.py:27-136)."""
+    V_list: List[np.ndarray] = []
+    T_list: List[np.ndarray] = []
+    C_list: List[np.ndarray] = []
+    offset = 0
+    for kind, args, cid in conductor_grids(spec, target_h):
+        v, t = _GENERATORS[kind](*args)
         V_list.append(v)
         T_list.append(t + offset)
         C_list.append(np.full(t.shape[0], cid, np.int32))
@@ -179,4 +193,4 @@ def generate_mesh(spec: Any, target_h: float = 0.1, logger: Optional[Any] = None
     return _finish(np.vstack(V_list), np.vstack(T_list), np.concatenate(C_list))
 
 
-__all__ = ["TriMesh", "generate_mesh", "icosphere", "torus_mesh"]
+__all__ = ["TriMesh", "conductor_grids", "generate_mesh", "icosphere", "torus_mesh"]

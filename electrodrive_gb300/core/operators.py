@@ -71,8 +71,9 @@ class FmmOperator:
 
     def graph_state(self) -> tuple:
         """What a captured graph of this operator depends on besides its
-        buffers: the plan's arithmetic (two-float mode launches other kernels)."""
-        return (getattr(self.plan, "arithmetic", "native"),)
+        buffers: the plan's arithmetic (two-float mode launches other kernels)
+        and its launch shapes."""
+        return (getattr(self.plan, "arithmetic", "native"), tuple(sorted(self.plan.get_launch().items())))
 
     def set_active_mask(self, flags: Optional[Tensor], stride: int = 1) -> bool:
         """Batched plans: later applications skip the far-field rows and

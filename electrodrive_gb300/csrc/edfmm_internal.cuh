@@ -207,8 +207,10 @@ struct DevTree {
     std::vector<int32_t> level_offsets;  // host: level l nodes = level_nodes[off[l], off[l+1])
     DevBuf level_nodes;                  // int32 node ids grouped by level
     // FP64 trees in two-float mode: per point (x, y, z, charge) split into
-    // FP32 (hi, lo) pairs, 8 floats, refreshed with the charges
+    // FP32 (hi, lo) pairs, 8 floats, refreshed with the charges; per node
+    // (cx, cy, cz, expansion scale a) split the same way
     DevBuf pts_tf;
+    DevBuf nodes_tf;
     // batched plans: instance k owns nodes inst_node_off[k] .. inst_node_off[k+1]-1
     int n_inst = 0;
     DevBuf inst_node_off;  // int32 x (n_inst + 1)
@@ -283,8 +285,13 @@ struct FmmBuffers {
     ExtremeRows extreme, extreme_swapped;
     InstMask mask;  // set around the steps of a batched solve
     // FP64 plans: EDFMM_ARITH_TWO_FLOAT runs M2L and the near field in
-    // two-float arithmetic on the FP32 pipe (twofloat.cuh)
+    // two-float arithmetic on the FP32 pipe (twofloat.cuh); mult_tf holds
+    // the multipoles split into (hi, lo) pairs for the two-float M2L
     int arith = EDFMM_ARITH_NATIVE;
+    DevBuf mult_tf;
+    // launch shapes the autotuner may change (edfmm_plan_set_launch)
+    int m2l_tf_block = 128;  // two-float M2L threads per block (128 or 256, p = 8)
+    int near_overlap = 1;    // full matvec: near field on a second stream beside the far field
 };
 
 int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaStream_t s);
@@ -296,15 +303,21 @@ int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s);
 // the same in two-float arithmetic for FP64 plans, orders 6..8
-// (EDFMM_ERR_UNSUPPORTED for other orders, launching nothing)
-int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
-                      const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
-                      cudaStream_t s);
+// (EDFMM_ERR_UNSUPPORTED for other orders, launching nothing): node geometry
+// and multipoles split into (hi, lo) FP32 pairs (tnodes / snodes: 2 float4
+// per node; Mx: one float4 per complex coefficient), locals written as FP64
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+                      const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+                      int block, cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
                 FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 // the same-tree extreme-pair rows of buf (built once; synchronises s)
 int prepare_extreme_rows(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, cudaStream_t s);
+// two-float mode of an FP64 plan: split node geometry and the multipole
+// buffer (sized for the current order); called when the mode is set and
+// when the order changes
+int prepare_two_float(DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 
 struct NearArgs {
     const void *sigma = nullptr;      // original order (nullable)

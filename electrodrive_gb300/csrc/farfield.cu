@@ -53,6 +53,26 @@ __global__ void k_set_charges(typename Vec4<T>::type *pts, const int32_t *__rest
     pts[i].w = b ? a[o] * b[o] : a[o];
 }
 
+// two-float mode: node geometry (cx, cy, cz, a) and FP64 complex
+// coefficients split into (hi, lo) FP32 pairs
+__global__ void k_split_nodes(const double4 *__restrict__ center, const double4 *__restrict__ half, int64_t n,
+                              float4 *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4 c = center[i];
+    const tf32x2 x = tf_from_double(c.x), y = tf_from_double(c.y), z = tf_from_double(c.z),
+                 a = tf_from_double(half[i].w);
+    out[2 * i] = make_float4(x.hi, x.lo, y.hi, y.lo);
+    out[2 * i + 1] = make_float4(z.hi, z.lo, a.hi, a.lo);
+}
+__global__ void k_split_coeffs(const double2 *__restrict__ in, int64_t n, float4 *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 c = in[i];
+    const tf32x2 re = tf_from_double(c.x), im = tf_from_double(c.y);
+    out[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+
 // FP64 trees in two-float mode: the charges as above (a == NULL keeps them)
 // and every point split into (hi, lo) FP32 pairs, 8 floats per point
 __global__ void k_set_charges_split(double4 *pts, float4 *pts_tf, const int32_t *__restrict__ idx, int64_t n,
@@ -921,9 +941,14 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
     // FP64 plans in two-float mode: the rotation kernel on the FP32 pipe
     // (orders 6..8), which leaves extreme pairs like the FP32 kernel does
     bool two_float = false;
-    if (sizeof(T) == 8 && buf.arith == EDFMM_ARITH_TWO_FLOAT) {
-        int rc = launch_m2l_rot_tf(buf.p, M, off, src, tree.center.p, tree.half.p, stree.center.p, stree.half.p,
-                                   sbuf.multipoles.p, buf.locals.p, buf.nc_pad, buf.mask, s);
+    if (sizeof(T) == 8 && buf.arith == EDFMM_ARITH_TWO_FLOAT && buf.p >= 6 && buf.p <= 8 && tree.nodes_tf.p &&
+        stree.nodes_tf.p && sbuf.mult_tf.p) {
+        // the source multipoles split once per node, then the pairs
+        const int64_t nq = stree.n_nodes * (int64_t)sbuf.nc_pad;
+        k_split_coeffs<<<nblk(nq, 256), 256, 0, s>>>(dptr<double2>(sbuf.multipoles), nq, dptr<float4>(sbuf.mult_tf));
+        EDFMM_LAUNCH_CHECK("k_split_coeffs");
+        int rc = launch_m2l_rot_tf(buf.p, M, off, src, tree.nodes_tf.p, tree.half.p, stree.nodes_tf.p, stree.half.p,
+                                   sbuf.mult_tf.p, buf.locals.p, buf.nc_pad, buf.mask, buf.m2l_tf_block, s);
         if (rc == EDFMM_OK) two_float = true;
         else if (rc != EDFMM_ERR_UNSUPPORTED) return rc;
     }
@@ -989,6 +1014,20 @@ int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists
     return tgt_tree.dtype == EDFMM_F64 ? m2l_impl<double>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s)
                                        : m2l_impl<float>(tgt_tree, src_tree, lists, src_buf, tgt_buf, false, s);
 }
+int prepare_two_float(DevTree &tree, FmmBuffers &buf, cudaStream_t s) {
+    if (tree.dtype != EDFMM_F64) return EDFMM_OK;
+    const int64_t M = std::max<int64_t>(tree.n_nodes, 1);
+    int rc;
+    if ((rc = tree.nodes_tf.reserve(sizeof(float4) * 2 * (size_t)M))) return rc;
+    if ((rc = buf.mult_tf.reserve(sizeof(float4) * (size_t)buf.nc_pad * (size_t)M))) return rc;
+    if (tree.n_nodes > 0) {
+        k_split_nodes<<<nblk(tree.n_nodes, 256), 256, 0, s>>>(dptr<double4>(tree.center), dptr<double4>(tree.half),
+                                                              tree.n_nodes, dptr<float4>(tree.nodes_tf));
+        EDFMM_LAUNCH_CHECK("k_split_nodes");
+    }
+    return EDFMM_OK;
+}
+
 int prepare_extreme_rows(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, cudaStream_t s) {
     if (buf.extreme.built || tree.n_nodes == 0) return EDFMM_OK;
     const int32_t *off = dptr<int32_t>(lists.m2l_off), *src = dptr<int32_t>(lists.m2l_src);

@@ -388,9 +388,11 @@ __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? 3 : 1)
 
 // ---------------------------------------------------------------------------
 // Two-float M2L for FP64 plans.  The same rotation algorithm on the FP32 pipe
-// in two-float arithmetic (about 48 significant bits; twofloat.cuh): the
-// multipoles are read as FP64 and split, the pair geometry is formed in FP64
-// and split, and the locals are written back as FP64.  Each lane's
+// in two-float arithmetic (about 48 significant bits; twofloat.cuh).  The
+// source multipoles and the node geometry arrive already split into (hi, lo)
+// FP32 pairs (split once per node, not once per pair: a pair-time split
+// costs hundreds of FP64-pipe conversions), the pair geometry is formed in
+// two-float, and the locals are written back as FP64.  Each lane's
 // translated locals go back into its own coefficient slots (81 two-float
 // values at p = 8), and after every round of 32 pairs the warp adds the
 // slots of its lanes, lane i owning coefficients i, i + 32, i + 64 in
@@ -414,21 +416,22 @@ __device__ __forceinline__ void backward_tf(V &v, const Frame<tf32x2, P> &F) {
     if constexpr (n < P) backward_tf<P, n + 1>(v, F);
 }
 
-// One pair: v <- the translated locals (real block basis) of source row Mrow.
+// One pair: v <- the translated locals (real block basis) of source row Mrow
+// (split multipoles: (re hi, re lo, im hi, im lo) per coefficient).
 template <int P, typename V>
-__device__ __forceinline__ void rot_pair_tf(V &v, const double2 *__restrict__ Mrow, tf32x2 c, tf32x2 dx, tf32x2 dy,
+__device__ __forceinline__ void rot_pair_tf(V &v, const float4 *__restrict__ Mrow, tf32x2 c, tf32x2 dx, tf32x2 dy,
                                             tf32x2 dz) {
     using T = tf32x2;
 #pragma unroll
     for (int n = 0; n <= P; ++n) {
 #pragma unroll
         for (int m = 0; m <= n; ++m) {
-            const double2 x = Mrow[tri(n, m)];
+            const float4 x = Mrow[tri(n, m)];
             if (m == 0) {
-                v.set(n * n, tf_from_double(x.x));
+                v.set(n * n, T(x.x, x.y));
             } else {
-                v.set(n * n + 2 * m - 1, tf_from_double(x.x));
-                v.set(n * n + 2 * m, tf_from_double(x.y));
+                v.set(n * n + 2 * m - 1, T(x.x, x.y));
+                v.set(n * n + 2 * m, T(x.z, x.w));
             }
         }
     }
@@ -453,14 +456,17 @@ __device__ __forceinline__ void rot_pair_tf(V &v, const double2 *__restrict__ Mr
     backward_tf<P, 0>(v, F);
 }
 
-template <int P>
-__global__ void __launch_bounds__(kRotThreads, 2)
+// tnodes / snodes: per node (cx hi, cx lo, cy hi, cy lo), (cz hi, cz lo, a hi, a lo).
+// NT = 128 (two blocks per SM) or 256 (one block of 8 warps per SM: one
+// instruction-fetch stream per SM for the long pair code).
+template <int P, int NT>
+__global__ void __launch_bounds__(NT, 256 / NT)
     k_m2l_rot_tf(int64_t n_nodes, const int32_t *__restrict__ off, const int32_t *__restrict__ src,
-                 const double4 *__restrict__ tcenter, const double4 *__restrict__ thalf,
-                 const double4 *__restrict__ center, const double4 *__restrict__ half,
-                 const double2 *__restrict__ Mexp, double2 *__restrict__ Lexp, int nc_pad, const InstMask mask) {
+                 const float4 *__restrict__ tnodes, const double4 *__restrict__ thalf,
+                 const float4 *__restrict__ snodes, const double4 *__restrict__ half,
+                 const float4 *__restrict__ Mexp, double2 *__restrict__ Lexp, int nc_pad, const InstMask mask) {
     using T = tf32x2;
-    constexpr int NV = (P + 1) * (P + 1), NT = kRotThreads, NR = (NV + 31) / 32;
+    constexpr int NV = (P + 1) * (P + 1), NR = (NV + 31) / 32;
     extern __shared__ __align__(16) unsigned char rot_smem[];
     __shared__ int max_rounds;
     T *slots = reinterpret_cast<T *>(rot_smem);  // slot i of thread u at slots[i * NT + u]
@@ -469,11 +475,15 @@ __global__ void __launch_bounds__(kRotThreads, 2)
     const int lane = threadIdx.x & 31;
     const int wbase = threadIdx.x & ~31;
     const bool live = t < n_nodes && inst_active(mask, (int)t);
-    double4 ct{};
-    double iaL = 1.0;
+    T ctx = T(0), cty = T(0), ctz = T(0), iaT = T(1);
+    double iaL = 1.0;  // FP64, for the extreme-pair test (the same test as the pair lists of the FP64 kernel)
     int b = 0, e = 0;
     if (live) {
-        ct = tcenter[t];
+        const float4 u = tnodes[2 * t], w = tnodes[2 * t + 1];
+        ctx = T(u.x, u.y);
+        cty = T(u.z, u.w);
+        ctz = T(w.x, w.y);
+        iaT = tf_recip(T(w.z, w.w));
         iaL = 1.0 / thalf[t].w;
         b = off[t];
         e = off[t + 1];
@@ -487,16 +497,18 @@ __global__ void __launch_bounds__(kRotThreads, 2)
     __syncthreads();
     const int rounds = max_rounds;
     for (int r = 0; r < rounds; ++r) {
+        // the block's warps walk the (long, straight-line) pair code together
+        // and share its instruction fetches; every thread runs `rounds` rounds
+        __syncthreads();
         const int k = b + r * 32 + lane;
         bool have = false;
         if (k < e) {
             const int s = __ldg(src + k);
-            const double4 cs = center[s];
-            const double c = half[s].w * iaL;
-            if (!(c > (double)kRotExtremeRatio)) {
+            if (!(half[s].w * iaL > (double)kRotExtremeRatio)) {
                 have = true;
-                rot_pair_tf<P>(v, Mexp + (int64_t)s * nc_pad, tf_from_double(c), tf_from_double((ct.x - cs.x) * iaL),
-                               tf_from_double((ct.y - cs.y) * iaL), tf_from_double((ct.z - cs.z) * iaL));
+                const float4 u = snodes[2 * s], w = snodes[2 * s + 1];
+                rot_pair_tf<P>(v, Mexp + (int64_t)s * nc_pad, T(w.z, w.w) * iaT, (ctx - T(u.x, u.y)) * iaT,
+                               (cty - T(u.z, u.w)) * iaT, (ctz - T(w.x, w.y)) * iaT);
             }
         }
         if (!have) {
@@ -528,7 +540,7 @@ __global__ void __launch_bounds__(kRotThreads, 2)
             int n = 0;
             while ((n + 1) * (n + 1) <= i) ++n;
             const int q = i - n * n;  // 0: Re X0; 2m - 1: Re Xm; 2m: Im Xm
-            const double val = tf_to_double(acc[j]) * iaL;
+            const double val = tf_to_double(acc[j] * iaT);
             if (q == 0) {
                 out[2 * tri(n, 0)] = val;
                 out[2 * tri(n, 0) + 1] = 0.0;
@@ -541,19 +553,19 @@ __global__ void __launch_bounds__(kRotThreads, 2)
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <int P>
-int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
-                  const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+template <int P, int NT>
+int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+                  const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                   cudaStream_t s) {
-    constexpr int NV = (P + 1) * (P + 1), NT = kRotThreads;
+    constexpr int NV = (P + 1) * (P + 1);
     constexpr size_t smem = (size_t)NV * NT * sizeof(tf32x2);
     static const cudaError_t attr =
-        cudaFuncSetAttribute(k_m2l_rot_tf<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_m2l_rot_tf<P, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr != cudaSuccess)
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot_tf shared memory attribute: ") + cudaGetErrorString(attr));
-    k_m2l_rot_tf<P><<<nblk(M * 32, NT), NT, smem, s>>>(
-        M, off, src, static_cast<const double4 *>(tcen), static_cast<const double4 *>(thal),
-        static_cast<const double4 *>(cen), static_cast<const double4 *>(hal), static_cast<const double2 *>(Mx),
+    k_m2l_rot_tf<P, NT><<<nblk(M * 32, NT), NT, smem, s>>>(
+        M, off, src, static_cast<const float4 *>(tnodes), static_cast<const double4 *>(thal),
+        static_cast<const float4 *>(snodes), static_cast<const double4 *>(hal), static_cast<const float4 *>(Mx),
         static_cast<double2 *>(Lx), nc_pad, mask);
     EDFMM_LAUNCH_CHECK("k_m2l_rot_tf");
     return EDFMM_OK;
@@ -609,14 +621,16 @@ int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_
 
 // Two-float M2L of an FP64 plan (orders 6..8); returns EDFMM_ERR_UNSUPPORTED
 // for other orders (the caller then runs the FP64 kernel).
-int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal,
-                      const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
-                      cudaStream_t s) {
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+                      const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
+                      int block, cudaStream_t s) {
     if (M <= 0) return EDFMM_OK;
+    if (p == 8 && block == 256)
+        return launch_rot_tf<8, 256>(M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
     switch (p) {
-        case 6: return launch_rot_tf<6>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
-        case 7: return launch_rot_tf<7>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
-        case 8: return launch_rot_tf<8>(M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
+        case 6: return launch_rot_tf<6, 128>(M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
+        case 7: return launch_rot_tf<7, 128>(M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
+        case 8: return launch_rot_tf<8, 128>(M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
         default: return EDFMM_ERR_UNSUPPORTED;
     }
 }

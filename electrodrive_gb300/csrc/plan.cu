@@ -405,6 +405,8 @@ int edfmm_plan_set_arithmetic(edfmm_plan *p, int mode, void *stream) {
     cudaStream_t s = S(stream);
     if (mode == EDFMM_ARITH_NATIVE) {
         p->tree.pts_tf.release();
+        p->tree.nodes_tf.release();
+        p->fmm.mult_tf.release();
         p->fmm.arith = EDFMM_ARITH_NATIVE;
         return EDFMM_OK;
     }
@@ -413,11 +415,38 @@ int edfmm_plan_set_arithmetic(edfmm_plan *p, int mode, void *stream) {
         if (int rc = p->tree.pts_tf.reserve(sizeof(float) * 8 * (size_t)p->tree.n_points)) return rc;
         if (int rc = set_charges(p->tree, nullptr, nullptr, s)) return rc;  // splits the points and charges
     }
+    if (int rc = prepare_two_float(p->tree, p->fmm, s)) return rc;  // split nodes, split-multipole buffer
     // the pairs the two-float M2L leaves to the FP64 kernel, built now (it
     // synchronises the stream) rather than inside a later matvec
     if (int rc = prepare_extreme_rows(p->tree, p->lists, p->fmm, s)) return rc;
     p->fmm.arith = EDFMM_ARITH_TWO_FLOAT;
     return EDFMM_OK;
+}
+
+int edfmm_plan_set_launch(edfmm_plan *p, int knob, int value) {
+    if (int rc = check_plan(p)) return rc;
+    switch (knob) {
+    case EDFMM_LAUNCH_M2L_TF_BLOCK:
+        if (value != 128 && value != 256) return fail(EDFMM_ERR_ARG, "two-float M2L block must be 128 or 256");
+        p->fmm.m2l_tf_block = value;
+        return EDFMM_OK;
+    case EDFMM_LAUNCH_NEAR_OVERLAP:
+        if (value != 0 && value != 1) return fail(EDFMM_ERR_ARG, "near-field overlap must be 0 or 1");
+        p->fmm.near_overlap = value;
+        return EDFMM_OK;
+    default:
+        return fail(EDFMM_ERR_ARG, "unknown launch knob");
+    }
+}
+
+int edfmm_plan_get_launch(const edfmm_plan *p, int knob, int *value) {
+    if (int rc = check_plan(p)) return rc;
+    if (!value) return fail(EDFMM_ERR_ARG, "value is NULL");
+    switch (knob) {
+    case EDFMM_LAUNCH_M2L_TF_BLOCK: *value = p->fmm.m2l_tf_block; return EDFMM_OK;
+    case EDFMM_LAUNCH_NEAR_OVERLAP: *value = p->fmm.near_overlap; return EDFMM_OK;
+    default: return fail(EDFMM_ERR_ARG, "unknown launch knob");
+    }
 }
 
 int edfmm_plan_rebuild_lists(edfmm_plan *p, double mac_theta, void *stream) {
@@ -472,6 +501,9 @@ int edfmm_plan_set_order(edfmm_plan *p, int expansion_order, void *stream) {
     if (rc) return rc;
     EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.multipoles.p, 0, esz, s));
     EDFMM_CUDA_TRY(cudaMemsetAsync(p->fmm.locals.p, 0, esz, s));
+    if (p->fmm.arith == EDFMM_ARITH_TWO_FLOAT) {
+        if ((rc = prepare_two_float(p->tree, p->fmm, s))) return rc;  // split-multipole buffer at the new order
+    }
     return EDFMM_OK;
 }
 
@@ -618,7 +650,7 @@ int edfmm_plan_matvec(edfmm_plan *p, const void *sigma, const void *areas, const
     int rc;
     if (swapped && (rc = lists_build_swapped(p->tree, p->lists, s))) return rc;
     if ((rc = set_charges(p->tree, sigma, areas, s))) return rc;
-    if (far && near) {
+    if (far && near && p->fmm.near_overlap) {
         // The near field depends only on the charges: it runs on a second
         // stream beside P2M -> M2M -> M2L -> L2L, into tree-order sums that
         // the final pass (L2P + epilogue) adds.  Fork and join through

@@ -144,6 +144,20 @@ EDFMM_API int edfmm_plan_rebuild_lists(edfmm_plan *plan, double mac_theta, void 
 EDFMM_API int edfmm_plan_set_arithmetic(edfmm_plan *plan, int mode, void *stream);
 
 /*
+ * Launch shapes of a plan's matvec that the autotuner chooses by timing (no
+ * counterpart in the reference): EDFMM_LAUNCH_M2L_TF_BLOCK, threads per block
+ * of the two-float M2L at p = 8 (128: two blocks per SM; 256: one block of
+ * eight warps per SM, one instruction stream for the long pair code);
+ * EDFMM_LAUNCH_NEAR_OVERLAP, 1 to run the near field on a second stream beside
+ * the far-field chain, 0 for one fused pass after it.  Results are the same
+ * either way (bit for bit).
+ */
+#define EDFMM_LAUNCH_M2L_TF_BLOCK 1
+#define EDFMM_LAUNCH_NEAR_OVERLAP 2
+EDFMM_API int edfmm_plan_set_launch(edfmm_plan *plan, int knob, int value);
+EDFMM_API int edfmm_plan_get_launch(const edfmm_plan *plan, int knob, int *value);
+
+/*
  * Change the expansion order p (FmmConfig.expansion_order,
  * electrodrive/fmm3d/config.py:90-106); reallocates the expansion buffers.
  */
@@ -508,6 +522,37 @@ EDFMM_API int edfmm_pcn_loss(const float *y_dev, const double *scale_dev, const 
                              const double *areas_dev, int64_t n, float *dy_dev, double *loss_dev, void *stream);
 EDFMM_API int edfmm_pcn_adam(float *params_dev, const float *grads_dev, float *m_dev, float *v_dev, int64_t count,
                              float lr, float beta1, float beta2, float eps, int step, void *stream);
+
+/*
+ * Tensor-grid conductor meshes on the GPU (the mesh generators of
+ * electrodrive/core/bem_mesh.py:27-212: _mesh_sphere, _mesh_torus,
+ * _mesh_plane_patch, joined and finished as generate_mesh does).
+ * edfmm_mesh_grid writes one grid's na * nb vertices (row-major, at
+ * vertices_dev; the caller offsets the pointer) and its raw triangles (two
+ * per cell, vertex ids + vertex_offset) with their conductor id.  Tables
+ * (device, FP64): EDFMM_MESH_SPHERE ta = (sin, cos) of the polar angles,
+ * tb = (sin, cos) of the azimuths, params (cx, cy, cz, radius);
+ * EDFMM_MESH_TORUS ta = (sin, cos) of u, tb = (sin, cos) of v, params
+ * (cx, cy, cz, R, a); EDFMM_MESH_PLANE ta = x values, tb = y values,
+ * params (z).  edfmm_mesh_finish computes every raw panel's area
+ * 0.5 |(v1 - v0) x (v2 - v0)|, drops panels with area <= 1e-16 (order kept),
+ * and writes the kept panels' triangles, conductor ids, centroids, unit
+ * normals cross / (2 area + 1e-30) and areas; *n_out_host receives their
+ * count (the call synchronises `stream`).  Every operation follows numpy's
+ * evaluation order with correctly rounded arithmetic, so the arrays equal the
+ * host generators' bit for bit for the same tables.  Outputs are sized for
+ * n_triangles panels.
+ */
+#define EDFMM_MESH_SPHERE 1
+#define EDFMM_MESH_TORUS 2
+#define EDFMM_MESH_PLANE 3
+EDFMM_API int edfmm_mesh_grid(int kind, const double *params_host, const double *tab_a_dev, int64_t na,
+                              const double *tab_b_dev, int64_t nb, int64_t vertex_offset, int32_t conductor_id,
+                              double *vertices_dev, int32_t *triangles_dev, int32_t *conductor_ids_dev, void *stream);
+EDFMM_API int edfmm_mesh_finish(const double *vertices_dev, int64_t n_vertices, const int32_t *triangles_dev,
+                                const int32_t *conductor_ids_dev, int64_t n_triangles, int32_t *triangles_out_dev,
+                                int32_t *conductor_ids_out_dev, double *centroids_dev, double *normals_dev,
+                                double *areas_dev, int64_t *n_out_host, void *stream);
 
 /*
  * Measured FP64 FMA throughput (TFLOP/s): the roofline denominator of the

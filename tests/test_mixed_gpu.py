@@ -59,9 +59,13 @@ def test_autotuned_inner_operator_meets_its_bound_and_the_solve_converges(torus_
     S = torus_system
     op64 = S["ops"][torch.float64]
     op32, trials = autotune_inner_operator(op64, S["centroids"], S["areas"], S["self_corr"],
-                                           near=S["ops"][torch.float32].near, orders=(8, 6), max_rel_error=3e-7)
+                                           near=S["ops"][torch.float32].near, orders=(8, 6), max_rel_error=3e-7,
+                                           use_cache=False)
     assert {t["expansion_order"] for t in trials} == {8, 6}
-    chosen = [t for t in trials if t["expansion_order"] == op32.base.plan.info.expansion_order][0]
+    assert {t["launch"]["near_overlap"] for t in trials} == {0, 1}
+    launch = op32.base.plan.get_launch()
+    chosen = [t for t in trials if t["expansion_order"] == op32.base.plan.info.expansion_order
+              and t["launch"]["near_overlap"] == launch["near_overlap"]][0]
     assert chosen["rel_error"] <= 3e-7
     assert chosen["ms"] == min(t["ms"] for t in trials if t["rel_error"] <= 3e-7)
     b = S["b"]
