@@ -94,12 +94,14 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["fmm_matvec", "sphere_solve", "torus_solve", "batch_solve"],
+    ap.add_argument("--workload", choices=["fmm_matvec", "sphere_solve", "torus_solve", "batch_solve", "warm_start"],
                     default="fmm_matvec",
                     help="fmm_matvec: the headline operator benchmark; sphere_solve: 5,120-panel icosphere dense "
                          "FP64 solve; torus_solve: 200,000-panel torus, FMM + near correction, mixed-precision solve; "
                          "batch_solve: 256 sphere dimers of 2k-40k panels solved together")
     ap.add_argument("--batch", type=int, default=256, help="instances of the batch_solve workload")
+    ap.add_argument("--ws-geometries", type=int, default=500,
+                    help="warm_start: held-out geometries (10k-50k panels each) to evaluate")
     ap.add_argument("--torus-grid", default="500x200", help="torus_solve mesh grid n_u x n_v (2 n_u n_v panels)")
     ap.add_argument("--plain-full-cycle", action="store_true",
                     help="torus_solve: also time plain FP64 GMRES with the reference's full 256-step cycles")
@@ -366,6 +368,76 @@ def _solve_cpu_baseline(name, mesh, spec, opts):
             "solve_seconds_sample": sol["seconds"], "solve_seconds_scaled": est}
 
 
+def _reference_near_module(mesh, sysd, dev, stream, flush):
+    """The reference's own CUDA near-field module (electrodrive/core/
+    bem_near_cuda_kernel.cu, one thread per pair with atomic adds; built
+    unmodified from the reference's sources by oracle/ref_near.py) timed
+    beside this library's on-the-fly module (edfmm_near_quadrature_matvec:
+    one thread per pair in CSR order, rows summed in shared memory in pair
+    order, no atomics) on the same near set, order-2 rule, FP64: the
+    reference's API call, this library's API call (which groups the pairs
+    into rows by target once per pair tensor; the reference's API receives
+    them in any order) and its kernel alone on prebuilt rows."""
+    import numpy as np
+    import torch
+
+    from electrodrive_gb300 import _lib
+    from electrodrive_gb300.core.bem_near import apply_near_quadrature_matvec_cuda
+    from electrodrive_gb300.utils.config import K_E
+
+    try:
+        from oracle import ref_near
+
+        mod = ref_near.load()
+    except Exception as e:  # sources absent or the build failed
+        return {"unavailable": f"{type(e).__name__}: {str(e)[:200]}"}
+    near = sysd["ops"][torch.float64].near
+    pairs, _ = near.export()
+    n = sysd["n"]
+    C = sysd["centroids"].to(dev).contiguous()
+    A = sysd["areas"].contiguous()
+    PV = torch.as_tensor(np.ascontiguousarray(mesh.vertices[mesh.triangles]), dtype=torch.float64, device=dev)
+    sig = sysd["x0"].contiguous()
+    vfar = torch.zeros(n, dtype=torch.float64, device=dev)
+    ref_out = {}
+
+    def ref_call():
+        ref_out["v"] = mod.near_quadrature_matvec(vfar, sig, C, A, PV, pairs, float(K_E), 2)
+
+    ours_out = {}
+
+    def ours_call():
+        ours_out["v"] = apply_near_quadrature_matvec_cuda(vfar, sig, centroids=C, areas=A, panel_vertices=PV,
+                                                         near_pairs=pairs, quad_order=2)
+    # this library's kernel alone on rows built once
+    key = pairs[:, 0] * n + pairs[:, 1]
+    pr = pairs[torch.argsort(key, stable=True)]
+    counts = torch.bincount(pr[:, 0], minlength=n)
+    row_off = torch.cat([counts.new_zeros(1), torch.cumsum(counts, 0)]).to(torch.int32)
+    cols = pr[:, 1].to(torch.int32).contiguous()
+    kout = torch.empty_like(vfar)
+    L = _lib.load_library()
+    pv9 = PV.reshape(-1, 9)
+
+    def ours_kernel():
+        _lib.check(L.edfmm_near_quadrature_matvec(_lib.ptr(vfar), _lib.ptr(sig), _lib.ptr(C), _lib.ptr(A),
+                                                  _lib.ptr(pv9), _lib.ptr(row_off), _lib.ptr(cols), n, float(K_E), 2,
+                                                  _lib.EDFMM_F64, _lib.ptr(kout), _lib.stream_handle(dev)),
+                   "edfmm_near_quadrature_matvec")
+    t_ref = statistics.median(_time_cuda(ref_call, dev, stream, flush, 3, 10))
+    t_api = statistics.median(_time_cuda(ours_call, dev, stream, flush, 3, 10))
+    t_k = statistics.median(_time_cuda(ours_kernel, dev, stream, flush, 3, 10))
+    ref_v, our_v = ref_out["v"], ours_out["v"]
+    i, j = pairs[:, 0], pairs[:, 1]
+    r = torch.linalg.norm(C[i] - C[j], dim=1)
+    scale = torch.zeros(n, dtype=torch.float64, device=dev).index_add_(0, i, K_E * A[j] * sig[j].abs() / r)
+    err = float(((ref_v - our_v).abs() / scale.clamp_min(1e-300)).max())
+    return {"pairs": int(pairs.shape[0]), "quad_order": 2, "dtype": "f64",
+            "reference_api_ms": t_ref, "ours_api_ms": t_api, "ours_kernel_ms": t_k,
+            "speedup_api": t_ref / t_api, "speedup_kernel_vs_reference_api": t_ref / t_k,
+            "max_diff_over_term_scale": err, "kernel_equals_api": bool(torch.equal(kout, our_v))}
+
+
 def run_solve_workload(args, rank, world, local, emit=True):
     """sphere_solve / torus_solve: one BEM solve per step (solves/s).
     Returns the JSON record (printed by rank 0 when ``emit``)."""
@@ -457,6 +529,10 @@ def run_solve_workload(args, rank, world, local, emit=True):
     if args.profile_run:
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "ms_per_step": ms, "profile_run": True,
                "config": {"workload": workload}}
+        if name == "torus_solve":
+            p32 = sysd["ops"][torch.float32].base.plan
+            out["config"].update({"n_m2l_pairs_fp32": int(p32.info.n_m2l_pairs),
+                                  "expansion_order_fp32": int(p32.info.expansion_order)})
         if rank == 0 and emit:
             print(json.dumps(out), flush=True)
         return out
@@ -632,6 +708,7 @@ def run_solve_workload(args, rank, world, local, emit=True):
         extra["mixed_cold_start"] = {"ms": t_cold, "solves_per_s": 1e3 / t_cold, "outer_iters": cold["info"]["outer"],
                                      "inner_iters": cold["info"]["inner_iters"]}
         extra["warm_start"] = "learned (electrodrive_gb300/data/pcn_weights.npz)" if net is not None else "none"
+        extra["reference_near_module"] = _reference_near_module(mesh, sysd, dev, stream, flush)
         if net is not None:
             from electrodrive_gb300.core.warm_start import relative_error
 
@@ -640,7 +717,7 @@ def run_solve_workload(args, rank, world, local, emit=True):
         cfg = BEMConfig(use_near_quadrature_matvec=True)
         e2e_call = lambda: bem_solve(spec, cfg, mesh=mesh, operator="fmm", self_integral="quadrature", mixed=True,
                                      mixed_rtol=1e-6, inner_restart=40, inner_expansion_order=order32,
-                                     fp64_arithmetic="two_float")
+                                     fp64_arithmetic="two_float", warm_start=net)
         h2d = n * 8 * (3 + 1 + 9 + 3 + 1) * 2
 
     # end to end through the public API: host mesh -> solve -> host sigma
@@ -775,7 +852,8 @@ def run_batch_workload(args, rank, world, local, emit=True):
     if args.profile_run:
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "ms_per_step": ms, "profile_run": True,
                "config": {"workload": workload, "inner_operator": {k: tune[k] for k in ("leaf_size",
-                                                                                        "expansion_order")}}}
+                                                                                        "expansion_order")},
+                          "n_m2l_pairs_fp32": int(system.op32.plan.info.n_m2l_pairs)}}
         if rank == 0 and emit:
             print(json.dumps(out), flush=True)
         return out
@@ -890,6 +968,174 @@ def run_batch_workload(args, rank, world, local, emit=True):
         return out
 
 
+WS_FLOPS_PER_PANEL = 2 * (16 * 128 + 3 * 128 * 128 + 128)  # network forward, per panel (dense layers)
+
+
+def _ws_cpu_baseline(sample_cases, mean_panels: float, budget_s: float = 10.0):
+    """The oracle's plain cold-start solve (FP64 FMM p = 8, all host cores,
+    the reference's 256-step cycles, 1e-6) on the smallest of the sampled
+    geometries until ``budget_s``, as solves/s of a geometry of
+    ``mean_panels`` panels (the FMM's cost grows in proportion)."""
+    cpu = _batch_cpu_baseline(sample_cases, int(sum(m.n_panels for m, _ in sample_cases)), budget_s=budget_s)
+    secs, est = cpu["solve_seconds_sample"], cpu["solve_seconds_scaled"]
+    per_panel = est / sum(m.n_panels for m, _ in sample_cases)
+    return dict(cpu, value=1.0 / (per_panel * mean_panels),
+                sample=cpu["sample"] + f"; expressed per geometry of {mean_panels:.0f} panels (the held-out mean)")
+
+
+def run_warm_start_workload(args, rank, world, local, emit=True):
+    """warm_start: the learned warm start on held-out geometries (random
+    spheres, ellipsoids, tori and dimers of 10k-50k panels, seeds 7000+,
+    disjoint from the training and test seeds).  Per geometry: its converged
+    density (the FP64 FMM operator in two-float arithmetic, refined to
+    1e-10), then from the cold start (b / I_self), the base guess (b / A(1))
+    and the learned start, the Jacobi GMRES iterations and time to a 1e-6
+    true residual with the FP64 operator and the mixed FP32/FP64 solve to
+    1e-6 (start included).  value = held-out solves/s of the learned mixed
+    solve (mean time per geometry)."""
+    import numpy as np
+
+    from electrodrive_gb300.core.warm_start import KINDS, random_case
+
+    K = max(1, int(args.ws_geometries))
+    workload = (f"warm_start_heldout_{K}_geometries_sphere_ellipsoid_torus_dimer_10k-50k_panels_seeds7000+_"
+                "fmm_p8_mixed_fp32_fp64_rtol1e-6")
+
+    def cases():
+        rng = np.random.default_rng(7000)
+        for i in range(K):
+            yield random_case(rng, KINDS[i % len(KINDS)], int(rng.integers(10000, 50001)))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        allc = list(cases())
+        cpu = _ws_cpu_baseline(allc[:8], float(np.mean([m.n_panels for m, _ in allc])))
+        out = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "solves/s",
+               "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 / cpu["value"],
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic", "config": {"workload": workload}, "cpu_baseline": cpu,
+               "e2e": {"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if emit:
+            print(json.dumps(out), flush=True)
+        return out
+
+    import torch
+
+    from electrodrive_gb300 import _lib
+    from electrodrive_gb300.core.warm_start import PointCloudNet, compare_starts, make_sample
+    from electrodrive_gb300.train_warm_start import summarize
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    net = PointCloudNet.load(os.path.join(ROOT, "electrodrive_gb300", "data", "pcn_weights.npz"), device=dev)
+    evals, panels, kinds, largest = [], [], [], None
+    l0 = _lib.launch_count()
+    t_all = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for i, (mesh, spec) in enumerate(cases()):
+            s = make_sample(mesh, spec, device=dev, operator="fmm")
+            evals.append(compare_starts(net, s))
+            panels.append(mesh.n_panels)
+            kinds.append(KINDS[i % len(KINDS)])
+            if largest is None or mesh.n_panels > largest[0]:
+                largest = (mesh.n_panels, s["centroids"], s["normals"], s["areas"], s["b"])
+            del s
+    t_all = time.perf_counter() - t_all
+    launches = _lib.launch_count() - l0
+    # end to end through the public API on the first geometries: host mesh ->
+    # bem_solve(mixed, learned start) -> host sigma, set-up included
+    from electrodrive_gb300.core.bem import bem_solve
+    from electrodrive_gb300.utils.config import BEMConfig
+
+    e2e_n = min(K, 16)
+    e2e_s, e2e_h2d, e2e_d2h = [], [], []
+    for i, (mesh, spec) in enumerate(cases()):
+        if i >= e2e_n:
+            break
+        call = lambda: bem_solve(spec, BEMConfig(), mesh=mesh, operator="fmm", self_integral="quadrature",
+                                 mixed=True, mixed_rtol=1e-6, warm_start=net)
+        if i == 0:
+            call()  # warm (graph capture, workspaces)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = call()
+        sig_host = res["surface_charge_density"]
+        e2e_s.append(time.perf_counter() - t0)
+        e2e_h2d.append(8 * (3 + 1 + 9 + 3 + 1) * mesh.n_panels)
+        e2e_d2h.append(int(np.asarray(sig_host).nbytes))
+    summ = summarize(evals)
+    learned_s = [e["learned"]["mixed"]["seconds"] for e in evals]
+    cold_s = [e["cold"]["mixed"]["seconds"] for e in evals]
+    base_s = [e["base"]["mixed"]["seconds"] for e in evals]
+    ms = 1e3 * float(np.mean(learned_s))
+    value = world * 1e3 / ms
+    # roofline of the network's forward pass (BF16 tensor-core GEMMs) on the largest geometry
+    n_l, c_l, nr_l, a_l, b_l = largest
+    f = net.features(c_l, nr_l, a_l, b_l)
+    stream = torch.cuda.current_stream(dev)
+    net.forward(f)
+    torch.cuda.synchronize(dev)
+    tt = []
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        net.forward(f)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        tt.append(e0.elapsed_time(e1))
+    t_fwd = statistics.median(tt)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except Exception:
+        pass
+    ach = WS_FLOPS_PER_PANEL * n_l / (t_fwd * 1e-3) / 1e12
+    peak = peaks.get("bf16_tflops") or 1900.0
+    roof = {"kernel": "k_pcn_linear (network forward, BF16 mma.sync, largest held-out geometry)", "bound": "tensor",
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops" if peaks.get("bf16_tflops") else "fallback 1.9 PFLOP/s",
+            "panels": n_l, "forward_ms": t_fwd}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = _ws_cpu_baseline([c for c, _ in zip(cases(), range(8))], float(np.mean(panels)))
+        except Exception as e:
+            cpu = {"value": None, "error": str(e)[:200]}
+    per_kind = {}
+    for k in KINDS:
+        idx = [j for j, kk in enumerate(kinds) if kk == k]
+        if idx:
+            per_kind[k] = {"geometries": len(idx),
+                           "mixed_ms": {st: 1e3 * float(np.mean([evals[j][st]["mixed"]["seconds"] for j in idx]))
+                                        for st in ("cold", "base", "learned")},
+                           "mixed_outer": {st: float(np.mean([evals[j][st]["mixed"]["outer"] for j in idx]))
+                                           for st in ("cold", "base", "learned")},
+                           "gmres_iters": {st: float(np.mean([evals[j][st]["iters"] for j in idx]))
+                                           for st in ("cold", "base", "learned")}}
+    out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": 1,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+           "data": "synthetic",
+           "config": {"workload": workload, "geometries": K, "panels_mean": float(np.mean(panels)),
+                      "panels_min": int(min(panels)), "panels_max": int(max(panels)),
+                      "weights": "electrodrive_gb300/data/pcn_weights.npz", "wall_s": t_all},
+           "held_out": summ,
+           "mixed_speedup_learned_vs_cold": float(np.mean(cold_s) / np.mean(learned_s)),
+           "mixed_speedup_learned_vs_base": float(np.mean(base_s) / np.mean(learned_s)),
+           "fraction_learned_faster_than_cold": float(np.mean([a < b for a, b in zip(learned_s, cold_s)])),
+           "per_kind": per_kind,
+           "e2e": {"value": world / float(np.mean(e2e_s)), "unit": "solves/s",
+                   "h2d_bytes_per_step": int(np.mean(e2e_h2d)), "d2h_bytes_per_step": int(np.mean(e2e_d2h)),
+                   "ms_per_step": 1e3 * float(np.mean(e2e_s)), "geometries": e2e_n,
+                   "includes": "bem_solve(mixed=True, warm_start=net) from the host mesh: self integrals, trees "
+                               "and lists, the learned start, the solve and the sigma read-back"},
+           "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof, "cpu_baseline": cpu}
+    if rank == 0 and emit:
+        print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -897,6 +1143,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload == "batch_solve":
         run_batch_workload(args, rank, world, local)
+        return
+    if args.workload == "warm_start":
+        run_warm_start_workload(args, rank, world, local)
         return
     if args.workload != "fmm_matvec":
         run_solve_workload(args, rank, world, local)
@@ -1062,12 +1311,17 @@ def main():
         torch.cuda.empty_cache()
         out["workloads"] = {}
         for sub, steps in (("torus_solve", min(args.steps, 5)), ("sphere_solve", min(args.steps, 5)),
-                           ("batch_solve", min(args.steps, 3))):
+                           ("batch_solve", min(args.steps, 3)), ("warm_start", None)):
             sargs = argparse.Namespace(**vars(args))
-            sargs.workload, sargs.steps = sub, steps
+            sargs.workload = sub
+            if steps is not None:
+                sargs.steps = steps
+            else:
+                sargs.ws_geometries = min(args.ws_geometries, 48)  # held-out sample in the default run
             t0 = time.perf_counter()
             try:
-                fn = run_batch_workload if sub == "batch_solve" else run_solve_workload
+                fn = {"batch_solve": run_batch_workload, "warm_start": run_warm_start_workload}.get(
+                    sub, run_solve_workload)
                 rec = fn(sargs, rank, world, local, emit=False)
                 rec["wall_s"] = time.perf_counter() - t0
             except Exception as e:  # a failing sub-record must not lose the headline line

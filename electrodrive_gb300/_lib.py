@@ -33,6 +33,7 @@ EDFMM_ARITH_NATIVE = 0
 EDFMM_ARITH_TWO_FLOAT = 1
 EDFMM_LAUNCH_M2L_TF_BLOCK = 1
 EDFMM_LAUNCH_NEAR_OVERLAP = 2
+EDFMM_LAUNCH_M2L_PACKED = 3
 EDFMM_MESH_SPHERE = 1
 EDFMM_MESH_TORUS = 2
 EDFMM_MESH_PLANE = 3
@@ -346,7 +347,8 @@ class Plan:
                   "edfmm_plan_set_arithmetic")
         self.arithmetic = mode
 
-    _KNOBS = {"m2l_tf_block": EDFMM_LAUNCH_M2L_TF_BLOCK, "near_overlap": EDFMM_LAUNCH_NEAR_OVERLAP}
+    _KNOBS = {"m2l_tf_block": EDFMM_LAUNCH_M2L_TF_BLOCK, "near_overlap": EDFMM_LAUNCH_NEAR_OVERLAP,
+              "m2l_packed": EDFMM_LAUNCH_M2L_PACKED}
 
     def set_launch(self, **knobs):
         """Launch shapes: m2l_tf_block (128 or 256), near_overlap (0 or 1)."""

@@ -99,7 +99,9 @@ def dimer_case_device(seed: int, n_panels: Optional[int] = None, device=None):
 
 class BatchSystem:
     """Device-resident batched system: FP64 and FP32 batched FMM operators,
-    right-hand side, Jacobi diagonal and instance offsets."""
+    right-hand side, Jacobi diagonal and instance offsets.  The cases' meshes
+    are host TriMesh arrays or DeviceTriMesh tensors (generated on the GPU:
+    then nothing of the geometry crosses from the host)."""
 
     def __init__(self, cases: Sequence[Tuple[TriMesh, Dict[str, Any]]], *, leaf_size: int = 64,
                  expansion_order: int = 8, inner_leaf_size: Optional[int] = None,
@@ -122,21 +124,32 @@ class BatchSystem:
         sizes = [m.n_panels for m, _ in self.cases]
         self.offsets = [0] + list(np.cumsum(sizes).astype(int))
         self.n = int(self.offsets[-1])
-        C = np.concatenate([m.centroids for m, _ in self.cases])
-        A = np.concatenate([m.areas for m, _ in self.cases])
-        self.normals = torch.as_tensor(np.concatenate([m.normals for m, _ in self.cases]), dtype=torch.float64,
-                                       device=dev)
-        # panel vertex triples gathered on the device from the (smaller)
-        # vertex and triangle arrays
-        vbase = np.concatenate([[0], np.cumsum([m.vertices.shape[0] for m, _ in self.cases])])
-        V = torch.as_tensor(np.concatenate([m.vertices for m, _ in self.cases]), dtype=torch.float64, device=dev)
-        tri = torch.as_tensor(np.concatenate([np.asarray(m.triangles, dtype=np.int64) + vbase[k]
-                                              for k, (m, _) in enumerate(self.cases)]), device=dev)
+        if self.cases and isinstance(self.cases[0][0].vertices, Tensor):
+            # meshes generated on the device (core.mesh_device): concatenated there
+            ms = [m for m, _ in self.cases]
+            vbase = np.concatenate([[0], np.cumsum([m.vertices.shape[0] for m in ms])])
+            V = torch.cat([m.vertices.to(dev) for m in ms])
+            tri = torch.cat([m.triangles.to(dev).long() + int(vbase[k]) for k, m in enumerate(ms)])
+            self.normals = torch.cat([m.normals.to(dev) for m in ms])
+            self.C64 = torch.cat([m.centroids.to(dev) for m in ms])
+            self.areas = torch.cat([m.areas.to(dev) for m in ms])
+            self.h2d_bytes = 0
+        else:
+            C = np.concatenate([m.centroids for m, _ in self.cases])
+            A = np.concatenate([m.areas for m, _ in self.cases])
+            self.normals = torch.as_tensor(np.concatenate([m.normals for m, _ in self.cases]), dtype=torch.float64,
+                                           device=dev)
+            # panel vertex triples gathered on the device from the (smaller)
+            # vertex and triangle arrays
+            vbase = np.concatenate([[0], np.cumsum([m.vertices.shape[0] for m, _ in self.cases])])
+            V = torch.as_tensor(np.concatenate([m.vertices for m, _ in self.cases]), dtype=torch.float64, device=dev)
+            tri = torch.as_tensor(np.concatenate([np.asarray(m.triangles, dtype=np.int64) + vbase[k]
+                                                  for k, (m, _) in enumerate(self.cases)]), device=dev)
+            # host -> device bytes of the set-up (centroids, areas, normals, vertices, triangles)
+            self.h2d_bytes = int(8 * (3 + 1 + 3) * self.n + V.numel() * 8 + tri.numel() * 8)
+            self.C64 = torch.as_tensor(C, dtype=torch.float64, device=dev)
+            self.areas = torch.as_tensor(A, dtype=torch.float64, device=dev)
         PV = V[tri]
-        # host -> device bytes of the set-up (centroids, areas, normals, vertices, triangles)
-        self.h2d_bytes = int(8 * (3 + 1 + 3) * self.n + V.numel() * 8 + tri.numel() * 8)
-        self.C64 = torch.as_tensor(C, dtype=torch.float64, device=dev)
-        self.areas = torch.as_tensor(A, dtype=torch.float64, device=dev)
         mark("host_concat_and_copy")
         I_self = self_integrals(PV, self.C64, order=2, depth=3, device=dev)
         self.self_corr = I_self / self.areas.clamp_min(torch.finfo(torch.float64).tiny)

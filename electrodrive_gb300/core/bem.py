@@ -208,7 +208,8 @@ def _info_ok(info: Dict[str, Any]) -> Tuple[bool, float, int]:
 
 def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtype, mixed: bool, mixed_rtol: float,
                 inner_restart: int, inner_expansion_order: Optional[int], operator: str, fmm_threshold: int,
-                use_graph: bool, self_integral: str, logger, fp64_arithmetic: str = "native") -> Dict[str, Any]:
+                use_graph: bool, self_integral: str, logger, fp64_arithmetic: str = "native",
+                warm_start: Optional[Any] = None) -> Dict[str, Any]:
     """One refinement pass of bem.py:1629-2404 on a given mesh: set-up, the
     linear solve with its retry and fallback chain, and the pass results.
     Returns {"error": msg} on a failure the reference reports as an error."""
@@ -276,7 +277,16 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
 
     sigma = info = None
     if mixed:
-        x, minfo = solve_mixed(op, op32, b, A_diag=diag if use_precond else None, x0=x0, rtol=mixed_rtol,
+        xm0 = x0
+        if warm_start is not None:
+            # the learned start (features, network, one FP32 operator
+            # application); the reference's chain below keeps x0 = b / I_self
+            from .warm_start import panel_geometry, warm_start as learned_start
+
+            xs = learned_start(warm_start, panel_geometry(mesh, dev), b, op32)
+            if bool(torch.isfinite(xs).all()):
+                xm0 = xs.to(dtype)
+        x, minfo = solve_mixed(op, op32, b, A_diag=diag if use_precond else None, x0=xm0, rtol=mixed_rtol,
                                inner_restart=inner_restart, use_graph=use_graph)
         bn = float(torch.linalg.norm(b))
         if minfo["success"]:
@@ -322,7 +332,7 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
               *, mesh: Optional[TriMesh] = None, operator: str = "auto", fmm_threshold: int = 20000,
               use_graph: bool = True, self_integral: str = "auto", mixed: bool = False, mixed_rtol: float = 1e-6,
               inner_restart: int = 40, inner_expansion_order: Optional[int] = None,
-              fp64_arithmetic: str = "two_float") -> Dict[str, Any]:
+              fp64_arithmetic: str = "two_float", warm_start: Optional[Any] = None) -> Dict[str, Any]:
     """The reference's bem_solve (bem.py:1550-2695) on the GPU operator.
 
     h-refinement (bem.py:1667-2495): pass k meshes at h = initial_h *
@@ -352,7 +362,9 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
     reference's chain in FP64); ``fp64_arithmetic`` ("two_float", the
     default, or "native") is the arithmetic of that FP64 FMM operator's M2L
     and near field (two-float: about 48 significant bits on the FP32 pipe,
-    within about 1e-13 of IEEE FP64).
+    within about 1e-13 of IEEE FP64); ``warm_start`` (a trained
+    :class:`~electrodrive_gb300.core.warm_start.PointCloudNet`) starts the
+    mixed solve from the network's prediction instead of b / I_self.
     """
     if differentiable:
         raise NotImplementedError("the differentiable (xitorch) path is not part of electrodrive_gb300")
@@ -401,7 +413,7 @@ def bem_solve(spec: Any, cfg: Optional[BEMConfig] = None, logger: Optional[Any] 
         res = _solve_pass(spec, cfg, m, current_h, dev=dev, dtype=dtype, mixed=mixed, mixed_rtol=mixed_rtol,
                           inner_restart=inner_restart, inner_expansion_order=inner_expansion_order, operator=operator,
                           fmm_threshold=fmm_threshold, use_graph=use_graph, self_integral=self_integral,
-                          logger=logger, fp64_arithmetic=fp64_arithmetic)
+                          logger=logger, fp64_arithmetic=fp64_arithmetic, warm_start=warm_start)
         if "error" in res:
             msg = res.pop("error")
             return error_result(msg, **res)

@@ -11,7 +11,7 @@
 from __future__ import annotations
 
 import ctypes as C
-from typing import Optional
+from typing import List, Optional, Tuple
 
 import numpy as np
 import torch
@@ -105,26 +105,52 @@ class NearCorrection:
         return out
 
 
+# rows by target of the last few pair tensors passed to
+# apply_near_quadrature_matvec_cuda: (tensor, its version counter, n, device,
+# (row_off, cols)); the tensor is held, so its storage cannot be reused
+# under a cached entry
+_PAIR_ROWS: List[Tuple[Tensor, int, int, torch.device, Tuple[Tensor, Tensor]]] = []
+
+
+def _pair_rows(near_pairs, n: int, dev: torch.device) -> Tuple[Tensor, Tensor]:
+    """CSR rows by target (row_off int32 (n+1), cols int32, sources ascending
+    within a row) of a (P, 2) (i, j) pair list."""
+    if isinstance(near_pairs, Tensor):
+        for t, ver, nn, d, rows in _PAIR_ROWS:
+            if t is near_pairs and ver == near_pairs._version and nn == n and d == dev:
+                return rows
+    pr = torch.as_tensor(near_pairs).to(dev, torch.int64).reshape(-1, 2)
+    if pr.shape[0]:
+        pr = pr[torch.argsort(pr[:, 0] * n + pr[:, 1], stable=True)]  # (i, j) lexicographic
+        counts = torch.bincount(pr[:, 0], minlength=n)
+        row_off = torch.cat([counts.new_zeros(1), torch.cumsum(counts, 0)]).to(torch.int32)
+        cols = pr[:, 1].to(torch.int32).contiguous()
+    else:
+        row_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+        cols = torch.zeros(1, dtype=torch.int32, device=dev)
+    if isinstance(near_pairs, Tensor):
+        _PAIR_ROWS.append((near_pairs, near_pairs._version, n, dev, (row_off, cols)))
+        del _PAIR_ROWS[:-4]
+    return row_off, cols
+
+
 def apply_near_quadrature_matvec_cuda(V_far: Tensor, sigma: Tensor, *, centroids: Tensor, areas: Tensor,
                                       panel_vertices: Tensor, near_pairs, quad_order: int = 2,
                                       K_E: Optional[float] = None) -> Tensor:
     """The reference module's call (bem_near_cuda.py:175-290) on CUDA tensors.
 
-    ``near_pairs`` is a (P, 2) (i, j) array; pairs are regrouped into rows by
-    target on the host once per call (the reference passes them unsorted).
+    ``near_pairs`` is a (P, 2) (i, j) array or tensor (the reference passes
+    them in any order); they are grouped into rows by target on the device,
+    once per pair tensor: a solve that passes the same tensor every matvec
+    reuses the rows (a tensor changed in place is regrouped).
     """
     from ..utils.config import K_E as _KE
 
     ke = float(_KE if K_E is None else K_E)
     L = _lib.load_library()
     dev, dt = V_far.device, V_far.dtype
-    pr = torch.as_tensor(near_pairs).to("cpu", torch.int64).numpy()
     n = int(V_far.shape[0])
-    order = np.lexsort((pr[:, 1], pr[:, 0])) if pr.size else np.zeros(0, np.int64)
-    pr = pr[order]
-    counts = np.bincount(pr[:, 0], minlength=n) if pr.size else np.zeros(n, np.int64)
-    row_off = torch.as_tensor(np.concatenate([[0], np.cumsum(counts)]).astype(np.int32), device=dev)
-    cols = torch.as_tensor(pr[:, 1].astype(np.int32) if pr.size else np.zeros(1, np.int32), device=dev)
+    row_off, cols = _pair_rows(near_pairs, n, dev)
     T = lambda x: x.to(dev, dt).contiguous()
     out = torch.empty_like(V_far)
     with torch.cuda.device(dev):

@@ -175,6 +175,16 @@ def _rotation(rng) -> np.ndarray:
                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
 
 
+_ICO_CACHE: Dict[int, TriMesh] = {}
+
+
+def _ico(sub: int) -> TriMesh:
+    """The unit icosphere of ``sub`` subdivisions (built once per process)."""
+    if sub not in _ICO_CACHE:
+        _ICO_CACHE[sub] = icosphere(sub)
+    return _ICO_CACHE[sub]
+
+
 def _transform(mesh: TriMesh, R: np.ndarray, scale=(1.0, 1.0, 1.0), shift=(0.0, 0.0, 0.0), cid: int = 0) -> TriMesh:
     v = (mesh.vertices * np.asarray(scale)[None, :]) @ R.T + np.asarray(shift)[None, :]
     return _finish(v, mesh.triangles.copy(), np.full(mesh.triangles.shape[0], cid, np.int32))
@@ -186,14 +196,20 @@ def _join(a: TriMesh, b: TriMesh) -> TriMesh:
     return _finish(v, t, np.concatenate([a.conductor_ids, b.conductor_ids]))
 
 
+def _ico_sub(panels: float) -> int:
+    """Icosphere subdivisions (20 * 4^k panels) closest to ``panels``, 3..6."""
+    return int(min(6, max(3, round(math.log(max(panels, 20.0) / 20.0, 4)))))
+
+
 def random_case(rng: np.random.Generator, kind: str, panels: int = 4000) -> Tuple[TriMesh, Dict[str, Any]]:
-    """A random conductor geometry of about ``panels`` panels, a random
-    potential per conductor and a unit-scale point charge outside it."""
+    """A random conductor geometry of about ``panels`` panels (icospheres come
+    in 20 * 4^k panels: 1,280 to 81,920), a random potential per conductor
+    and a unit-scale point charge outside it."""
     R = _rotation(rng)
     if kind in ("sphere", "ellipsoid"):
-        sub = 3 if panels < 3000 else 4
+        sub = _ico_sub(panels)
         axes = (rng.uniform(0.5, 1.5),) * 3 if kind == "sphere" else tuple(rng.uniform(0.5, 2.0, 3))
-        mesh = _transform(icosphere(sub), R, axes)
+        mesh = _transform(_ico(sub), R, axes)
         conds = [dict(type=kind, potential=float(rng.uniform(-1, 1)), id=0)]
     elif kind == "torus":
         Rt = rng.uniform(0.8, 1.5)
@@ -206,9 +222,9 @@ def random_case(rng: np.random.Generator, kind: str, panels: int = 4000) -> Tupl
         r1, r2 = rng.uniform(0.5, 1.5, 2)
         gap = rng.uniform(0.1, 1.0)
         axis = R[:, 0]
-        sub = 3 if panels < 6000 else 4
-        a = _transform(icosphere(sub), np.eye(3), (r1, r1, r1), -axis * (r1 + gap / 2), 0)
-        b = _transform(icosphere(sub), np.eye(3), (r2, r2, r2), axis * (r2 + gap / 2), 1)
+        sub = _ico_sub(panels / 2.0)
+        a = _transform(_ico(sub), np.eye(3), (r1, r1, r1), -axis * (r1 + gap / 2), 0)
+        b = _transform(_ico(sub), np.eye(3), (r2, r2, r2), axis * (r2 + gap / 2), 1)
         mesh = _join(a, b)
         conds = [dict(type="sphere", potential=float(rng.uniform(-1, 1)), id=0),
                  dict(type="sphere", potential=float(rng.uniform(-1, 1)), id=1)]
@@ -226,21 +242,37 @@ def random_case(rng: np.random.Generator, kind: str, panels: int = 4000) -> Tupl
 KINDS = ("sphere", "ellipsoid", "torus", "dimer")
 
 
-def make_sample(mesh: TriMesh, spec: Dict[str, Any], *, device=None, tol: float = 1e-10) -> Dict[str, Any]:
-    """Solve one case with the plain method (dense FP64 operator, Jacobi GMRES)
-    and keep what training and evaluation need, on the device."""
-    from .bem import assemble_system
+def make_sample(mesh: TriMesh, spec: Dict[str, Any], *, device=None, tol: float = 1e-10, operator: str = "auto",
+                keep_ops: bool = True) -> Dict[str, Any]:
+    """Solve one case to ``tol`` and keep what training and evaluation need,
+    on the device.  ``operator``: "dense" (FP64 dense operator, Jacobi GMRES;
+    the default up to 8,000 panels) or "fmm" (FP64 FMM operator with M2L and
+    near field in two-float arithmetic, refined around FP32 FMM GMRES; the
+    default above).  ``keep_ops=False`` drops the operators (training needs
+    only the panel data, b, the base guess and the converged density)."""
+    from .bem import assemble_system, solve_mixed
     from .bem_solver import gmres_restart
 
-    sysd = assemble_system(mesh, spec, kind="dense", dtypes=(torch.float64,), device=device)
-    op = sysd["ops"][torch.float64]
-    b, diag = sysd["b"], sysd["diag"]
-    sigma, info = gmres_restart(op, b, restart=100, tol=tol, maxiter=2000, precond="jacobi", A_diag=diag,
-                                x0=sysd["x0"], use_graph=True, early_exit=10)
+    kind = "dense" if operator == "dense" or (operator == "auto" and mesh.n_panels <= 8000) else "fmm"
+    if kind == "dense":
+        sysd = assemble_system(mesh, spec, kind="dense", dtypes=(torch.float64,), device=device)
+        op, op32 = sysd["ops"][torch.float64], None
+        b, diag = sysd["b"], sysd["diag"]
+        sigma, info = gmres_restart(op, b, restart=100, tol=tol, maxiter=2000, precond="jacobi", A_diag=diag,
+                                    x0=sysd["x0"], use_graph=True, early_exit=10)
+    else:
+        sysd = assemble_system(mesh, spec, kind="fmm", dtypes=(torch.float64, torch.float32), device=device)
+        op, op32 = sysd["ops"][torch.float64], sysd["ops"][torch.float32]
+        op.base.plan.set_arithmetic("two_float")
+        b, diag = sysd["b"], sysd["diag"]
+        sigma, info = solve_mixed(op, op32, b, A_diag=diag, x0=sysd["x0"], rtol=tol, inner_restart=100)
     dev = b.device
-    return dict(mesh=mesh, spec=spec, op=op, b=b, diag=diag, sigma=sigma.to(torch.float64), areas=sysd["areas"],
-                scale=base_guess(op, b), normals=torch.as_tensor(mesh.normals, device=dev),
-                centroids=torch.as_tensor(mesh.centroids, device=dev), solve_info=info)
+    out = dict(mesh=mesh, spec=spec, op=op, op32=op32, b=b, diag=diag, sigma=sigma.to(torch.float64),
+               areas=sysd["areas"], scale=base_guess(op, b), normals=torch.as_tensor(mesh.normals, device=dev),
+               centroids=torch.as_tensor(mesh.centroids, device=dev), solve_info=info, operator=kind)
+    if not keep_ops:
+        out["op"] = out["op32"] = None
+    return out
 
 
 def train(net: PointCloudNet, samples: List[Dict[str, Any]], *, epochs: int = 100, lr: float = 1e-3,
@@ -292,17 +324,45 @@ def iterations_to(op, b: Tensor, diag: Tensor, x0: Tensor, rtol: float = 1e-6, r
     return dict(iters=info["iters"], seconds=dt, code=info["code"], rel_resid=rel, r0=r0 / bn)
 
 
-def compare_starts(net: Optional[PointCloudNet], sample: Dict[str, Any], rtol: float = 1e-6) -> Dict[str, Any]:
-    """Iterations and time to rtol from the cold start (b / I_self), the base
-    guess (b / A(1)) and the learned start; plus each start's relative error."""
+def _timed_start(fn) -> Tuple[Tensor, float]:
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x0 = fn()
+    torch.cuda.synchronize()
+    return x0, time.perf_counter() - t0
+
+
+def compare_starts(net: Optional[PointCloudNet], sample: Dict[str, Any], rtol: float = 1e-6,
+                   mixed: bool = True) -> Dict[str, Any]:
+    """For the cold start (b / I_self, the reference's x0), the base guess
+    (b / A(1)) and the learned start: each start's relative error against the
+    converged density, the Jacobi GMRES iterations and time to ``rtol`` with
+    the FP64 operator, and (``mixed`` and an FP32 operator in the sample) the
+    mixed FP32/FP64 refinement solve to ``rtol``: refinement steps, inner
+    iterations, FP64 operator applications and time, the time to compute the
+    start included."""
+    from .bem import solve_mixed
+
     op, b, diag, sigma, areas = sample["op"], sample["b"], sample["diag"], sample["sigma"], sample["areas"]
-    starts = {"cold": b / diag, "base": sample["scale"]}
+    geom = panel_geometry(sample["mesh"], b.device)
+    makers = {"cold": lambda: b / diag, "base": lambda: base_guess(op, b)}
     if net is not None:
-        starts["learned"] = warm_start(net, sample["mesh"], b, op)
+        makers["learned"] = lambda: warm_start(net, geom, b, op)
+    op32 = sample.get("op32")
     out = {}
-    for name, x0 in starts.items():
+    for name, make in makers.items():
+        x0, t_start = _timed_start(make)
         r = iterations_to(op, b, diag, x0, rtol)
         r["start_error"] = relative_error(x0, sigma, areas)
+        r["start_seconds"] = t_start
+        if mixed and op32 is not None:
+            solve_mixed(op, op32, b, A_diag=diag, x0=make(), rtol=rtol)  # warm (graphs, workspaces)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            xm, info = solve_mixed(op, op32, b, A_diag=diag, x0=make(), rtol=rtol)
+            torch.cuda.synchronize()
+            r["mixed"] = dict(seconds=time.perf_counter() - t0, outer=info["outer"], inner_iters=info["inner_iters"],
+                              fp64_matvecs=info["matvec64"], code=info["code"], rel_resid=info["rel_resid"])
         out[name] = r
     return out
 

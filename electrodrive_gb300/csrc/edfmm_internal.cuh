@@ -240,6 +240,12 @@ __device__ __forceinline__ bool inst_active(const InstMask &m, int node) {
 
 int tree_build(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth,
                DevTree &tree, cudaStream_t s);
+// One tree per instance (rows inst_off[k] .. inst_off[k+1]-1, host offsets),
+// built together level by level as one forest: nodes of instance k are the
+// DFS range [inst_node_off[k], inst_node_off[k+1]), each tree equal to
+// tree_build of its rows alone; nodes grouped by level across instances.
+int tree_build_forest(const void *points_dev, const int64_t *inst_off, int n_inst, int dtype, int leaf_size,
+                      int max_depth, DevTree &tree, cudaStream_t s);
 
 struct DevLists {
     int64_t n_p2p = 0, n_m2l = 0;
@@ -254,9 +260,6 @@ struct DevLists {
 };
 
 int lists_build(const DevTree &tree, double theta, DevLists &lists, cudaStream_t s);
-// pack per-instance trees and lists into one (batch.cu)
-int pack_batch(std::vector<DevTree> &trees, std::vector<DevLists> &lists, int dtype, DevTree &T, DevLists &L,
-               cudaStream_t s);
 int lists_build_swapped(const DevTree &tree, DevLists &lists, cudaStream_t s);
 // lists between two trees: rows = target-tree nodes, sources = source-tree nodes
 // (the reference's build_interaction_lists(source_tree, target_tree))
@@ -292,13 +295,14 @@ struct FmmBuffers {
     // launch shapes the autotuner may change (edfmm_plan_set_launch)
     int m2l_tf_block = 128;  // two-float M2L threads per block (128 or 256, p = 8)
     int near_overlap = 1;    // full matvec: near field on a second stream beside the far field
+    int m2l_packed = 1;      // two-float M2L: matrices on packed FP32x2 instructions
 };
 
 int set_charges(const DevTree &tree, const void *sigma, const void *areas, cudaStream_t s);
 int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s);
-// rotation-based M2L (m2l_rot.cu), orders 1..8, FP32 and FP64
+// rotation-based M2L (m2l_rot.cu, kernels in m2l_rot.cuh), orders 1..8, FP32 and FP64
 int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s);
@@ -308,7 +312,7 @@ int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_
 // per node; Mx: one float4 per complex coefficient), locals written as FP64
 int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
                       const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
-                      int block, cudaStream_t s);
+                      int block, bool packed, cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,
                 FmmBuffers &tgt_buf, cudaStream_t s);
 int run_l2l(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);

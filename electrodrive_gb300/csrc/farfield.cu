@@ -31,7 +31,7 @@ namespace edfmm {
 namespace {
 
 constexpr float kExtremeRatio = 256.0f;
-constexpr int kRotPMaxUsed = 8;  // rotation-based M2L (m2l_rot.cu) for p <= 8
+constexpr int kRotPMaxUsed = 8;  // rotation-based M2L (m2l_rot.cuh) for p <= 8
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -948,7 +948,8 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
         k_split_coeffs<<<nblk(nq, 256), 256, 0, s>>>(dptr<double2>(sbuf.multipoles), nq, dptr<float4>(sbuf.mult_tf));
         EDFMM_LAUNCH_CHECK("k_split_coeffs");
         int rc = launch_m2l_rot_tf(buf.p, M, off, src, tree.nodes_tf.p, tree.half.p, stree.nodes_tf.p, stree.half.p,
-                                   sbuf.mult_tf.p, buf.locals.p, buf.nc_pad, buf.mask, buf.m2l_tf_block, s);
+                                   sbuf.mult_tf.p, buf.locals.p, buf.nc_pad, buf.mask, buf.m2l_tf_block,
+                                   buf.m2l_packed != 0, s);
         if (rc == EDFMM_OK) two_float = true;
         else if (rc != EDFMM_ERR_UNSUPPORTED) return rc;
     }

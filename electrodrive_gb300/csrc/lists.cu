@@ -209,6 +209,13 @@ int build_csr(const int2 *pairs, int64_t np, int64_t rows, int key_x, DevBuf &of
     return sort_csr_rows(dptr<int32_t>(off), dptr<int32_t>(vals), rows, max_row, s);
 }
 
+// the first front of a forest's traversal: (root, root) for every root
+// (level 0 of the tree; a single tree has one root, DFS id 0)
+__global__ void k_root_pairs(const int32_t *level_nodes, int K, int2 *front) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < K) front[k] = make_int2(level_nodes[k], level_nodes[k]);
+}
+
 template <typename T>
 int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists &L, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
@@ -230,10 +237,18 @@ int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists
     }
     PairBuf m2l, p2p;
     DevBuf front, next, code, cm, cp, cn, om, op, on, tmp, tot;
-    if ((rc = tot.reserve(sizeof(int64_t) * 3)) || (rc = front.reserve(sizeof(int2)))) return rc;
-    int2 root = make_int2(0, 0);
-    EDFMM_CUDA_TRY(cudaMemcpyAsync(front.p, &root, sizeof(int2), cudaMemcpyHostToDevice, s));
-    int64_t nf = 1;
+    // a same-tree forest (batched plan) starts from every (root, root) pair;
+    // no pair ever joins two trees, so each tree gets its own lists
+    const int n_roots = same && tree.level_offsets.size() > 1 ? tree.level_offsets[1] - tree.level_offsets[0] : 1;
+    if ((rc = tot.reserve(sizeof(int64_t) * 3)) || (rc = front.reserve(sizeof(int2) * n_roots))) return rc;
+    if (n_roots > 1) {
+        k_root_pairs<<<nblk(n_roots, 256), 256, 0, s>>>(dptr<int32_t>(tree.level_nodes), n_roots, dptr<int2>(front));
+        EDFMM_LAUNCH_CHECK("k_root_pairs");
+    } else {
+        int2 root = make_int2(0, 0);
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(front.p, &root, sizeof(int2), cudaMemcpyHostToDevice, s));
+    }
+    int64_t nf = n_roots;
     while (nf > 0) {
         if ((rc = code.reserve(nf)) || (rc = cm.reserve(4 * nf)) || (rc = cp.reserve(4 * nf)) || (rc = cn.reserve(4 * nf)) ||
             (rc = om.reserve(4 * nf)) || (rc = op.reserve(4 * nf)) || (rc = on.reserve(4 * nf)) ||

@@ -350,49 +350,83 @@ __global__ void k_cast(const double *in, T *out, int64_t n) {
 }
 
 // the reference CUDA module's on-the-fly correction: rule on the unit triangle
-// (u, v) with weights normalised to 1, scaled by A_j; one warp per target row
+// (u, v) with weights normalised to 1, scaled by A_j.  One thread per pair
+// (CSR order) for kNearRows consecutive target rows per block, the pairs'
+// corrections staged in shared memory and summed per row by one thread in
+// pair order (deterministic, no atomics; a row of any length).  1 / r is
+// one FP64 reciprocal square root of max(r^2, 1e-24), i.e. 1 / max(r, 1e-12)
+// as the reference clamps it, instead of a square root and a division.
+constexpr int kNearThreads = 256, kNearRows = 32;
+
 template <typename T>
-__global__ void k_near_onthefly(int64_t n, const int32_t *__restrict__ row_off, const int32_t *__restrict__ cols,
-                                const T *__restrict__ cent, const T *__restrict__ areas, const T *__restrict__ sigma,
-                                const T *__restrict__ verts, int q, T ke, const T *__restrict__ v_far,
-                                T *__restrict__ v_out) {
-    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= n) return;
-    const T cx = cent[3 * i], cy = cent[3 * i + 1], cz = cent[3 * i + 2];
+__device__ __forceinline__ T near_rinv(T r2) {
+    if constexpr (sizeof(T) == 8) return rsqrt(r2 < 1e-24 ? 1e-24 : r2);
+    else return rsqrtf(r2 < 1e-24f ? 1e-24f : r2);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kNearThreads)
+    k_near_onthefly(int64_t n, const int32_t *__restrict__ row_off, const int32_t *__restrict__ cols,
+                    const T *__restrict__ cent, const T *__restrict__ areas, const T *__restrict__ sigma,
+                    const T *__restrict__ verts, int q, T ke, const T *__restrict__ v_far, T *__restrict__ v_out) {
+    __shared__ T delta[kNearThreads];
+    __shared__ int32_t rows[kNearRows + 1];  // row_off of this block's rows
+    const int64_t r0 = (int64_t)blockIdx.x * kNearRows;
+    const int nr = (int)(n - r0 < kNearRows ? n - r0 : kNearRows);
+    if (threadIdx.x <= nr) rows[threadIdx.x] = row_off[r0 + threadIdx.x];
+    __syncthreads();
+    const int kb = rows[0], kend = rows[nr];
     T acc = 0;
-    for (int k = row_off[i] + lane; k < row_off[i + 1]; k += 32) {
-        const int j = cols[k];
-        const T aj = areas[j], sj = sigma[j];
-        if (aj <= (T)0 || sj == (T)0) continue;
-        const T dx = cx - cent[3 * j], dy = cy - cent[3 * j + 1], dz = cz - cent[3 * j + 2];
-        T rf = sqrt(dx * dx + dy * dy + dz * dz);
-        rf = rf < (T)1e-12 ? (T)1e-12 : rf;
-        const T *v = verts + 9 * (int64_t)j;
-        const T e1x = v[3] - v[0], e1y = v[4] - v[1], e1z = v[5] - v[2];
-        const T e2x = v[6] - v[0], e2y = v[7] - v[1], e2z = v[8] - v[2];
-        T inear = 0;
-        for (int kk = 0; kk < q; ++kk) {
-            T u, w, wk;
-            if (q == 1) {
-                u = w = (T)(1.0 / 3.0);
-                wk = (T)1;
-            } else {
-                u = kk == 0 ? (T)(2.0 / 3.0) : (T)(1.0 / 6.0);
-                w = kk == 1 ? (T)(2.0 / 3.0) : (T)(1.0 / 6.0);
-                wk = (T)(1.0 / 3.0);
+    int tr = 0;  // summing thread: its row's position in the block's pair range
+    for (int base = kb; base < kend; base += kNearThreads) {
+        const int k = base + (int)threadIdx.x;
+        T d = 0;
+        if (k < kend) {
+            // the target row of pair k: the last row starting at or before k
+            int hi = nr - 1;
+            while (tr < hi) {
+                const int mid = (tr + hi + 1) >> 1;
+                if (rows[mid] <= k) tr = mid;
+                else hi = mid - 1;
             }
-            const T yx = v[0] + u * e1x + w * e2x, yy = v[1] + u * e1y + w * e2y, yz = v[2] + u * e1z + w * e2z;
-            const T ex = cx - yx, ey = cy - yy, ez = cz - yz;
-            T r = sqrt(ex * ex + ey * ey + ez * ez);
-            r = r < (T)1e-12 ? (T)1e-12 : r;
-            inear += (ke / r) * (wk * aj);
+            const int j = cols[k];
+            const T aj = areas[j], sj = sigma[j];
+            if (aj > (T)0 && sj != (T)0) {
+                const int64_t i = r0 + tr;
+                const T cx = cent[3 * i], cy = cent[3 * i + 1], cz = cent[3 * i + 2];
+                const T dx = cx - cent[3 * j], dy = cy - cent[3 * j + 1], dz = cz - cent[3 * j + 2];
+                const T rfi = near_rinv(dx * dx + dy * dy + dz * dz);
+                const T *v = verts + 9 * (int64_t)j;
+                const T v0x = v[0], v0y = v[1], v0z = v[2];
+                const T e1x = v[3] - v0x, e1y = v[4] - v0y, e1z = v[5] - v0z;
+                const T e2x = v[6] - v0x, e2y = v[7] - v0y, e2z = v[8] - v0z;
+                T inear = 0;
+                for (int kk = 0; kk < q; ++kk) {
+                    T u, w, wk;
+                    if (q == 1) {
+                        u = w = (T)(1.0 / 3.0);
+                        wk = (T)1;
+                    } else {
+                        u = kk == 0 ? (T)(2.0 / 3.0) : (T)(1.0 / 6.0);
+                        w = kk == 1 ? (T)(2.0 / 3.0) : (T)(1.0 / 6.0);
+                        wk = (T)(1.0 / 3.0);
+                    }
+                    const T ex = cx - (v0x + u * e1x + w * e2x), ey = cy - (v0y + u * e1y + w * e2y);
+                    const T ez = cz - (v0z + u * e1z + w * e2z);
+                    inear += ke * near_rinv(ex * ex + ey * ey + ez * ez) * (wk * aj);
+                }
+                d = sj * (inear - ke * aj * rfi);
+            }
         }
-        acc += sj * (inear - ke * aj / rf);
+        delta[threadIdx.x] = d;
+        __syncthreads();
+        if ((int)threadIdx.x < nr) {
+            const int lo = max(rows[threadIdx.x], base), hi = min(rows[threadIdx.x + 1], base + kNearThreads);
+            for (int kk = lo; kk < hi; ++kk) acc += delta[kk - base];
+        }
+        __syncthreads();
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) v_out[i] = v_far[i] + acc;
+    if ((int)threadIdx.x < nr) v_out[r0 + threadIdx.x] = v_far[r0 + threadIdx.x] + acc;
 }
 
 }  // namespace
@@ -671,11 +705,11 @@ EDFMM_API int edfmm_near_quadrature_matvec(const void *v_far_dev, const void *si
     if (quad_order > 2) return fail(EDFMM_ERR_UNSUPPORTED, "quad_order must be 1 or 2");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (dtype == EDFMM_F64)
-        k_near_onthefly<double><<<nb(n * 32, 128), 128, 0, s>>>(
+        k_near_onthefly<double><<<nb(n, kNearRows), kNearThreads, 0, s>>>(
             n, row_off_dev, cols_dev, (const double *)centroids_dev, (const double *)areas_dev, (const double *)sigma_dev,
             (const double *)panel_vertices_dev, q, k_e, (const double *)v_far_dev, (double *)v_out_dev);
     else
-        k_near_onthefly<float><<<nb(n * 32, 128), 128, 0, s>>>(
+        k_near_onthefly<float><<<nb(n, kNearRows), kNearThreads, 0, s>>>(
             n, row_off_dev, cols_dev, (const float *)centroids_dev, (const float *)areas_dev, (const float *)sigma_dev,
             (const float *)panel_vertices_dev, q, (float)k_e, (const float *)v_far_dev, (float *)v_out_dev);
     EDFMM_LAUNCH_CHECK("k_near_onthefly");

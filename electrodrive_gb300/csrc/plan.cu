@@ -268,24 +268,21 @@ int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int 
     int rc = upload_tables();
     if (rc) return rc;
     cudaStream_t s = S(stream);
-    const size_t esz_pt = (dtype == EDFMM_F64 ? 8 : 4) * 3;
     // every build below runs on `s`: temporaries are recycled in stream order
     BlockCacheScope cache_scope;
-    std::vector<DevTree> trees(n_instances);
-    std::vector<DevLists> lists(n_instances);
-    for (int i = 0; i < n_instances; ++i) {
-        const void *pts = static_cast<const char *>(points_dev) + esz_pt * offsets[i];
-        if ((rc = tree_build(pts, offsets[i + 1] - offsets[i], dtype, leaf_size, max_depth, trees[i], s))) return rc;
-        if ((rc = lists_build(trees[i], mac_theta, lists[i], s))) return rc;
-    }
+    // one forest over all instances, level by level (each instance's tree and
+    // lists equal what edfmm_plan_create builds for it alone)
     edfmm_plan *p = new edfmm_plan();
     cudaGetDevice(&p->device);
     p->mac_theta = mac_theta;
     p->leaf_size = leaf_size;
     p->max_depth = max_depth;
-    rc = pack_batch(trees, lists, dtype, p->tree, p->lists, s);
-    trees.clear();
-    lists.clear();
+    if (offsets[n_instances] >= (int64_t)INT32_MAX) {
+        delete p;
+        return fail(EDFMM_ERR_UNSUPPORTED, "batched plan exceeds 32-bit point indices");
+    }
+    rc = tree_build_forest(points_dev, offsets, n_instances, dtype, leaf_size, max_depth, p->tree, s);
+    if (!rc) rc = lists_build(p->tree, mac_theta, p->lists, s);
     if (!rc) rc = shrink_tree_lists(p->tree, p->lists, s);
     if (!rc) {
         p->fmm.p = expansion_order;
@@ -434,6 +431,10 @@ int edfmm_plan_set_launch(edfmm_plan *p, int knob, int value) {
         if (value != 0 && value != 1) return fail(EDFMM_ERR_ARG, "near-field overlap must be 0 or 1");
         p->fmm.near_overlap = value;
         return EDFMM_OK;
+    case EDFMM_LAUNCH_M2L_PACKED:
+        if (value != 0 && value != 1) return fail(EDFMM_ERR_ARG, "packed M2L must be 0 or 1");
+        p->fmm.m2l_packed = value;
+        return EDFMM_OK;
     default:
         return fail(EDFMM_ERR_ARG, "unknown launch knob");
     }
@@ -445,6 +446,7 @@ int edfmm_plan_get_launch(const edfmm_plan *p, int knob, int *value) {
     switch (knob) {
     case EDFMM_LAUNCH_M2L_TF_BLOCK: *value = p->fmm.m2l_tf_block; return EDFMM_OK;
     case EDFMM_LAUNCH_NEAR_OVERLAP: *value = p->fmm.near_overlap; return EDFMM_OK;
+    case EDFMM_LAUNCH_M2L_PACKED: *value = p->fmm.m2l_packed; return EDFMM_OK;
     default: return fail(EDFMM_ERR_ARG, "unknown launch knob");
     }
 }
@@ -716,6 +718,7 @@ int edfmm_targets_create(edfmm_plan *p, const void *targets_dev, int64_t m, void
     *out = nullptr;
     if (int rc = check_plan(p)) return rc;
     if (m < 0 || (m > 0 && !targets_dev)) return fail(EDFMM_ERR_ARG, "need m >= 0 target points");
+    if (p->tree.n_inst > 0) return fail(EDFMM_ERR_UNSUPPORTED, "batched plans have no two-tree lists");
     cudaStream_t s = S(stream);
     edfmm_targets *t = new edfmm_targets();
     t->plan = p;

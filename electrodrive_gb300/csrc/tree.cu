@@ -342,7 +342,8 @@ __global__ void __launch_bounds__(kChunk) k_copy_back(const int2 *rng, const int
 // children of split nodes -> next level
 __global__ void k_make_children(int K, const uint8_t *is_leaf, const int32_t *oct_start, const int32_t *oct_cnt,
                                 const int32_t *child_off, int level_base, int next_base, int2 *next_rng,
-                                int32_t *next_parent, int32_t *children_bfs) {
+                                int32_t *next_parent, int32_t *children_bfs, const int32_t *root,
+                                int32_t *next_root) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K) return;
     int j = child_off[i];
@@ -351,6 +352,7 @@ __global__ void k_make_children(int K, const uint8_t *is_leaf, const int32_t *oc
         if (!is_leaf[i] && c > 0) {
             next_rng[j] = make_int2(oct_start[8 * i + o], oct_start[8 * i + o] + c);
             next_parent[j] = level_base + i;
+            next_root[j] = root[i];
             children_bfs[8 * i + o] = next_base + j;
             ++j;
         } else {
@@ -376,11 +378,22 @@ __global__ void k_dfs_ids(const int2 *rng, const int32_t *lev, int64_t M, const 
     dfs[b] = base_at[s] + lev[b] - minlev_at[s];
 }
 
+// Floor of the expansion scale of each tree of the forest: 2^-40 of its
+// root's radius (1 for a root of radius 0); level 0 holds the roots.
+template <typename T>
+__global__ void k_root_floors(const typename Vec4<T>::type *root_cen, int K, T *floors) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const T r = root_cen[k].w;
+    floors[k] = r > (T)0 ? (T)(r * (T)9.094947017729282e-13) : (T)1;
+}
+
 template <typename T>
 __global__ void k_permute_nodes(int64_t M, const int32_t *dfs, const int2 *rng, const int32_t *lev,
                                 const int32_t *par_bfs, const int32_t *ch_bfs,
                                 const typename Vec4<T>::type *cen, const typename Vec4<T>::type *hal,
-                                const uint8_t *leaf, T scale_floor, int2 *o_rng, int32_t *o_lev, int32_t *o_par,
+                                const uint8_t *leaf, const int32_t *root, const T *floors, int2 *o_rng,
+                                int32_t *o_lev, int32_t *o_par,
                                 int32_t *o_ch, typename Vec4<T>::type *o_cen, typename Vec4<T>::type *o_hal,
                                 uint8_t *o_leaf, int32_t *level_nodes) {
     int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -395,7 +408,7 @@ __global__ void k_permute_nodes(int64_t M, const int32_t *dfs, const int2 *rng, 
     }
     o_cen[d] = cen[b];
     typename Vec4<T>::type h = hal[b];
-    T r = cen[b].w;
+    const T r = cen[b].w, scale_floor = floors[root[b]];
     h.w = r > scale_floor ? r : scale_floor;
     o_hal[d] = h;
     o_leaf[d] = leaf[b];
@@ -434,11 +447,22 @@ inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 template <typename T> struct Level {
     int K = 0;
     int base = 0;  // BFS id of the level's first node
-    DevBuf rng, parent, center, half, leaf, children;
+    DevBuf rng, parent, center, half, leaf, children, root;
 };
 
+__global__ void k_inst_node_off(const int32_t *level_nodes, int K, int32_t M, int32_t *off) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < K) off[k] = level_nodes[k];  // DFS id of root k
+    if (k == K) off[K] = M;
+}
+
+// A forest when inst_off (host, n_inst + 1 point offsets) is given: level 0
+// holds one root per instance over its rows, every later level the children
+// of all instances' split nodes, so each level is one set of launches for
+// the whole batch.  Each tree is the one a single build of its rows gives.
 template <typename T>
-int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, DevTree &tree, cudaStream_t s) {
+int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, DevTree &tree, cudaStream_t s,
+               const int64_t *inst_off, int n_inst) {
     using T4 = typename Vec4<T>::type;
     using O = typename OrdT<T>::type;
     int rc;
@@ -465,18 +489,26 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
 
     std::vector<Level<T>> levels;
     levels.emplace_back();
+    const int K0 = inst_off ? n_inst : 1;
+    std::vector<int2> h_r0(K0);
+    std::vector<int32_t> h_p0(K0, -1), h_root0(K0);
     {
         Level<T> &L0 = levels.back();
-        L0.K = 1;
+        L0.K = K0;
         L0.base = 0;
-        if ((rc = L0.rng.reserve(sizeof(int2))) || (rc = L0.parent.reserve(sizeof(int32_t)))) return rc;
-        int2 r0 = make_int2(0, (int)n);
-        int32_t p0 = -1;
-        EDFMM_CUDA_TRY(cudaMemcpyAsync(L0.rng.p, &r0, sizeof(int2), cudaMemcpyHostToDevice, s));
-        EDFMM_CUDA_TRY(cudaMemcpyAsync(L0.parent.p, &p0, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        if ((rc = L0.rng.reserve(sizeof(int2) * K0)) || (rc = L0.parent.reserve(sizeof(int32_t) * K0)) ||
+            (rc = L0.root.reserve(sizeof(int32_t) * K0)))
+            return rc;
+        for (int k = 0; k < K0; ++k) {
+            h_r0[k] = inst_off ? make_int2((int)inst_off[k], (int)inst_off[k + 1]) : make_int2(0, (int)n);
+            h_root0[k] = k;
+        }
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(L0.rng.p, h_r0.data(), sizeof(int2) * K0, cudaMemcpyHostToDevice, s));
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(L0.parent.p, h_p0.data(), sizeof(int32_t) * K0, cudaMemcpyHostToDevice, s));
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(L0.root.p, h_root0.data(), sizeof(int32_t) * K0, cudaMemcpyHostToDevice, s));
     }
     DevBuf cnt, off, chunk_node, bb, ccnt, oct_start, oct_cnt, nchild, child_off;
-    int64_t total_nodes = 1;
+    int64_t total_nodes = K0;  // the roots
     for (int lev = 0;; ++lev) {
         Level<T> &L = levels[lev];
         const int K = L.K;
@@ -534,12 +566,15 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
         next.K = (int)Kn;
         next.base = next_base;
         if (Kn > 0) {
-            if ((rc = next.rng.reserve(sizeof(int2) * Kn)) || (rc = next.parent.reserve(sizeof(int32_t) * Kn))) return rc;
+            if ((rc = next.rng.reserve(sizeof(int2) * Kn)) || (rc = next.parent.reserve(sizeof(int32_t) * Kn)) ||
+                (rc = next.root.reserve(sizeof(int32_t) * Kn)))
+                return rc;
         }
         k_make_children<<<nblk(K, 256), 256, 0, s>>>(K, dptr<uint8_t>(L.leaf), dptr<int32_t>(oct_start),
                                                      dptr<int32_t>(oct_cnt), dptr<int32_t>(child_off), L.base, next_base,
                                                      dptr<int2>(next.rng), dptr<int32_t>(next.parent),
-                                                     dptr<int32_t>(L.children));
+                                                     dptr<int32_t>(L.children), dptr<int32_t>(L.root),
+                                                     dptr<int32_t>(next.root));
         EDFMM_LAUNCH_CHECK("k_make_children");
         if (Kn == 0) break;
         total_nodes += Kn;
@@ -549,10 +584,11 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
     const int64_t M = total_nodes;
     const int nlev = (int)levels.size();
     // concatenate the levels (BFS order)
-    DevBuf b_rng, b_lev, b_par, b_ch, b_cen, b_hal, b_leaf;
+    DevBuf b_rng, b_lev, b_par, b_ch, b_cen, b_hal, b_leaf, b_root;
     if ((rc = b_rng.reserve(sizeof(int2) * M)) || (rc = b_lev.reserve(sizeof(int32_t) * M)) ||
         (rc = b_par.reserve(sizeof(int32_t) * M)) || (rc = b_ch.reserve(sizeof(int32_t) * 8 * M)) ||
-        (rc = b_cen.reserve(sizeof(T4) * M)) || (rc = b_hal.reserve(sizeof(T4) * M)) || (rc = b_leaf.reserve(M)))
+        (rc = b_cen.reserve(sizeof(T4) * M)) || (rc = b_hal.reserve(sizeof(T4) * M)) || (rc = b_leaf.reserve(M)) ||
+        (rc = b_root.reserve(sizeof(int32_t) * M)))
         return rc;
     std::vector<int32_t> hlev(M);
     tree.level_offsets.assign(nlev + 1, 0);
@@ -566,6 +602,8 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
         EDFMM_CUDA_TRY(cudaMemcpyAsync(dptr<T4>(b_cen) + b, L.center.p, sizeof(T4) * L.K, cudaMemcpyDeviceToDevice, s));
         EDFMM_CUDA_TRY(cudaMemcpyAsync(dptr<T4>(b_hal) + b, L.half.p, sizeof(T4) * L.K, cudaMemcpyDeviceToDevice, s));
         EDFMM_CUDA_TRY(cudaMemcpyAsync(dptr<uint8_t>(b_leaf) + b, L.leaf.p, L.K, cudaMemcpyDeviceToDevice, s));
+        EDFMM_CUDA_TRY(cudaMemcpyAsync(dptr<int32_t>(b_root) + b, L.root.p, sizeof(int32_t) * L.K,
+                                       cudaMemcpyDeviceToDevice, s));
         for (int i = 0; i < L.K; ++i) hlev[b + i] = l;
         tree.level_offsets[l + 1] = L.base + L.K;
     }
@@ -585,11 +623,11 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
     k_dfs_ids<<<nblk(M, 256), 256, 0, s>>>(dptr<int2>(b_rng), dptr<int32_t>(b_lev), M, dptr<int32_t>(base_at),
                                            dptr<int32_t>(minlev_at), dptr<int32_t>(dfs));
     EDFMM_LAUNCH_CHECK("k_dfs_ids");
-    // root radius sets the floor of the expansion scale
-    T4 root_c;
-    EDFMM_CUDA_TRY(cudaMemcpyAsync(&root_c, b_cen.p, sizeof(T4), cudaMemcpyDeviceToHost, s));
-    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
-    T floor_ = root_c.w > (T)0 ? (T)(root_c.w * (T)9.094947017729282e-13) : (T)1;  // 2^-40 of the root radius
+    // each root's radius sets the floor of its tree's expansion scales
+    DevBuf floors;
+    if ((rc = floors.reserve(sizeof(T) * K0))) return rc;
+    k_root_floors<T><<<nblk(K0, 256), 256, 0, s>>>(dptr<T4>(b_cen), K0, dptr<T>(floors));
+    EDFMM_LAUNCH_CHECK("k_root_floors");
     if ((rc = tree.range.reserve(sizeof(int2) * M)) || (rc = tree.level.reserve(sizeof(int32_t) * M)) ||
         (rc = tree.parent.reserve(sizeof(int32_t) * M)) || (rc = tree.children.reserve(sizeof(int32_t) * 8 * M)) ||
         (rc = tree.center.reserve(sizeof(T4) * M)) || (rc = tree.half.reserve(sizeof(T4) * M)) ||
@@ -597,7 +635,8 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
         return rc;
     k_permute_nodes<T><<<nblk(M, 256), 256, 0, s>>>(
         M, dptr<int32_t>(dfs), dptr<int2>(b_rng), dptr<int32_t>(b_lev), dptr<int32_t>(b_par), dptr<int32_t>(b_ch),
-        dptr<T4>(b_cen), dptr<T4>(b_hal), dptr<uint8_t>(b_leaf), floor_, dptr<int2>(tree.range), dptr<int32_t>(tree.level),
+        dptr<T4>(b_cen), dptr<T4>(b_hal), dptr<uint8_t>(b_leaf), dptr<int32_t>(b_root), dptr<T>(floors),
+        dptr<int2>(tree.range), dptr<int32_t>(tree.level),
         dptr<int32_t>(tree.parent), dptr<int32_t>(tree.children), dptr<T4>(tree.center), dptr<T4>(tree.half),
         dptr<uint8_t>(tree.is_leaf), dptr<int32_t>(tree.level_nodes));
     EDFMM_LAUNCH_CHECK("k_permute_nodes");
@@ -631,6 +670,15 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
     tree.n_leaves = nleaves;
     tree.max_level = nlev - 1;
     tree.depth_warnings = hwarn;
+    tree.n_inst = 0;
+    if (inst_off) {
+        // instance k owns the DFS range [root_k, root_{k+1}) (roots are BFS 0..K0-1)
+        tree.n_inst = K0;
+        if ((rc = tree.inst_node_off.reserve(sizeof(int32_t) * (K0 + 1)))) return rc;
+        k_inst_node_off<<<nblk(K0 + 1, 256), 256, 0, s>>>(dptr<int32_t>(tree.level_nodes), K0, (int32_t)M,
+                                                           dptr<int32_t>(tree.inst_node_off));
+        EDFMM_LAUNCH_CHECK("k_inst_node_off");
+    }
     return EDFMM_OK;
 }
 
@@ -638,8 +686,15 @@ int build_impl(const void *points_dev, int64_t n, int leaf_size, int max_depth, 
 
 int tree_build(const void *points_dev, int64_t n, int dtype, int leaf_size, int max_depth, DevTree &tree,
                cudaStream_t s) {
-    if (dtype == EDFMM_F64) return build_impl<double>(points_dev, n, leaf_size, max_depth, tree, s);
-    return build_impl<float>(points_dev, n, leaf_size, max_depth, tree, s);
+    if (dtype == EDFMM_F64) return build_impl<double>(points_dev, n, leaf_size, max_depth, tree, s, nullptr, 1);
+    return build_impl<float>(points_dev, n, leaf_size, max_depth, tree, s, nullptr, 1);
+}
+
+int tree_build_forest(const void *points_dev, const int64_t *inst_off, int n_inst, int dtype, int leaf_size,
+                      int max_depth, DevTree &tree, cudaStream_t s) {
+    const int64_t n = inst_off[n_inst];
+    if (dtype == EDFMM_F64) return build_impl<double>(points_dev, n, leaf_size, max_depth, tree, s, inst_off, n_inst);
+    return build_impl<float>(points_dev, n, leaf_size, max_depth, tree, s, inst_off, n_inst);
 }
 
 }  // namespace edfmm

@@ -105,9 +105,10 @@ EDFMM_API int edfmm_plan_create(const void *points_dev, int64_t n, int dtype, in
  * instance k at rows [offsets[k], offsets[k+1]) (offsets: host array of
  * n_instances + 1 values, offsets[0] = 0, every instance non-empty).  Each
  * instance gets the tree and lists edfmm_plan_create would build for it
- * alone; they are packed into one plan whose matvec is the block-diagonal
- * operator (no interaction between instances), one launch per stage for the
- * whole batch.
+ * alone, built for all instances together level by level (one forest, one
+ * set of launches per tree level and per list front); the plan's matvec is
+ * the block-diagonal operator (no interaction between instances), one launch
+ * per stage for the whole batch.
  */
 EDFMM_API int edfmm_plan_create_batch(const void *points_dev, const int64_t *offsets, int n_instances, int dtype,
                                       int leaf_size, int max_depth, double mac_theta, int expansion_order,
@@ -150,10 +151,14 @@ EDFMM_API int edfmm_plan_set_arithmetic(edfmm_plan *plan, int mode, void *stream
  * eight warps per SM, one instruction stream for the long pair code);
  * EDFMM_LAUNCH_NEAR_OVERLAP, 1 to run the near field on a second stream beside
  * the far-field chain, 0 for one fused pass after it.  Results are the same
- * either way (bit for bit).
+ * either way (bit for bit).  EDFMM_LAUNCH_M2L_PACKED (FP64 plans in two-float
+ * mode), 1 (the default) to run the two-float M2L's rotation matrices on
+ * packed FP32x2 instructions, two matrix rows per instruction, 0 for the
+ * scalar form; the results are the same bit for bit.
  */
 #define EDFMM_LAUNCH_M2L_TF_BLOCK 1
 #define EDFMM_LAUNCH_NEAR_OVERLAP 2
+#define EDFMM_LAUNCH_M2L_PACKED 3
 EDFMM_API int edfmm_plan_set_launch(edfmm_plan *plan, int knob, int value);
 EDFMM_API int edfmm_plan_get_launch(const edfmm_plan *plan, int knob, int *value);
 
@@ -445,7 +450,8 @@ EDFMM_API int edfmm_measure_fp32_peak(int iters, void *stream, double *tflops_ou
  * (zero for distances within the dtype's epsilon; far part as minus the
  * gradient of the local expansions), the FMM counterpart of the dense
  * bem_E_field_targets (electrodrive/core/bem_kernel.py:914).  The targets
- * object keeps a pointer to the plan, which must outlive it.
+ * object keeps a pointer to the plan, which must outlive it.  A batched plan
+ * (edfmm_plan_create_batch) has no targets: EDFMM_ERR_UNSUPPORTED.
  */
 typedef struct edfmm_targets edfmm_targets;
 EDFMM_API int edfmm_targets_create(edfmm_plan *plan, const void *targets_dev, int64_t m, void *stream,

@@ -130,6 +130,42 @@ def test_on_the_fly_module_matches_oracle(cuda_lib, oracle, order):
 
 
 @pytest.mark.gpu
+def test_on_the_fly_module_long_and_empty_rows(cuda_lib, oracle):
+    """Rows longer than one block's pair tile (999 pairs), empty rows, a block
+    boundary inside the pair list, the pair rows reused for the same tensor
+    and rebuilt after the tensor changes in place."""
+    from electrodrive_gb300.core.bem_near import apply_near_quadrature_matvec_cuda
+
+    rng = np.random.default_rng(11)
+    n = 1000
+    PV = rng.normal(size=(n, 3, 3)) * 0.05 + rng.uniform(-1, 1, size=(n, 1, 3))
+    C = PV.mean(axis=1)
+    A = 0.5 * np.linalg.norm(np.cross(PV[:, 1] - PV[:, 0], PV[:, 2] - PV[:, 0]), axis=1)
+    sig = rng.uniform(-1, 1, n)
+    rows = [np.stack([np.full(n - 1, 5), np.delete(np.arange(n), 5)], 1)]
+    for i in range(40, n, 3):  # every third row from 40 on: a few random sources
+        js = rng.choice(np.delete(np.arange(n), i), size=int(rng.integers(1, 12)), replace=False)
+        rows.append(np.stack([np.full(js.size, i), np.sort(js)], 1))
+    pairs = np.concatenate(rows).astype(np.int64)
+    w = oracle.near_weights(C, A, PV, pairs, 2, 0)
+    ref = np.zeros(n)
+    np.add.at(ref, pairs[:, 0], w * sig[pairs[:, 1]])
+    T = lambda x: torch.as_tensor(x, device="cuda")
+    vfar = T(rng.uniform(-1, 1, n))
+    pt = T(pairs[rng.permutation(pairs.shape[0])])
+    call = lambda p: apply_near_quadrature_matvec_cuda(vfar, T(sig), centroids=T(C), areas=T(A), panel_vertices=T(PV),
+                                                      near_pairs=p, quad_order=2).cpu().numpy()
+    i, j = pairs[:, 0], pairs[:, 1]
+    scale = np.zeros(n)
+    np.add.at(scale, i, K_E * A[j] * np.abs(sig[j]) / np.linalg.norm(C[i] - C[j], axis=1))
+    want = vfar.cpu().numpy() + ref
+    for _ in range(2):  # the second call reuses the rows of the same tensor
+        assert np.all(np.abs(call(pt) - want) <= 1e-12 * (scale + np.abs(want)) + 1e-300)
+    pt[:, 1] = pt[:, 0]  # in place: every pair becomes (i, i); the rows must be rebuilt
+    assert np.array_equal(call(pt), call(pt.clone()))
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", ["sphere_h05", "torus_h045_near"])
 def test_bem_solve_matches_reference_bem_solve(cuda_lib, name):
     from electrodrive_gb300.core.bem import bem_solve

@@ -62,6 +62,27 @@ def test_two_float_matvec_matches_fp64_and_oracle(cuda_lib, oracle, kind, n):
     assert np.linalg.norm(v2 - ref) <= 1e-11 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("order,block", [(6, 128), (7, 128), (8, 128), (8, 256)])
+def test_packed_and_scalar_two_float_m2l_are_bit_identical(cuda_lib, order, block):
+    """The two-float M2L with its rotation matrices on packed FP32x2
+    instructions (the default) and in scalar form give the same bits."""
+    from electrodrive_gb300._lib import Plan
+
+    pts = _points("clusters", 9000, 7)
+    n = pts.shape[0]
+    rng = np.random.default_rng(8)
+    T = lambda x: torch.as_tensor(x, dtype=torch.float64, device="cuda")
+    s, a = T(rng.uniform(-1, 1, n)), T(rng.uniform(0.5, 1.5, n) / n)
+    plan = Plan(T(pts), leaf_size=32, expansion_order=order)
+    plan.set_arithmetic("two_float")
+    plan.set_launch(m2l_tf_block=block)
+    out = {}
+    for packed in (1, 0):
+        plan.set_launch(m2l_packed=packed)
+        out[packed] = plan.matvec(s, a, None, k_e=1.0, flags=4)  # far field alone
+    assert torch.equal(out[0], out[1])
+
+
 def test_two_float_reference_pair_order_and_mode_switch(cuda_lib):
     from electrodrive_gb300._lib import EDFMM_REFERENCE_PAIR_ORDER, Plan
 

@@ -116,22 +116,56 @@ def test_training_lowers_the_loss(cuda_lib):
 @pytest.mark.gpu
 @pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained weights committed")
 def test_trained_network_against_the_cold_start(cuda_lib):
-    """Held-out geometries (seeds the training never used).  What the network
-    gains: a start far closer to the converged density than the cold start
-    (b / I_self) and than the base guess it corrects (b / A(1)).  What GMRES
-    gains from that is small on these Jacobi-preconditioned systems (the first
-    iterations remove the smooth error the network predicts, and the rest of
-    the iterations go to the rest of the spectrum), so the iteration check is
-    "no worse".  Every start reaches the same true residual."""
+    """Held-out geometries (seeds the training never used) of 10k-20k panels
+    on the FMM operator.  What the network gains: a start far closer to the
+    converged density than the cold start (b / I_self) and than the base
+    guess it corrects (b / A(1)), and from it fewer FP64 refinement steps of
+    the mixed FP32/FP64 solver (the cold start needs two on every geometry,
+    the learned start one: 2.0 against 1.01 on the 100 held-out geometries of
+    the training report).  Plain Jacobi GMRES iterations barely move on these
+    systems (the first iterations remove the smooth error the network
+    predicts, the rest go to the rest of the spectrum), so they are only
+    checked to converge.  Every start reaches the same true residual."""
     from electrodrive_gb300.core.warm_start import KINDS, PointCloudNet, compare_starts, make_sample, random_case
 
     net = PointCloudNet.load(WEIGHTS)
     rng = np.random.default_rng(987654)
-    res = [compare_starts(net, make_sample(*random_case(rng, KINDS[i % 4], 3000))) for i in range(8)]
+    res = []
+    for i in range(8):
+        mesh, spec = random_case(rng, KINDS[i % 4], int(rng.integers(10000, 20000)))
+        res.append(compare_starts(net, make_sample(mesh, spec, operator="fmm")))
     for r in res:
         for k in ("cold", "base", "learned"):
             assert r[k]["code"] == 0 and r[k]["rel_resid"] <= 1e-6 * (1 + 1e-9)
+            m = r[k]["mixed"]
+            assert m["code"] == 0 and m["rel_resid"] <= 1e-6 * (1 + 1e-9), (k, m)
     err = {k: np.mean([r[k]["start_error"] for r in res]) for k in ("cold", "base", "learned")}
-    its = {k: np.mean([r[k]["iters"] for r in res]) for k in ("cold", "base", "learned")}
+    outer = {k: np.mean([r[k]["mixed"]["outer"] for r in res]) for k in ("cold", "base", "learned")}
+    fp64 = {k: np.mean([r[k]["mixed"]["fp64_matvecs"] for r in res]) for k in ("cold", "base", "learned")}
     assert err["learned"] < 0.5 * err["base"] and err["learned"] < 0.01 * err["cold"], err
-    assert its["learned"] <= its["cold"] + 2, its
+    assert outer["learned"] <= outer["cold"] - 0.75 and outer["learned"] <= outer["base"], outer
+    assert fp64["learned"] <= fp64["cold"] - 0.75 and fp64["learned"] <= fp64["base"], fp64
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained weights committed")
+def test_bem_solve_with_the_learned_start(cuda_lib):
+    """bem_solve(mixed=True, warm_start=net): the same density as the cold
+    mixed solve (both stop at a 1e-6 relative FP64 residual) in fewer
+    refinement steps."""
+    from electrodrive_gb300.core.bem import bem_solve
+    from electrodrive_gb300.core.warm_start import PointCloudNet, random_case
+    from electrodrive_gb300.utils.config import BEMConfig
+
+    net = PointCloudNet.load(WEIGHTS)
+    mesh, spec = random_case(np.random.default_rng(4242), "torus", 12000)
+    kw = dict(mesh=mesh, operator="fmm", self_integral="quadrature", mixed=True, mixed_rtol=1e-6)
+    cold = bem_solve(spec, BEMConfig(), **kw)
+    learned = bem_solve(spec, BEMConfig(), warm_start=net, **kw)
+    for r in (cold, learned):
+        assert "error" not in r and r["gmres_stats"]["precision"] == "mixed", r.get("error")
+    a, c = np.asarray(mesh.areas), np.asarray(cold["surface_charge_density"])
+    d = np.asarray(learned["surface_charge_density"]) - c
+    assert np.sqrt((a * d * d).sum() / (a * c * c).sum()) < 1e-4
+    assert learned["gmres_stats"]["outer"] < cold["gmres_stats"]["outer"], (learned["gmres_stats"]["outer"],
+                                                                            cold["gmres_stats"]["outer"])
