@@ -73,11 +73,12 @@ M2L_FLOPS_PER_PAIR = m2l_flops_per_pair(8)
 # taken from an ncu capture of k_m2l_rot<float, 8> at N = 262,144 (44.54 MB read
 # for 9,091,877 pairs)
 M2L_DRAM_BYTES_PER_PAIR = 44.54e6 / 9_091_877
-# DRAM bytes per M2L pair of k_m2l_rot<float, p> on the 200,000-panel torus
-# (FP32 inner operator), from ncu captures of that kernel on that mesh
-M2L_DRAM_BYTES_PER_PAIR_TORUS = {8: 14_461_269 / 2_315_072}
+# DRAM bytes (read + write) per M2L pair of k_m2l_rot<float, p> on the
+# 200,000-panel torus (FP32 inner operator), from ncu captures of that kernel
+# on that mesh (median over the profile run's launches)
+M2L_DRAM_BYTES_PER_PAIR_TORUS = {8: 14_461_269 / 2_315_072, 6: 12_600_576 / 2_315_072}
 # the same for the 256-dimer batch (FP32 inner operator, autotuned order)
-M2L_DRAM_BYTES_PER_PAIR_BATCH = {}
+M2L_DRAM_BYTES_PER_PAIR_BATCH = {6: (244_023_808 + 55_725_312) / 39_011_439}
 # DRAM bytes of one k_dense_partial<double> launch at n = 5,120 (ncu capture)
 DENSE_DRAM_BYTES_PER_MATVEC_5120 = 293_120
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
