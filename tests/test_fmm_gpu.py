@@ -46,7 +46,8 @@ def test_p2p_matches_reference_potentials(cuda_lib, path):
     assert rel(phi, ref) < tol
 
 
-@pytest.mark.parametrize("n,p", [(5000, 8), (20000, 8), (8000, 4), (6000, 6), (4000, 10), (3000, 1)])
+@pytest.mark.parametrize("n,p", [(5000, 8), (20000, 8), (8000, 4), (6000, 6), (4000, 10), (3000, 1), (7000, 7),
+                                 (5000, 5), (3000, 2), (4000, 3)])
 def test_matvec_matches_oracle_fmm_fp32(cuda_lib, oracle, n, p):
     rng = np.random.default_rng(n + p)
     pts = rng.random((n, 3)).astype(np.float32)
@@ -72,7 +73,7 @@ def _torus_points(n_u, n_v):
     return np.stack([x, y, z], -1).reshape(-1, 3)
 
 
-@pytest.mark.parametrize("p", [3, 6, 8])
+@pytest.mark.parametrize("p", [3, 6, 7, 8])
 @pytest.mark.parametrize("kind", ["cube", "torus"])
 def test_matvec_fp64_plan_matches_oracle(cuda_lib, oracle, p, kind):
     rng = np.random.default_rng(11 + p)
