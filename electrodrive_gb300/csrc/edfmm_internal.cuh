@@ -253,6 +253,10 @@ struct DevLists {
     int64_t max_p2p_row = 0, max_m2l_row = 0;
     DevBuf p2p_off, p2p_src;  // CSR by target, sources ascending
     DevBuf m2l_off, m2l_src;
+    // the target tree's leaves in decreasing near-field work (sum over the
+    // leaf's P2P sources of n_source * n_target): the near-field kernel takes
+    // them in this order, so that its last wave holds the short leaves
+    DevBuf p2p_leaves;
     // transposed M2L CSR (rows = listed sources), built on demand for the
     // reference's swapped pair order
     bool have_m2l_swapped = false;

@@ -17,6 +17,8 @@
 // The output is stored as CSR rows by target with sources ascending, i.e.
 // the reference's (tgt, src) sort order (interaction_lists.py:474-485).
 #include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include "edfmm_internal.cuh"
 
@@ -216,6 +218,54 @@ __global__ void k_root_pairs(const int32_t *level_nodes, int K, int2 *front) {
     if (k < K) front[k] = make_int2(level_nodes[k], level_nodes[k]);
 }
 
+// near-field work of each target leaf: (sum of its P2P sources' points) x its
+// points, plus one for the epilogue of a leaf without sources
+__global__ void k_leaf_work(const int32_t *__restrict__ leaves, int64_t nl, const int32_t *__restrict__ off,
+                            const int32_t *__restrict__ src, const int2 *__restrict__ trange,
+                            const int2 *__restrict__ srange, int64_t *__restrict__ work) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nl) return;
+    const int t = leaves[i];
+    int64_t w = 0;
+    for (int k = off[t]; k < off[t + 1]; ++k) {
+        const int2 r = srange[src[k]];
+        w += r.y - r.x;
+    }
+    work[i] = w * (int64_t)(trange[t].y - trange[t].x) + 1;
+}
+
+// L.p2p_leaves: the target tree's leaves by decreasing work, in 64 buckets of
+// log2(work) in quarter steps (a counting sort; leaves keep their tree order
+// within a bucket, so the order is deterministic)
+int order_p2p_leaves(const DevTree &tree, const DevTree &stree, DevLists &L, cudaStream_t s) {
+    const int64_t nl = tree.n_leaves;
+    if (nl <= 0) return EDFMM_OK;
+    int rc;
+    DevBuf work;
+    if ((rc = work.reserve(sizeof(int64_t) * nl)) || (rc = L.p2p_leaves.reserve(sizeof(int32_t) * nl))) return rc;
+    k_leaf_work<<<nblk(nl, 256), 256, 0, s>>>(dptr<int32_t>(tree.leaves), nl, dptr<int32_t>(L.p2p_off),
+                                              dptr<int32_t>(L.p2p_src), dptr<int2>(tree.range), dptr<int2>(stree.range),
+                                              dptr<int64_t>(work));
+    EDFMM_LAUNCH_CHECK("k_leaf_work");
+    std::vector<int64_t> w(nl);
+    std::vector<int32_t> leaves(nl), order(nl);
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(w.data(), work.p, sizeof(int64_t) * nl, cudaMemcpyDeviceToHost, s));
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(leaves.data(), tree.leaves.p, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    constexpr int kBuckets = 256;
+    auto bucket = [](int64_t v) {
+        const int b = (int)std::floor(4.0 * std::log2((double)v));
+        return kBuckets - 1 - std::min(std::max(b, 0), kBuckets - 1);  // decreasing work
+    };
+    std::vector<int64_t> start(kBuckets + 1, 0);
+    for (int64_t i = 0; i < nl; ++i) ++start[bucket(w[i]) + 1];
+    for (int b = 0; b < kBuckets; ++b) start[b + 1] += start[b];
+    for (int64_t i = 0; i < nl; ++i) order[start[bucket(w[i])]++] = leaves[i];
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(L.p2p_leaves.p, order.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return EDFMM_OK;
+}
+
 template <typename T>
 int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists &L, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
@@ -296,7 +346,7 @@ int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists
     EDFMM_CUDA_TRY(cudaMemcpyAsync(&hi, acc.p, sizeof(hi), cudaMemcpyDeviceToHost, s));
     EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
     L.p2p_interactions = (int64_t)hi;
-    return EDFMM_OK;
+    return order_p2p_leaves(tree, stree, L, s);
 }
 
 }  // namespace

@@ -536,7 +536,7 @@ int near_impl(const DevTree &tree, const DevLists &lists, const FmmBuffers &buf,
     using T4 = typename Vec4<T>::type;
     if (tree.n_leaves == 0) return EDFMM_OK;
     NearParams<T> P;
-    P.leaves = dptr<int32_t>(tree.leaves);
+    P.leaves = lists.p2p_leaves.p ? dptr<int32_t>(lists.p2p_leaves) : dptr<int32_t>(tree.leaves);
     P.n_leaves = tree.n_leaves;
     P.off = dptr<int32_t>(lists.p2p_off);
     P.src = dptr<int32_t>(lists.p2p_src);
