@@ -257,6 +257,10 @@ struct DevLists {
     // leaf's P2P sources of n_source * n_target): the near-field kernel takes
     // them in this order, so that its last wave holds the short leaves
     DevBuf p2p_leaves;
+    // the target tree's nodes by decreasing M2L pair count: the M2L kernels
+    // give warp w row m2l_rows[w], so that a block's warps (which run their
+    // rounds of pairs together) hold rows of similar length
+    DevBuf m2l_rows;
     // transposed M2L CSR (rows = listed sources), built on demand for the
     // reference's swapped pair order
     bool have_m2l_swapped = false;
@@ -307,14 +311,16 @@ int run_p2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2m(const DevTree &tree, FmmBuffers &buf, cudaStream_t s);
 int run_m2l(const DevTree &tree, const DevLists &lists, FmmBuffers &buf, bool swapped, cudaStream_t s);
 // rotation-based M2L (m2l_rot.cu, kernels in m2l_rot.cuh), orders 1..8, FP32 and FP64
-int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
+int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows,
+                   const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s);
 // the same in two-float arithmetic for FP64 plans, orders 6..8
 // (EDFMM_ERR_UNSUPPORTED for other orders, launching nothing): node geometry
 // and multipoles split into (hi, lo) FP32 pairs (tnodes / snodes: 2 float4
 // per node; Mx: one float4 per complex coefficient), locals written as FP64
-int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows,
+                      const void *tnodes, const void *thal,
                       const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                       int block, bool packed, cudaStream_t s);
 int run_m2l_two(const DevTree &tgt_tree, const DevTree &src_tree, const DevLists &lists, const FmmBuffers &src_buf,

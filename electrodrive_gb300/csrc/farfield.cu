@@ -929,6 +929,7 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
     if (M == 0 || stree.n_nodes == 0) return EDFMM_OK;
     const int32_t *off = swapped ? dptr<int32_t>(lists.m2l_swapped_off) : dptr<int32_t>(lists.m2l_off);
     const int32_t *src = swapped ? dptr<int32_t>(lists.m2l_swapped_src) : dptr<int32_t>(lists.m2l_src);
+    const int32_t *rows = swapped ? nullptr : dptr<int32_t>(lists.m2l_rows);
     if (buf.p > kRotPMaxUsed) {
         // orders above 8: the shared-memory kernel (scales by the larger radius)
         k_m2l_generic<T><<<nblk(M, 4), 128, 0, s>>>(M, nullptr, off, src, dptr<T4>(tree.center), dptr<T4>(tree.half),
@@ -947,14 +948,14 @@ int m2l_impl(const DevTree &tree, const DevTree &stree, const DevLists &lists, c
         const int64_t nq = stree.n_nodes * (int64_t)sbuf.nc_pad;
         k_split_coeffs<<<nblk(nq, 256), 256, 0, s>>>(dptr<double2>(sbuf.multipoles), nq, dptr<float4>(sbuf.mult_tf));
         EDFMM_LAUNCH_CHECK("k_split_coeffs");
-        int rc = launch_m2l_rot_tf(buf.p, M, off, src, tree.nodes_tf.p, tree.half.p, stree.nodes_tf.p, stree.half.p,
+        int rc = launch_m2l_rot_tf(buf.p, M, off, src, rows, tree.nodes_tf.p, tree.half.p, stree.nodes_tf.p, stree.half.p,
                                    sbuf.mult_tf.p, buf.locals.p, buf.nc_pad, buf.mask, buf.m2l_tf_block,
                                    buf.m2l_packed != 0, s);
         if (rc == EDFMM_OK) two_float = true;
         else if (rc != EDFMM_ERR_UNSUPPORTED) return rc;
     }
     if (!two_float) {
-        if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, tree.center.p,
+        if (int rc = launch_m2l_rot(sizeof(T) == 8 ? EDFMM_F64 : EDFMM_F32, buf.p, M, off, src, rows, tree.center.p,
                                     tree.half.p, stree.center.p, stree.half.p, sbuf.multipoles.p, buf.locals.p,
                                     buf.nc_pad, buf.mask, s))
             return rc;

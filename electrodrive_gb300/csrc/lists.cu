@@ -266,6 +266,27 @@ int order_p2p_leaves(const DevTree &tree, const DevTree &stree, DevLists &L, cud
     return EDFMM_OK;
 }
 
+// L.m2l_rows: the target tree's nodes by decreasing M2L pair count (a
+// counting sort on the count; nodes keep their DFS order within a count)
+int order_m2l_rows(const DevTree &tree, DevLists &L, cudaStream_t s) {
+    const int64_t M = tree.n_nodes;
+    if (M <= 0) return EDFMM_OK;
+    int rc;
+    if ((rc = L.m2l_rows.reserve(sizeof(int32_t) * M))) return rc;
+    std::vector<int32_t> off(M + 1), order(M);
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(off.data(), L.m2l_off.p, sizeof(int32_t) * (M + 1), cudaMemcpyDeviceToHost, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t top = 0;
+    for (int64_t t = 0; t < M; ++t) top = std::max<int64_t>(top, off[t + 1] - off[t]);
+    std::vector<int64_t> start(top + 2, 0);  // bucket b = top - count
+    for (int64_t t = 0; t < M; ++t) ++start[top - (off[t + 1] - off[t]) + 1];
+    for (int64_t b = 0; b <= top; ++b) start[b + 1] += start[b];
+    for (int64_t t = 0; t < M; ++t) order[start[top - (off[t + 1] - off[t])]++] = (int32_t)t;
+    EDFMM_CUDA_TRY(cudaMemcpyAsync(L.m2l_rows.p, order.data(), sizeof(int32_t) * M, cudaMemcpyHostToDevice, s));
+    EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return EDFMM_OK;
+}
+
 template <typename T>
 int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists &L, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
@@ -346,7 +367,8 @@ int lists_impl(const DevTree &stree, const DevTree &tree, double theta, DevLists
     EDFMM_CUDA_TRY(cudaMemcpyAsync(&hi, acc.p, sizeof(hi), cudaMemcpyDeviceToHost, s));
     EDFMM_CUDA_TRY(cudaStreamSynchronize(s));
     L.p2p_interactions = (int64_t)hi;
-    return order_p2p_leaves(tree, stree, L, s);
+    if ((rc = order_p2p_leaves(tree, stree, L, s))) return rc;
+    return order_m2l_rows(tree, L, s);
 }
 
 }  // namespace

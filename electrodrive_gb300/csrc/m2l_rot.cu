@@ -8,26 +8,28 @@ namespace edfmm {
 // scale above 256x the target's are left to the caller's generic kernel).
 // Rows of instances inactive under ``mask`` are skipped (their locals are
 // left as they were).
-int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const void *tcen,
+int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows,
+                   const void *tcen,
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s) {
     if (M <= 0) return EDFMM_OK;
-    return dtype == EDFMM_F64 ? m2l_rot_f64(p, M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s)
-                              : m2l_rot_f32(p, M, off, src, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
+    return dtype == EDFMM_F64 ? m2l_rot_f64(p, M, off, src, rows, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s)
+                              : m2l_rot_f32(p, M, off, src, rows, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
 }
 
 // Two-float M2L of an FP64 plan (orders 6..8); returns EDFMM_ERR_UNSUPPORTED
 // for other orders (the caller then runs the FP64 kernel).
-int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+int launch_m2l_rot_tf(int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows,
+                      const void *tnodes, const void *thal,
                       const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                       int block, bool packed, cudaStream_t s) {
     if (M <= 0) return EDFMM_OK;
     switch (p) {
-        case 6: return m2l_rot_tf6(packed, M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
-        case 7: return m2l_rot_tf7(packed, M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
+        case 6: return m2l_rot_tf6(packed, M, off, src, rows, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
+        case 7: return m2l_rot_tf7(packed, M, off, src, rows, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
         case 8:
-            return block == 256 ? m2l_rot_tf8w(packed, M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s)
-                                : m2l_rot_tf8(packed, M, off, src, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
+            return block == 256 ? m2l_rot_tf8w(packed, M, off, src, rows, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s)
+                                : m2l_rot_tf8(packed, M, off, src, rows, tnodes, thal, snodes, hal, Mx, Lx, nc_pad, mask, s);
         default: return EDFMM_ERR_UNSUPPORTED;
     }
 }

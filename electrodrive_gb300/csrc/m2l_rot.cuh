@@ -441,6 +441,7 @@ __host__ __device__ constexpr bool pk_started(int I) {
 template <typename T, int P, bool V_IN_SMEM>
 __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? (rot_binomial<T, P>() ? 4 : 3) : 1)
     k_m2l_rot(int64_t n_nodes, const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+              const int32_t *__restrict__ rows,
               const typename Vec4<T>::type *__restrict__ tcenter, const typename Vec4<T>::type *__restrict__ thalf,
               const typename Vec4<T>::type *__restrict__ center, const typename Vec4<T>::type *__restrict__ half,
               const typename Vec2<T>::type *__restrict__ Mexp, typename Vec2<T>::type *__restrict__ Lexp,
@@ -451,7 +452,9 @@ __global__ void __launch_bounds__(kRotThreads, sizeof(T) == 4 ? (rot_binomial<T,
     __shared__ int max_rounds;
     T2 *sq = reinterpret_cast<T2 *>(rot_smem);
     AccC<T, NT> acc{sq + threadIdx.x};
-    const int64_t t = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+    // warp w takes target row rows[w] (rows by decreasing pair count), or row w
+    const int64_t w = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+    const int64_t t = rows && w < n_nodes ? (int64_t)rows[w] : w;
     const int lane = threadIdx.x & 31;
     const bool live = t < n_nodes && inst_active(mask, (int)t);
     typename Vec4<T>::type ct{};
@@ -817,6 +820,7 @@ __device__ __forceinline__ void rot_pair_tf(V &v, const float4 *__restrict__ Mro
 template <int P, int NT, bool PK>
 __global__ void __launch_bounds__(NT, 256 / NT)
     k_m2l_rot_tf(int64_t n_nodes, const int32_t *__restrict__ off, const int32_t *__restrict__ src,
+                 const int32_t *__restrict__ rows,
                  const float4 *__restrict__ tnodes, const double4 *__restrict__ thalf,
                  const float4 *__restrict__ snodes, const double4 *__restrict__ half,
                  const float4 *__restrict__ Mexp, double2 *__restrict__ Lexp, int nc_pad, const InstMask mask) {
@@ -830,7 +834,9 @@ __global__ void __launch_bounds__(NT, 256 / NT)
     VS v;
     if constexpr (PK) v = VS{slots_hi + threadIdx.x, slots_lo + threadIdx.x};
     else v = VS{slots + threadIdx.x};
-    const int64_t t = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+    // warp w takes target row rows[w] (rows by decreasing pair count), or row w
+    const int64_t w = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+    const int64_t t = rows && w < n_nodes ? (int64_t)rows[w] : w;
     const int lane = threadIdx.x & 31;
     const int wbase = threadIdx.x & ~31;
     const bool live = t < n_nodes && inst_active(mask, (int)t);
@@ -922,7 +928,8 @@ __global__ void __launch_bounds__(NT, 256 / NT)
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <int P, int NT, bool PK>
-int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void *tnodes, const void *thal,
+int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *tnodes,
+                  const void *thal,
                   const void *snodes, const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                   cudaStream_t s) {
     constexpr int NV = (P + 1) * (P + 1);
@@ -932,7 +939,7 @@ int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void 
     if (attr != cudaSuccess)
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot_tf shared memory attribute: ") + cudaGetErrorString(attr));
     k_m2l_rot_tf<P, NT, PK><<<nblk(M * 32, NT), NT, smem, s>>>(
-        M, off, src, static_cast<const float4 *>(tnodes), static_cast<const double4 *>(thal),
+        M, off, src, rows, static_cast<const float4 *>(tnodes), static_cast<const double4 *>(thal),
         static_cast<const float4 *>(snodes), static_cast<const double4 *>(hal), static_cast<const float4 *>(Mx),
         static_cast<double2 *>(Lx), nc_pad, mask);
     EDFMM_LAUNCH_CHECK("k_m2l_rot_tf");
@@ -940,7 +947,8 @@ int launch_rot_tf(int64_t M, const int32_t *off, const int32_t *src, const void 
 }
 
 template <typename T, int P, bool V_IN_SMEM>
-int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tcen, const void *thal, const void *cen,
+int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *tcen,
+               const void *thal, const void *cen,
                const void *hal, const void *Mx, void *Lx, int nc_pad, const InstMask &mask, cudaStream_t s) {
     using T4 = typename Vec4<T>::type;
     using T2 = typename Vec2<T>::type;
@@ -951,7 +959,7 @@ int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tc
     if (attr != cudaSuccess)
         return fail(EDFMM_ERR_CUDA, std::string("k_m2l_rot shared memory attribute: ") + cudaGetErrorString(attr));
     k_m2l_rot<T, P, V_IN_SMEM><<<nblk(M * 32, NT), NT, smem, s>>>(
-        M, off, src, static_cast<const T4 *>(tcen), static_cast<const T4 *>(thal), static_cast<const T4 *>(cen),
+        M, off, src, rows, static_cast<const T4 *>(tcen), static_cast<const T4 *>(thal), static_cast<const T4 *>(cen),
         static_cast<const T4 *>(hal), static_cast<const T2 *>(Mx), static_cast<T2 *>(Lx), nc_pad, mask);
     EDFMM_LAUNCH_CHECK("k_m2l_rot");
     return EDFMM_OK;
@@ -965,22 +973,22 @@ int launch_rot(int64_t M, const int32_t *off, const int32_t *src, const void *tc
 // source halves) and two-float orders 6, 7 and 8 with 128 or 256 threads
 // (m2l_rot_tf*.cu; a..d = target nodes, target halves, source nodes, source
 // halves).
-int m2l_rot_f32(int p, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_f32(int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
-int m2l_rot_f64(int p, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_f64(int p, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
-int m2l_rot_tf6(bool packed, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_tf6(bool packed, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
-int m2l_rot_tf7(bool packed, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_tf7(bool packed, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
-int m2l_rot_tf8(bool packed, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_tf8(bool packed, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
-int m2l_rot_tf8w(bool packed, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_tf8w(bool packed, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s);
 

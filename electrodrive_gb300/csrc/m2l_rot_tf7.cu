@@ -3,11 +3,11 @@
 
 namespace edfmm {
 
-int m2l_rot_tf7(bool packed, int64_t M, const int32_t *off, const int32_t *src, const void *a, const void *b,
+int m2l_rot_tf7(bool packed, int64_t M, const int32_t *off, const int32_t *src, const int32_t *rows, const void *a, const void *b,
                 const void *c, const void *d, const void *Mx, void *Lx, int nc_pad, const InstMask &mask,
                 cudaStream_t s) {
-    return packed ? launch_rot_tf<7, 128, true>(M, off, src, a, b, c, d, Mx, Lx, nc_pad, mask, s)
-                  : launch_rot_tf<7, 128, false>(M, off, src, a, b, c, d, Mx, Lx, nc_pad, mask, s);
+    return packed ? launch_rot_tf<7, 128, true>(M, off, src, rows, a, b, c, d, Mx, Lx, nc_pad, mask, s)
+                  : launch_rot_tf<7, 128, false>(M, off, src, rows, a, b, c, d, Mx, Lx, nc_pad, mask, s);
 }
 
 }  // namespace edfmm

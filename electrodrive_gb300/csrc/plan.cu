@@ -123,7 +123,7 @@ int shrink_tree_lists(DevTree &t, DevLists &l, cudaStream_t s) {
     DevBuf *bufs[] = {&t.pts,      &t.index_map,     &t.center,      &t.half,    &t.range,
                       &t.parent,   &t.children,      &t.level,       &t.is_leaf, &t.leaves,
                       &t.level_nodes, &t.inst_node_off, &l.p2p_off,  &l.p2p_src, &l.m2l_off,
-                      &l.m2l_src,  &l.m2l_swapped_off, &l.m2l_swapped_src, &l.p2p_leaves};
+                      &l.m2l_src,  &l.m2l_swapped_off, &l.m2l_swapped_src, &l.p2p_leaves, &l.m2l_rows};
     for (DevBuf *b : bufs)
         if (int rc = b->shrink_to_fit(s)) return rc;
     return EDFMM_OK;
@@ -347,10 +347,10 @@ int edfmm_plan_convert(const edfmm_plan *src, int dtype, int expansion_order, vo
     if (!rc) rc = cast_buf(a.half, a.dtype, t.half, dtype, 4 * a.n_nodes, s);
     const DevBuf *from[] = {&a.index_map, &a.range, &a.parent, &a.children, &a.level, &a.is_leaf, &a.leaves,
                             &a.level_nodes, &a.inst_node_off, &la.p2p_off, &la.p2p_src, &la.m2l_off, &la.m2l_src,
-                            &la.m2l_swapped_off, &la.m2l_swapped_src, &la.p2p_leaves};
+                            &la.m2l_swapped_off, &la.m2l_swapped_src, &la.p2p_leaves, &la.m2l_rows};
     DevBuf *to[] = {&t.index_map, &t.range, &t.parent, &t.children, &t.level, &t.is_leaf, &t.leaves,
                     &t.level_nodes, &t.inst_node_off, &l.p2p_off, &l.p2p_src, &l.m2l_off, &l.m2l_src,
-                    &l.m2l_swapped_off, &l.m2l_swapped_src, &l.p2p_leaves};
+                    &l.m2l_swapped_off, &l.m2l_swapped_src, &l.p2p_leaves, &l.m2l_rows};
     for (size_t i = 0; !rc && i < sizeof(from) / sizeof(from[0]); ++i) rc = clone_buf(*from[i], *to[i], s);
     if (!rc) rc = alloc_expansions(p, dtype, expansion_order, s);  // synchronises the stream
     if (rc) {
