@@ -55,7 +55,11 @@ def bc_vector(spec: Any, mesh: TriMesh) -> np.ndarray:
         except Exception:
             v = 0.0
         id_to_v[int(_cget(c, "id", i))] = v
-    return np.asarray([id_to_v.get(int(cid), 0.0) for cid in mesh.conductor_ids], dtype=np.float64)
+    ids = np.asarray(mesh.conductor_ids).astype(np.int64, copy=False)
+    out = np.zeros(ids.shape[0], dtype=np.float64)  # panels of unknown conductors: 0
+    for cid, v in id_to_v.items():
+        out[ids == cid] = v
+    return out
 
 
 def point_charges(spec: Any) -> List[Tuple[float, Tuple[float, float, float]]]:
@@ -528,7 +532,8 @@ def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: T
     """The FP32 FMM operator for the inner solves of iterative refinement:
     among expansion orders, leaf sizes and launch shapes (near field beside
     the far field or fused after it), the fastest whose output on a fixed
-    random density is within ``max_rel_error`` of ``op64``'s (the FP32
+    random density is within ``max_rel_error`` of ``op64``'s (of candidates
+    within 5% of the fastest, the most accurate; the FP32
     operator at p = 8 is about 2e-7 away; looser operators make the first
     refinement step fall short of 1e-6).  ``near`` is the FP32 near
     correction the operator adds.  The choice is kept in the autotune cache
@@ -582,7 +587,7 @@ def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: T
             if err <= max_rel_error:
                 return op, [dict(leaf_size=int(c["leaf_size"]), expansion_order=int(c["expansion_order"]),
                                  launch=dict(rec.get("launch", {})), ms=t, rel_error=err, from_cache=True)]
-    trials, best = [], None
+    trials, ops = [], {}
     for leaf in leaf_sizes:
         for p in orders:
             op = make(leaf, p)
@@ -590,11 +595,14 @@ def autotune_inner_operator(op64, centroids: Tensor, areas: Tensor, self_corr: T
                 op.base.plan.set_launch(**launch)
                 t, err = timed(op)
                 trials.append(dict(leaf_size=leaf, expansion_order=p, launch=dict(launch), ms=t, rel_error=err))
-                if err <= max_rel_error and (best is None or t < best[0]):
-                    best = (t, op, leaf, p, dict(launch), err)
-    if best is None:
+            ops[(leaf, p)] = op
+    choice = at.select_trial(trials, max_rel_error)
+    if choice is None:
         raise RuntimeError("no inner operator met the accuracy bound")
-    t, op, leaf, p, launch, err = best
+    t, leaf, p, launch, err = choice["ms"], choice["leaf_size"], choice["expansion_order"], choice["launch"], \
+        choice["rel_error"]
+    op = ops.pop((leaf, p))
+    ops.clear()
     at.apply_launch(op.base.plan, launch)
     if use_cache:
         at.append_record({"fingerprint": fingerprint, "problem_size_bucket": bucket, "kind": "inner_fp32",

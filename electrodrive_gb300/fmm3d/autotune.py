@@ -188,6 +188,24 @@ def time_matvec(plan: _lib.Plan, sigma: torch.Tensor, areas: torch.Tensor, reps:
 
 LAUNCH_CHOICES: Tuple[Dict[str, int], ...] = ({"near_overlap": 1}, {"near_overlap": 0})
 
+# candidates this close to the fastest count as equally fast
+TIME_SLACK = 0.05
+
+
+def select_trial(trials: List[Dict[str, Any]], max_rel_error: float,
+                 time_slack: float = TIME_SLACK) -> Optional[Dict[str, Any]]:
+    """Among trials (dicts with ``ms`` and ``rel_error``) within the accuracy
+    bound, the most accurate of those no more than ``time_slack`` slower than
+    the fastest: an inner operator nearer the bound costs the solver
+    iterations that a matvec a few percent faster does not win back.  None if
+    no trial meets the bound."""
+    ok = [t for t in trials if t["rel_error"] <= max_rel_error]
+    if not ok:
+        return None
+    fastest = min(t["ms"] for t in ok)
+    pool = [t for t in ok if t["ms"] <= (1.0 + time_slack) * fastest]
+    return min(pool, key=lambda t: (t["rel_error"], t["ms"]))
+
 
 def autotune_for_problem(base_cfg: FmmConfig, problem_size: int, *, dry_run: bool = True,
                          target_rel_error: float = 1e-2, max_trials: int = 24, device: Optional[torch.device] = None,

@@ -76,3 +76,14 @@ def test_inner_operator_choice_is_cached_and_rechecked(cuda_lib, tmp_path, monke
     assert len(trials2) == 1 and trials2[0]["from_cache"] and trials2[0]["rel_error"] <= 3e-7
     assert op2.base.plan.info.expansion_order == op.base.plan.info.expansion_order
     assert op2.base.plan.get_launch() == op.base.plan.get_launch()
+
+
+def test_select_trial_prefers_accuracy_among_equally_fast():
+    from electrodrive_gb300.fmm3d.autotune import select_trial
+
+    trials = [dict(name="a", ms=10.0, rel_error=2.9e-7), dict(name="b", ms=10.4, rel_error=1.7e-7),
+              dict(name="c", ms=12.0, rel_error=1.0e-7), dict(name="d", ms=9.0, rel_error=5e-7)]
+    # d is fastest but misses the bound; b is within 5% of a and more accurate; c is too slow
+    assert select_trial(trials, 3e-7)["name"] == "b"
+    assert select_trial(trials, 3e-7, time_slack=0.0)["name"] == "a"
+    assert select_trial(trials, 1e-8) is None
