@@ -310,26 +310,33 @@ __device__ double uniform_sum(V3 a, V3 b, V3 c, V3 t, int order, int depth, doub
     return ke * (area * h * h / 3.0) * s;
 }
 
-__global__ void k_near_weights_rows(const double *__restrict__ cent, const double *__restrict__ areas,
-                                    const double *__restrict__ verts, int64_t n, const int32_t *__restrict__ row_off,
-                                    const int32_t *__restrict__ cols, int order, int depth, double ke,
-                                    double *__restrict__ w) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.y + threadIdx.y;
-    if (i >= n) return;
-    const V3 ci = ld3(cent + 3 * i);
-    for (int k = row_off[i] + threadIdx.x; k < row_off[i + 1]; k += blockDim.x) {
-        const int j = cols[k];
-        const double aj = areas[j];
-        double v = 0.0;
-        if (aj > 0.0) {
-            const double inear =
-                uniform_sum(ld3(verts + 9 * (int64_t)j), ld3(verts + 9 * (int64_t)j + 3), ld3(verts + 9 * (int64_t)j + 6),
-                            ci, order, depth, ke);
-            const double ifar = ke * aj / fmax(dist_np(ci, ld3(cent + 3 * (int64_t)j)), 1e-12);
-            v = inear - ifar;
-        }
-        w[k] = v;
+// one thread per pair k of the CSR rows (rows hold a few pairs each, and a
+// pair's rule is ~200 FP64 evaluations at depth 3); its row i is the last
+// row starting at or before k
+__global__ void k_near_weights_pairs(const double *__restrict__ cent, const double *__restrict__ areas,
+                                     const double *__restrict__ verts, int64_t n, int64_t np,
+                                     const int32_t *__restrict__ row_off, const int32_t *__restrict__ cols, int order,
+                                     int depth, double ke, double *__restrict__ w) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    int64_t lo = 0, hi = n - 1;  // row_off[lo] <= k < row_off[n]
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (row_off[mid] <= k) lo = mid;
+        else hi = mid - 1;
     }
+    const V3 ci = ld3(cent + 3 * lo);
+    const int j = cols[k];
+    const double aj = areas[j];
+    double v = 0.0;
+    if (aj > 0.0) {
+        const double inear =
+            uniform_sum(ld3(verts + 9 * (int64_t)j), ld3(verts + 9 * (int64_t)j + 3), ld3(verts + 9 * (int64_t)j + 6),
+                        ci, order, depth, ke);
+        const double ifar = ke * aj / fmax(dist_np(ci, ld3(cent + 3 * (int64_t)j)), 1e-12);
+        v = inear - ifar;
+    }
+    w[k] = v;
 }
 
 template <typename T>
@@ -584,11 +591,10 @@ EDFMM_API int edfmm_near_create(const void *centroids_dev, const void *areas_dev
         for (int64_t i = 0; i < n; ++i) mx = std::max<int64_t>(mx, hoff[i + 1] - hoff[i]);
         h->max_row = mx;
         if ((rc = sort_csr_rows(dptr<int32_t>(h->row_off), dptr<int32_t>(h->cols), n, mx, s))) return done(rc);
-        dim3 blk(32, 4);
-        k_near_weights_rows<<<nb(n, 4), blk, 0, s>>>(c, a, static_cast<const double *>(panel_vertices_dev), n,
-                                                    dptr<int32_t>(h->row_off), dptr<int32_t>(h->cols), quad_order,
-                                                    depth, k_e, dptr<double>(h->w64));
-        EDFMM_LAUNCH_CHECK("k_near_weights_rows");
+        k_near_weights_pairs<<<nb(np, 128), 128, 0, s>>>(c, a, static_cast<const double *>(panel_vertices_dev), n, np,
+                                                         dptr<int32_t>(h->row_off), dptr<int32_t>(h->cols), quad_order,
+                                                         depth, k_e, dptr<double>(h->w64));
+        EDFMM_LAUNCH_CHECK("k_near_weights_pairs");
         if (dtype == EDFMM_F64) {
             EDFMM_CUDA_TRY(cudaMemcpyAsync(h->w.p, h->w64.p, 8 * np, cudaMemcpyDeviceToDevice, s));
         } else {

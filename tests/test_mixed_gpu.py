@@ -66,8 +66,11 @@ def test_autotuned_inner_operator_meets_its_bound_and_the_solve_converges(torus_
     launch = op32.base.plan.get_launch()
     chosen = [t for t in trials if t["expansion_order"] == op32.base.plan.info.expansion_order
               and t["launch"]["near_overlap"] == launch["near_overlap"]][0]
+    from electrodrive_gb300.fmm3d.autotune import TIME_SLACK, select_trial
+
     assert chosen["rel_error"] <= 3e-7
-    assert chosen["ms"] == min(t["ms"] for t in trials if t["rel_error"] <= 3e-7)
+    assert chosen is select_trial(trials, 3e-7)  # the most accurate of those within 5% of the fastest
+    assert chosen["ms"] <= (1 + TIME_SLACK) * min(t["ms"] for t in trials if t["rel_error"] <= 3e-7)
     b = S["b"]
     x, info = solve_mixed(op64, op32, b, A_diag=S["diag"], x0=S["x0"], rtol=1e-6)
     assert info["code"] == 0
