@@ -825,7 +825,7 @@ def run_batch_workload(args, rank, world, local, emit=True):
     system = BatchSystem(cases, device=dev)
     torch.cuda.synchronize(dev)
     t_setup = time.perf_counter() - t0
-    tune = autotune_inner(system)
+    tune = autotune_inner(system, inner_tol=args.inner_tol_floor)
     # the refinement's FP64 residuals and stopping test in two-float arithmetic
     system.op64.plan.set_arithmetic("two_float")
     result = {}

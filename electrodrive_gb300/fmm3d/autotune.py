@@ -192,16 +192,20 @@ LAUNCH_CHOICES: Tuple[Dict[str, int], ...] = ({"near_overlap": 1}, {"near_overla
 TIME_SLACK = 0.05
 
 
-def select_trial(trials: List[Dict[str, Any]], max_rel_error: float,
-                 time_slack: float = TIME_SLACK) -> Optional[Dict[str, Any]]:
-    """Among trials (dicts with ``ms`` and ``rel_error``) within the accuracy
-    bound, the most accurate of those no more than ``time_slack`` slower than
-    the fastest: an inner operator nearer the bound costs the solver
-    iterations that a matvec a few percent faster does not win back.  None if
-    no trial meets the bound."""
+def select_trial(trials: List[Dict[str, Any]], max_rel_error: float, time_slack: float = TIME_SLACK,
+                 inner_tol: Optional[float] = None) -> Optional[Dict[str, Any]]:
+    """The inner operator to use among trials (dicts with ``ms`` and
+    ``rel_error``) within the accuracy bound.  An operator whose error is a
+    fraction e of the tolerance the inner solves must reach (``inner_tol``)
+    slows their convergence as e approaches 1, so with ``inner_tol`` the
+    choice minimises ms / (1 - e); without it, the most accurate of the
+    trials no more than ``time_slack`` slower than the fastest.  None if no
+    trial meets the bound."""
     ok = [t for t in trials if t["rel_error"] <= max_rel_error]
     if not ok:
         return None
+    if inner_tol is not None:
+        return min(ok, key=lambda t: (t["ms"] / max(1.0 - t["rel_error"] / inner_tol, 1e-3), t["rel_error"]))
     fastest = min(t["ms"] for t in ok)
     pool = [t for t in ok if t["ms"] <= (1.0 + time_slack) * fastest]
     return min(pool, key=lambda t: (t["rel_error"], t["ms"]))

@@ -87,3 +87,7 @@ def test_select_trial_prefers_accuracy_among_equally_fast():
     assert select_trial(trials, 3e-7)["name"] == "b"
     assert select_trial(trials, 3e-7, time_slack=0.0)["name"] == "a"
     assert select_trial(trials, 1e-8) is None
+    # with the inner tolerance the error costs iterations: cost = ms / (1 - err / tol)
+    # a: 10 / (1 - 0.967) = 300, b: 10.4 / (1 - 0.567) = 24, c: 12 / (1 - 0.333) = 18
+    assert select_trial(trials, 3e-7, inner_tol=3e-7)["name"] == "c"
+    assert select_trial(trials, 3e-7, inner_tol=1e-5)["name"] == "a"  # a loose floor: speed decides
