@@ -76,9 +76,9 @@ M2L_DRAM_BYTES_PER_PAIR = 44.54e6 / 9_091_877
 # DRAM bytes (read + write) per M2L pair of k_m2l_rot<float, p> on the
 # 200,000-panel torus (FP32 inner operator), from ncu captures of that kernel
 # on that mesh (median over the profile run's launches)
-M2L_DRAM_BYTES_PER_PAIR_TORUS = {8: 14_461_269 / 2_315_072, 6: 12_600_576 / 2_315_072}
+M2L_DRAM_BYTES_PER_PAIR_TORUS = {(8, 64): 14_461_269 / 2_315_072, (6, 64): 12_600_576 / 2_315_072}  # (p, leaf)
 # the same for the 256-dimer batch (FP32 inner operator, autotuned order)
-M2L_DRAM_BYTES_PER_PAIR_BATCH = {6: (244_023_808 + 55_725_312) / 39_011_439}
+M2L_DRAM_BYTES_PER_PAIR_BATCH = {(6, 64): (244_023_808 + 55_725_312) / 39_011_439}  # (p, leaf)
 # DRAM bytes of one k_dense_partial<double> launch at n = 5,120 (ncu capture)
 DENSE_DRAM_BYTES_PER_MATVEC_5120 = 293_120
 # near field: 3 sub + 3 fma (r^2) + max + rsqrt + fma per interaction, counted
@@ -493,7 +493,8 @@ def run_solve_workload(args, rank, world, local, emit=True):
         from electrodrive_gb300.core.bem import autotune_inner_operator
 
         op32, inner_trials = autotune_inner_operator(op64, sysd["centroids"], sysd["areas"], sysd["self_corr"],
-                                                     near=sysd["ops"][torch.float32].near, device=dev)
+                                                     near=sysd["ops"][torch.float32].near, device=dev,
+                                                     leaf_sizes=(64, 128))
         sysd["ops"][torch.float32] = op32
         # the refinement's FP64 residuals and stopping test: the FP64 FMM
         # operator with M2L and near field in two-float arithmetic (every
@@ -674,7 +675,7 @@ def run_solve_workload(args, rank, world, local, emit=True):
         m2l_ms = statistics.median(_time_cuda(lambda: p32.stage("m2l", 0), dev, stream, flush, 2, 5))
         order32 = int(p32.info.expansion_order)
         achieved = p32.info.n_m2l_pairs * m2l_flops_per_pair(order32) / (m2l_ms * 1e-3) / 1e12
-        per_pair = M2L_DRAM_BYTES_PER_PAIR_TORUS.get(order32)
+        per_pair = M2L_DRAM_BYTES_PER_PAIR_TORUS.get((order32, int(p32.info.leaf_size)))
         roof = {"kernel": f"k_m2l_rot<float, {order32}> (M2L of the FP32 inner operator)", "bound": "fp32",
                 "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
@@ -913,7 +914,7 @@ def run_batch_workload(args, rank, world, local, emit=True):
         order = tune["expansion_order"]
         flops_pair = m2l_flops_per_pair(order) if 1 <= order <= 8 else None
         ach = p32.info.n_m2l_pairs * flops_pair / (m2l_ms * 1e-3) / 1e12 if flops_pair else None
-        per_pair = M2L_DRAM_BYTES_PER_PAIR_BATCH.get(order)
+        per_pair = M2L_DRAM_BYTES_PER_PAIR_BATCH.get((order, int(tune["leaf_size"])))
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32+f64", "data": "synthetic",

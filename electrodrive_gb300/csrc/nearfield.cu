@@ -164,7 +164,7 @@ __device__ __forceinline__ void accumulate_slot(const float *sx, int cnt, int sb
     const float *sy = sx + 64, *sz = sx + 128, *sw = sx + 192;
     const int np = (cnt + 1) >> 1;
     float2 ps = S.ps;
-#pragma unroll 4
+#pragma unroll 2  // measured: 2.31 ms against 2.39 (unroll 4) at 1M uniform points
     for (int j = part; j < np; j += G) {
         const float2 qx = *reinterpret_cast<const float2 *>(sx + 2 * j);
         const float2 qy = *reinterpret_cast<const float2 *>(sy + 2 * j);
