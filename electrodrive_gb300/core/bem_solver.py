@@ -231,13 +231,13 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
     if want_graph and M_python is None:
         ws = _graph_workspace(A, ("gmres", N, restart, work_dtype, dev, pinv is not None), lambda: dict(
             K=_Krylov(N, restart, work_dtype, dev), av=torch.empty(N, dtype=work_dtype, device=dev),
-            pinv=None if pinv is None else torch.empty_like(pinv), graphs={}, warmed=[False]))
+            pinv=None if pinv is None else torch.empty_like(pinv), graphs={}))
         if pinv is not None:
             ws["pinv"].copy_(pinv)
             pinv = ws["pinv"]
     else:
         ws = dict(K=_Krylov(N, restart, work_dtype, dev), av=torch.empty(N, dtype=work_dtype, device=dev),
-                  graphs={}, warmed=[False])
+                  graphs={})
     K, av = ws["K"], ws["av"]
 
     # refinement callers (final_check=False) skip A(0) at a zero start; the
@@ -263,29 +263,25 @@ def gmres_restart(A: Callable[[Tensor], Tensor], b: Tensor, M: Optional[Callable
             K.arnoldi(j, av, pinv if M_python is None else None)
 
     graphs: Dict[Tuple[int, int], Any] = ws["graphs"]
-    warmed = ws["warmed"]
+    seen = ws.setdefault("seen", set())
 
     def run_steps(j0: int, count: int):
-        """Arnoldi steps j0 .. j0+count-1, as a captured graph when allowed."""
+        """Arnoldi steps j0 .. j0+count-1, as a captured graph when allowed.
+        A step sequence is captured the second time it is asked for (a later
+        cycle, or a later solve with the same operator) and replayed from
+        then on; its first run launches the kernels directly, since a graph
+        that is never replayed costs more to capture and instantiate than
+        it saves (a one-cycle solve on a fresh operator)."""
         if not want_graph:
             inner_steps(count, j0)
             return
         key = (j0, count)
+        if key not in graphs and key not in seen:
+            seen.add(key)
+            inner_steps(count, j0)
+            return
         if key not in graphs:
-            if not warmed[0]:
-                # warm the operator's lazy state outside the capture
-                torch.cuda.synchronize(dev)
-                s = torch.cuda.Stream(device=dev)
-                s.wait_stream(torch.cuda.current_stream(dev))
-                with torch.cuda.stream(s):
-                    inner_steps(1, j0)
-                torch.cuda.current_stream(dev).wait_stream(s)
-                torch.cuda.synchronize(dev)
-                warmed[0] = True
-                if j0 == 0:
-                    start_cycle()  # the warm-up step overwrote w/H; recompute the start state
-                else:
-                    raise RuntimeError("graph warm-up must happen at the start of a cycle")
+            # the eager first run has set up the operator's lazy state
             g = torch.cuda.CUDAGraph()
             l0 = _lib.launch_count()
             with torch.cuda.graph(g):
@@ -505,23 +501,21 @@ def gmres_batched(A: Callable[[Tensor], Tensor], b: Tensor, segments: List[int],
             Kr.arnoldi(j, av, pinv)
 
     graphs: Dict[Tuple[int, int], Any] = ws["graphs"]
+    seen = ws.setdefault("seen", set())
 
     def run_steps(j0: int, count: int):
+        # captured the second time a step sequence is asked for (as in
+        # gmres_restart): its first run launches the kernels directly
         if not use_graph:
             steps_eager(j0, count)
             return
         key = (j0, count)
+        if key not in graphs and key not in seen:
+            seen.add(key)
+            steps_eager(j0, count)
+            return
         if key not in graphs:
-            if not graphs:
-                # warm the operator's lazy state outside the capture; the
-                # output is discarded, so the Krylov state is untouched
-                torch.cuda.synchronize(dev)
-                s = torch.cuda.Stream(device=dev)
-                s.wait_stream(torch.cuda.current_stream(dev))
-                with torch.cuda.stream(s):
-                    A(Kr.V[j0])
-                torch.cuda.current_stream(dev).wait_stream(s)
-                torch.cuda.synchronize(dev)
+            # the eager first run has set up the operator's lazy state
             g = torch.cuda.CUDAGraph()
             l0 = _lib.launch_count()
             with torch.cuda.graph(g):

@@ -1,5 +1,7 @@
 // The rotation-based M2L launchers (the kernels are in m2l_rot.cuh,
 // instantiated by m2l_rot_f32.cu, m2l_rot_f64.cu and m2l_rot_tf*.cu).
+#include <cstdint>
+
 #include "m2l_rot.cuh"
 
 namespace edfmm {
@@ -13,6 +15,9 @@ int launch_m2l_rot(int dtype, int p, int64_t M, const int32_t *off, const int32_
                    const void *thal, const void *cen, const void *hal, const void *Mx, void *Lx, int nc_pad,
                    const InstMask &mask, cudaStream_t s) {
     if (M <= 0) return EDFMM_OK;
+    // the FP32 kernel reads rows two coefficients (16 bytes) at a time
+    if (dtype != EDFMM_F64 && ((reinterpret_cast<uintptr_t>(Mx) & 15) != 0 || (nc_pad & 1) != 0))
+        return EDFMM_ERR_ARG;
     return dtype == EDFMM_F64 ? m2l_rot_f64(p, M, off, src, rows, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s)
                               : m2l_rot_f32(p, M, off, src, rows, tcen, thal, cen, hal, Mx, Lx, nc_pad, mask, s);
 }

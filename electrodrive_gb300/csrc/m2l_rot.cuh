@@ -353,11 +353,25 @@ template <typename T, int P> __host__ __device__ constexpr bool rot_binomial() {
 template <typename T, int P, typename V, typename A>
 __device__ __forceinline__ void rot_pair(V &v, A &acc, const typename Vec2<T>::type *__restrict__ Mrow, T c, T dx, T dy,
                                          T dz) {
+    // FP32 rows are read two coefficients per 16-byte load (rows of an even
+    // number of coefficients, 16-byte aligned): half the scattered loads
+    float4 x4{};
 #pragma unroll
     for (int n = 0; n <= P; ++n) {
 #pragma unroll
         for (int m = 0; m <= n; ++m) {
-            const typename Vec2<T>::type x = Mrow[tri(n, m)];
+            const int q = tri(n, m);
+            typename Vec2<T>::type x;
+            if constexpr (sizeof(T) == 4) {
+                if ((q & 1) == 0) {
+                    x4 = reinterpret_cast<const float4 *>(Mrow)[q >> 1];
+                    x = make_float2(x4.x, x4.y);
+                } else {
+                    x = make_float2(x4.z, x4.w);
+                }
+            } else {
+                x = Mrow[q];
+            }
             if (m == 0) {
                 v.set(n * n, x.x);
             } else {

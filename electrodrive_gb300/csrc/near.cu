@@ -262,11 +262,9 @@ __global__ void k_near_scan(const double *cent, const double *radii, int64_t n, 
 
 __global__ void k_set_last32(int32_t *off, int64_t rows, const int64_t *total) { off[rows] = (int32_t)*total; }
 
-// K_E w / max(|t - y|, 1e-12) at y = a + u (b - a) + v (c - a)
-__device__ __forceinline__ double grid_term(V3 a, V3 e1, V3 e2, double u, double v, V3 t) {
-    const double dx = t.x - fma(v, e2.x, fma(u, e1.x, a.x));
-    const double dy = t.y - fma(v, e2.y, fma(u, e1.y, a.y));
-    const double dz = t.z - fma(v, e2.z, fma(u, e1.z, a.z));
+// 1 / max(|d - o|, 1e-12) for a lattice point at offset o from the cell corner
+__device__ __forceinline__ double lattice_term(V3 d, V3 o) {
+    const double dx = d.x - o.x, dy = d.y - o.y, dz = d.z - o.z;
     return rsqrt(fmax(fma(dz, dz, fma(dy, dy, dx * dx)), 1e-24));
 }
 
@@ -274,39 +272,55 @@ __device__ __forceinline__ double grid_term(V3 a, V3 e1, V3 e2, double u, double
 // (a, b, c) (the reference refines recursively by edge midpoints).  The
 // leaves are the cells of the barycentric grid of step h = 2^-depth: the
 // upright cell (i, j) has corners (i, j), (i+1, j), (i, j+1) and the inverted
-// one (i+1, j), (i, j+1), (i+1, j+1), in units of h along b - a and c - a;
-// every leaf has area(a, b, c) / 4^depth.  Each point costs one FP64 rsqrt
-// instead of a square root and a division, and no leaf geometry is rebuilt.
+// one (i+1, j), (i, j+1), (i+1, j+1), in units of the lattice steps
+// E1 = h (b - a) and E2 = h (c - a); every leaf has area(a, b, c) / 4^depth.
+// The target's offset from a cell corner, t - a - i E1 - j E2, is formed once
+// per cell (three FMAs), and each rule point subtracts its fixed offset in
+// the cell from it: three subtractions and one FP64 rsqrt per point.
 __device__ double uniform_sum(V3 a, V3 b, V3 c, V3 t, int order, int depth, double ke) {
     const double area = tri_area(a, b, c);
     if (!(area > 0.0)) return 0.0;
     const int m = 1 << depth;
     const double h = 1.0 / (double)m;
-    const V3 e1{b.x - a.x, b.y - a.y, b.z - a.z}, e2{c.x - a.x, c.y - a.y, c.z - a.z};
+    const V3 E1{(b.x - a.x) * h, (b.y - a.y) * h, (b.z - a.z) * h};
+    const V3 E2{(c.x - a.x) * h, (c.y - a.y) * h, (c.z - a.z) * h};
+    const V3 d0{t.x - a.x, t.y - a.y, t.z - a.z};
+    auto off = [&](double u, double v) {
+        return V3{fma(v, E2.x, u * E1.x), fma(v, E2.y, u * E1.y), fma(v, E2.z, u * E1.z)};
+    };
     double s = 0.0;
     if (order <= 1) {
-        // leaf centroids: upright (i + 1/3, j + 1/3), inverted (i + 2/3, j + 2/3)
-        for (int i = 0; i < m; ++i)
+        // leaf centroids: upright (1/3, 1/3), inverted (2/3, 2/3) from the corner
+        const V3 ou = off(1.0 / 3.0, 1.0 / 3.0), oi = off(2.0 / 3.0, 2.0 / 3.0);
+        for (int i = 0; i < m; ++i) {
+            const V3 r{fma(-(double)i, E1.x, d0.x), fma(-(double)i, E1.y, d0.y), fma(-(double)i, E1.z, d0.z)};
             for (int j = 0; i + j < m; ++j) {
-                s += grid_term(a, e1, e2, (i + 1.0 / 3.0) * h, (j + 1.0 / 3.0) * h, t);
-                if (i + j < m - 1) s += grid_term(a, e1, e2, (i + 2.0 / 3.0) * h, (j + 2.0 / 3.0) * h, t);
+                const V3 d{fma(-(double)j, E2.x, r.x), fma(-(double)j, E2.y, r.y), fma(-(double)j, E2.z, r.z)};
+                s += lattice_term(d, ou);
+                if (i + j < m - 1) s += lattice_term(d, oi);
             }
+        }
         return ke * (area * h * h) * s;
     }
     // points 2/3 at one corner, 1/6 at the others: upright cell offsets
-    // (2/3, 1/6)... in (i, j) units, inverted cell the mirrored ones
+    // (q, q), (p, q), (q, p); inverted cell (1-q, 1-q), (1-p, 1-q), (1-q, 1-p)
     const double p = 2.0 / 3.0, q = 1.0 / 6.0;
-    for (int i = 0; i < m; ++i)
+    const V3 u0 = off(q, q), u1 = off(p, q), u2 = off(q, p);
+    const V3 v0 = off(1.0 - q, 1.0 - q), v1 = off(1.0 - p, 1.0 - q), v2 = off(1.0 - q, 1.0 - p);
+    for (int i = 0; i < m; ++i) {
+        const V3 r{fma(-(double)i, E1.x, d0.x), fma(-(double)i, E1.y, d0.y), fma(-(double)i, E1.z, d0.z)};
         for (int j = 0; i + j < m; ++j) {
-            s += grid_term(a, e1, e2, (i + q) * h, (j + q) * h, t);
-            s += grid_term(a, e1, e2, (i + p) * h, (j + q) * h, t);
-            s += grid_term(a, e1, e2, (i + q) * h, (j + p) * h, t);
+            const V3 d{fma(-(double)j, E2.x, r.x), fma(-(double)j, E2.y, r.y), fma(-(double)j, E2.z, r.z)};
+            s += lattice_term(d, u0);
+            s += lattice_term(d, u1);
+            s += lattice_term(d, u2);
             if (i + j < m - 1) {
-                s += grid_term(a, e1, e2, (i + 1.0 - q) * h, (j + 1.0 - q) * h, t);
-                s += grid_term(a, e1, e2, (i + 1.0 - p) * h, (j + 1.0 - q) * h, t);
-                s += grid_term(a, e1, e2, (i + 1.0 - q) * h, (j + 1.0 - p) * h, t);
+                s += lattice_term(d, v0);
+                s += lattice_term(d, v1);
+                s += lattice_term(d, v2);
             }
         }
+    }
     return ke * (area * h * h / 3.0) * s;
 }
 

@@ -198,24 +198,26 @@ __device__ __forceinline__ void accumulate_slot(const double4 *sp, int cnt, int 
     S.ps += ps;  // per-chunk partial, then one add: two-level summation
 }
 
-// Two-float: one source per step from the staged split arrays
-// (xh, xl, yh, yl, zh, zl, qh, ql; 64 each).  The coordinate differences
-// are formed from the split parts, so the cancellation of nearby points
-// loses nothing; 1 / r takes one Newton step from the FP32 estimate.
+// Two-float: one source per step from the staged split points
+// (s4[2j] = (xh, xl, yh, yl), s4[2j + 1] = (zh, zl, qh, ql): two 16-byte
+// shared loads).  The coordinate differences are formed from the split
+// parts, so the cancellation of nearby points loses nothing; 1 / r takes one
+// Newton step from the FP32 estimate.
 template <int G, bool SELF>
-__device__ __forceinline__ void accumulate_slot(const float *s8, int cnt, int sbase, int part, Slot<tf32x2> &S,
+__device__ __forceinline__ void accumulate_slot(const float4 *s4, int cnt, int sbase, int part, Slot<tf32x2> &S,
                                                 float eps2) {
     tf32x2 ps = tf32x2(0);
 #pragma unroll 2
     for (int j = part; j < cnt; j += G) {
-        const tf32x2 dx = S.x - tf32x2(s8[j], s8[64 + j]);
-        const tf32x2 dy = S.y - tf32x2(s8[128 + j], s8[192 + j]);
-        const tf32x2 dz = S.z - tf32x2(s8[256 + j], s8[320 + j]);
+        const float4 a = s4[2 * j], b = s4[2 * j + 1];
+        const tf32x2 dx = S.x - tf32x2(a.x, a.y);
+        const tf32x2 dy = S.y - tf32x2(a.z, a.w);
+        const tf32x2 dz = S.z - tf32x2(b.x, b.y);
         tf32x2 r2 = fma(dz, dz, fma(dy, dy, dx * dx));
         if (!(r2.hi >= eps2)) r2 = tf32x2(eps2, 0.0f);
         tf32x2 inv = tf_rsqrt(r2, rsqrt_normal(r2.hi));
         if (SELF && sbase + j == S.ti) inv = tf32x2(0);
-        ps = fma(tf32x2(s8[384 + j], s8[448 + j]), inv, ps);
+        ps = fma(tf32x2(b.z, b.w), inv, ps);
     }
     S.ps = S.ps + ps;  // per-chunk partial, then one add: two-level summation
 }
@@ -283,7 +285,8 @@ __device__ __forceinline__ void accumulate_slots(const C *chunk, int cnt, int sb
 // Targets tb..te-1 (at most 64) of leaf t: near field by slots, then the
 // local expansion and the epilogue with one lane per target.  Source chunks
 // of up to 64 points (one leaf, or a 64-point piece of a larger one) are
-// staged in shared memory (FP32 as x / y / z / q arrays, FP64 as points).
+// staged in shared memory (FP32 as x / y / z / q arrays, two-float as split
+// points, FP64 as points).
 // The leaf ids and ranges of the row are read 32 entries at a time (one per
 // lane) and broadcast by shuffles, and the next chunk's points are loaded
 // before the current chunk is computed, so the dependent global loads
@@ -298,6 +301,7 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
     using T4 = typename Vec4<T>::type;
     using ST = std::conditional_t<TF, tf32x2, T>;      // slot arithmetic
     using Pre = std::conditional_t<TF, SplitPt, T4>;  // prefetched source point
+    constexpr bool F32 = !TF && sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     const int nt = te - tb;
     bool on[5];
@@ -363,22 +367,12 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
                 const int cs = s, csb = sb, cnt = min(64, se - sb);
                 __syncwarp();
                 if constexpr (TF) {
-                    float *s8 = reinterpret_cast<float *>(sp);
-                    const float4 qs[4] = {qa.a, qa.b, qb.a, qb.b};
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const float4 u = qs[2 * h], w = qs[2 * h + 1];
-                        const int o = lane + 32 * h;
-                        s8[o] = u.x;
-                        s8[64 + o] = u.y;
-                        s8[128 + o] = u.z;
-                        s8[192 + o] = u.w;
-                        s8[256 + o] = w.x;
-                        s8[320 + o] = w.y;
-                        s8[384 + o] = w.z;
-                        s8[448 + o] = w.w;
-                    }
-                } else if constexpr (sizeof(T) == 4) {
+                    float4 *s4 = reinterpret_cast<float4 *>(sp);
+                    s4[2 * lane] = qa.a;
+                    s4[2 * lane + 1] = qa.b;
+                    s4[2 * lane + 64] = qb.a;
+                    s4[2 * lane + 65] = qb.b;
+                } else if constexpr (F32) {
                     float *sx = reinterpret_cast<float *>(sp);
                     sx[lane] = qa.x;
                     sx[64 + lane] = qa.y;
@@ -409,12 +403,12 @@ __device__ __forceinline__ void leaf_slots(const NearParams<T> &P, int t, int tb
                     qb = fetch(sb, se, lane + 32);
                 }
                 if constexpr (TF) {
-                    const float *s8 = reinterpret_cast<const float *>(sp);
+                    const float4 *s4 = reinterpret_cast<const float4 *>(sp);
                     if (P.same && cs == t)
-                        accumulate_slots<tf32x2, true>(s8, cnt, csb, lane, on, S, (float)eps2);
+                        accumulate_slots<tf32x2, true>(s4, cnt, csb, lane, on, S, (float)eps2);
                     else
-                        accumulate_slots<tf32x2, false>(s8, cnt, csb, lane, on, S, (float)eps2);
-                } else if constexpr (sizeof(T) == 4) {
+                        accumulate_slots<tf32x2, false>(s4, cnt, csb, lane, on, S, (float)eps2);
+                } else if constexpr (F32) {
                     const float *sx = reinterpret_cast<const float *>(sp);
                     if (P.same && cs == t)
                         accumulate_slots<T, true>(sx, cnt, csb, lane, on, S, eps2);

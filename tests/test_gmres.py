@@ -121,6 +121,36 @@ def test_device_gmres_early_exit(cuda_lib, graph):
     assert np.linalg.norm(x - x_ref) <= 1e-6 * np.linalg.norm(x_ref)
 
 
+@pytest.mark.gpu
+def test_device_gmres_graph_from_the_second_request(cuda_lib):
+    """A step sequence runs as direct launches the first time it is asked for
+    and from a captured graph afterwards (here: a second solve with the same
+    operator); the iterates are identical either way."""
+    from electrodrive_gb300.core import bem_solver as bs
+
+    A, b, x_ref, restart, tol, maxiter, pc, iters, code = _case("bemlike300_jacobi")
+    At = torch.as_tensor(A, device="cuda")
+    out = torch.empty(A.shape[0], dtype=torch.float64, device="cuda")
+
+    class Op:
+        capturable = True
+
+        def __call__(self, v):
+            torch.mv(At, v, out=out)
+            return out
+
+    op, bt = Op(), torch.as_tensor(b, device="cuda")
+    runs = []
+    for _ in range(2):
+        x, info = bs.gmres_restart(op, bt, restart=restart, tol=tol, maxiter=maxiter, precond="jacobi",
+                                   A_diag=torch.diag(At), use_graph=True, early_exit=4)
+        runs.append((x.clone(), info))
+    (x1, i1), (x2, i2) = runs
+    assert i1["code"] == 0 and i1["iters"] == i2["iters"]
+    assert torch.equal(x1, x2)
+    assert any(ws["graphs"] for ws in bs._GRAPH_CACHE[op].values())
+
+
 def test_jacobi_fallback_converges_or_reports_failure():
     """core.bem.jacobi_fallback_solve, the reference's damped-Jacobi last
     resort (electrodrive/core/bem.py:1156-1251), on CPU tensors: a diagonally
