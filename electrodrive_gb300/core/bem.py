@@ -280,6 +280,7 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
                              areas=A_dev.to(dtype), A_diag=diag, x0=x0, logger=logger, use_graph=use_graph)
 
     sigma = info = None
+    r_sigma = None  # the mixed solve's FP64 residual b - A sigma at its sigma
     if mixed:
         xm0 = x0
         if warm_start is not None:
@@ -295,6 +296,7 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
         bn = float(torch.linalg.norm(b))
         if minfo["success"]:
             sigma = x.to(dtype)
+            r_sigma = minfo["residual"]
             info = dict(iters=minfo["inner_iters"], resid=minfo["rel_resid"] * bn, success=True, code=0,
                         tol_abs=mixed_rtol * bn, used_preconditioner=use_precond, outer=minfo["outer"],
                         matvec64=minfo["matvec64"], history=minfo["history"], precision="mixed")
@@ -321,7 +323,12 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
             sigma, info = sj, ij
     if not bool(torch.isfinite(sigma).all()):
         return {"error": "BEM sigma contains NaN/Inf after linear solve."}
-    V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
+    if r_sigma is not None:
+        # V_free + A sigma = bc - (b - A sigma): the solve's last FP64
+        # residual already holds the operator application at sigma
+        V_tot = torch.nan_to_num(bc - r_sigma.to(dtype), nan=0.0, posinf=0.0, neginf=0.0)
+    else:
+        V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
     bc_resid = float(torch.max(torch.abs(V_tot - bc)))
     energy = float(0.5 * torch.sum(V_tot.double() * torch.nan_to_num(sigma).double() * A_dev))
     Nrm = torch.as_tensor(mesh.normals, dtype=dtype, device=dev)
@@ -678,8 +685,9 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
             rel = float((segment_norms(r, segments) / bseg).max())
             hist[-1] = rel
         if rel <= rtol:
+            # r is the FP64 residual b - A64 x of the returned x
             return x, dict(success=True, code=0, outer=it, inner_iters=inner_total, rel_resid=rel, history=hist,
-                           matvec64=matvec64, instance_inner_iters=inst_iters)
+                           matvec64=matvec64, instance_inner_iters=inst_iters, residual=r)
         if it == max_outer:
             break
         r32 = r.to(torch.float32)

@@ -32,6 +32,7 @@
 #include <memory>
 
 #include "edfmm_internal.cuh"
+#include "twofloat.cuh"
 
 namespace edfmm {
 namespace {
@@ -175,18 +176,41 @@ __global__ void k_near_targets(const double *__restrict__ tgt, int64_t m, const 
 
 __global__ void k_radii_bounds(const double *cent, const double *areas, int64_t n, double *radii,
                                unsigned long long *rmax, long long *lo, long long *hi) {
+    // per-lane values, reduced over the warp, then one atomic per warp
+    // and bound (a block of panels updates the same seven words)
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double r = disk_radius(areas[i]);
-    radii[i] = r;
-    if (isfinite(r)) atomicMax(rmax, (unsigned long long)__double_as_longlong(r));
-    for (int a = 0; a < 3; ++a) {
-        const double v = cent[3 * i + a];
-        if (!isfinite(v)) continue;
-        long long o = __double_as_longlong(v);
-        o = o >= 0 ? o : o ^ 0x7fffffffffffffffLL;
-        atomicMin(&lo[a], o);
-        atomicMax(&hi[a], o);
+    constexpr long long kLo = 0x7fffffffffffffffLL, kHi = (long long)0x8000000000000000ULL;
+    unsigned long long rm = 0;
+    long long l[3] = {kLo, kLo, kLo}, h[3] = {kHi, kHi, kHi};
+    if (i < n) {
+        const double r = disk_radius(areas[i]);
+        radii[i] = r;
+        if (isfinite(r)) rm = (unsigned long long)__double_as_longlong(r);
+        for (int a = 0; a < 3; ++a) {
+            const double v = cent[3 * i + a];
+            if (!isfinite(v)) continue;
+            long long o = __double_as_longlong(v);
+            o = o >= 0 ? o : o ^ 0x7fffffffffffffffLL;
+            l[a] = o;
+            h[a] = o;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long rr = __shfl_xor_sync(0xffffffffu, rm, o);
+        rm = rr > rm ? rr : rm;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const long long lo_o = __shfl_xor_sync(0xffffffffu, l[a], o), hi_o = __shfl_xor_sync(0xffffffffu, h[a], o);
+            l[a] = lo_o < l[a] ? lo_o : l[a];
+            h[a] = hi_o > h[a] ? hi_o : h[a];
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (rm) atomicMax(rmax, rm);
+        for (int a = 0; a < 3; ++a) {
+            if (l[a] != kLo) atomicMin(&lo[a], l[a]);
+            if (h[a] != kHi) atomicMax(&hi[a], h[a]);
+        }
     }
 }
 
@@ -246,9 +270,22 @@ __global__ void k_near_scan(const double *cent, const double *radii, int64_t n, 
                         const int j = items[k];
                         const double rj = radii[j];
                         if (!isfinite(rj)) continue;
-                        const double d = dist_np(pi, ld3(cent + 3 * (int64_t)j));
+                        // d = |c_i - c_j| in numpy's order, kept iff 0 < d <= th; the
+                        // squared distance decides all but the pairs within a few
+                        // ulps of the threshold, which take the square root
+                        const V3 pj = ld3(cent + 3 * (int64_t)j);
+                        const double ex = __dsub_rn(pi.x, pj.x), ey = __dsub_rn(pi.y, pj.y),
+                                     ez = __dsub_rn(pi.z, pj.z);
+                        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
                         const double th = __dmul_rn(factor, __dadd_rn(radii[i], rj));
-                        if (isfinite(d) && d > 0.0 && d <= th) {
+                        const double t2 = th * th;
+                        bool keep;
+                        if (!(d2 > 0.0) || !isfinite(d2) || !(th >= 0.0)) keep = false;
+                        else if (!(t2 >= 1e-290) || !isfinite(t2)) keep = __dsqrt_rn(d2) <= th;
+                        else if (d2 < t2 * (1.0 - 1e-14)) keep = true;
+                        else if (d2 > t2 * (1.0 + 1e-14)) keep = false;
+                        else keep = __dsqrt_rn(d2) <= th;
+                        if (keep) {
                             if (pass) cols[base + cnt] = j;
                             ++cnt;
                         }
@@ -324,6 +361,72 @@ __device__ double uniform_sum(V3 a, V3 b, V3 c, V3 t, int order, int depth, doub
     return ke * (area * h * h / 3.0) * s;
 }
 
+// 1 / sqrt(a) in two-float for a normal positive a: two Newton steps from the
+// FP32 estimate (the first leaves a one-signed error of about 1.5 e0^2 =
+// 2^-44.6, the second takes it to the two-float rounding level)
+__device__ __forceinline__ tf32x2 tf_rsqrt2(tf32x2 a) {
+    const tf32x2 y = tf_rsqrt(a, rsqrt_normal(a.hi));
+    const tf32x2 h = tf32x2(1.0f, 0.0f) - a * (y * y);
+    return tf_fast_two_sum(y.hi, __fadd_rn(y.lo, __fmul_rn(__fmul_rn(0.5f, y.hi), h.hi)));
+}
+
+__device__ __forceinline__ tf32x2 lattice_term_tf(const tf32x2 (&d)[3], const tf32x2 (&o)[3]) {
+    const tf32x2 dx = d[0] - o[0], dy = d[1] - o[1], dz = d[2] - o[2];
+    tf32x2 r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    if (!(r2.hi >= 1e-24f)) r2 = tf32x2(1e-24f, 0.0f);  // 1 / max(r, 1e-12)
+    return tf_rsqrt2(r2);
+}
+
+// uniform_sum (order >= 2) on the FP32 pipe: the target offsets and the rule
+// points' 1 / r in two-float arithmetic (about 2^-44 per term, against the
+// FP64 pipe's 1/64 of the FP32 rate on this GPU), each cell's six terms
+// summed in two-float and the cells in FP64.  The geometry (area, lattice
+// steps, point offsets) is formed in FP64 once per pair.
+__device__ double uniform_sum_tf(V3 a, V3 b, V3 c, V3 t, int depth, double ke) {
+    const double area = tri_area(a, b, c);
+    if (!(area > 0.0)) return 0.0;
+    const int m = 1 << depth;
+    const double h = 1.0 / (double)m;
+    const V3 E1{(b.x - a.x) * h, (b.y - a.y) * h, (b.z - a.z) * h};
+    const V3 E2{(c.x - a.x) * h, (c.y - a.y) * h, (c.z - a.z) * h};
+    auto tf3 = [](double x, double y, double z, tf32x2 (&o)[3]) {
+        o[0] = tf_from_double(x);
+        o[1] = tf_from_double(y);
+        o[2] = tf_from_double(z);
+    };
+    auto off = [&](double u, double v, tf32x2 (&o)[3]) {
+        tf3(fma(v, E2.x, u * E1.x), fma(v, E2.y, u * E1.y), fma(v, E2.z, u * E1.z), o);
+    };
+    const double p = 2.0 / 3.0, q = 1.0 / 6.0;
+    tf32x2 u0[3], u1[3], u2[3], v0[3], v1[3], v2[3], e1[3], e2[3], d0[3];
+    off(q, q, u0);
+    off(p, q, u1);
+    off(q, p, u2);
+    off(1.0 - q, 1.0 - q, v0);
+    off(1.0 - p, 1.0 - q, v1);
+    off(1.0 - q, 1.0 - p, v2);
+    tf3(-E1.x, -E1.y, -E1.z, e1);
+    tf3(-E2.x, -E2.y, -E2.z, e2);
+    tf3(t.x - a.x, t.y - a.y, t.z - a.z, d0);
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) {
+        tf32x2 r[3];
+        const tf32x2 fi((float)i, 0.0f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r[k] = fma(fi, e1[k], d0[k]);
+        for (int j = 0; i + j < m; ++j) {
+            tf32x2 d[3];
+            const tf32x2 fj((float)j, 0.0f);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) d[k] = fma(fj, e2[k], r[k]);
+            tf32x2 cs = lattice_term_tf(d, u0) + lattice_term_tf(d, u1) + lattice_term_tf(d, u2);
+            if (i + j < m - 1) cs = cs + lattice_term_tf(d, v0) + lattice_term_tf(d, v1) + lattice_term_tf(d, v2);
+            s += tf_to_double(cs);
+        }
+    }
+    return ke * (area * h * h / 3.0) * s;
+}
+
 // one thread per pair k of the CSR rows (rows hold a few pairs each, and a
 // pair's rule is ~200 FP64 evaluations at depth 3); its row i is the last
 // row starting at or before k
@@ -344,9 +447,10 @@ __global__ void k_near_weights_pairs(const double *__restrict__ cent, const doub
     const double aj = areas[j];
     double v = 0.0;
     if (aj > 0.0) {
+        const V3 a = ld3(verts + 9 * (int64_t)j), b = ld3(verts + 9 * (int64_t)j + 3),
+                 c = ld3(verts + 9 * (int64_t)j + 6);
         const double inear =
-            uniform_sum(ld3(verts + 9 * (int64_t)j), ld3(verts + 9 * (int64_t)j + 3), ld3(verts + 9 * (int64_t)j + 6),
-                        ci, order, depth, ke);
+            order <= 1 ? uniform_sum(a, b, c, ci, order, depth, ke) : uniform_sum_tf(a, b, c, ci, depth, ke);
         const double ifar = ke * aj / fmax(dist_np(ci, ld3(cent + 3 * (int64_t)j)), 1e-12);
         v = inear - ifar;
     }
