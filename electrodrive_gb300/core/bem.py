@@ -17,9 +17,10 @@ correction equation, and the loop stops on the FP64 relative true residual.
 from __future__ import annotations
 
 import math
+import threading
 import time
 from dataclasses import dataclass, field
-from typing import Any, Dict, List, Optional, Tuple
+from typing import Any, Callable, Dict, List, Optional, Tuple
 
 import numpy as np
 import torch
@@ -210,6 +211,42 @@ def _info_ok(info: Dict[str, Any]) -> Tuple[bool, float, int]:
     return bool(info.get("success", True)), resid, int(info.get("code", 0) or 0)
 
 
+def _near_in_background(C: Tensor, A: Tensor, PV: Tensor, dev, **kw) -> Callable[[], NearCorrection]:
+    """Start building NearCorrection(C, A, PV, **kw) on a side stream in a
+    worker thread (the library call releases the GIL) and return a function
+    that waits for it and orders the caller's stream after it."""
+    main = torch.cuda.current_stream(dev)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(main)  # C, A and PV were written on the caller's stream
+    box: Dict[str, Any] = {}
+
+    def run():
+        try:
+            with torch.cuda.device(dev), torch.cuda.stream(side):
+                box["near"] = NearCorrection(C, A, PV, device=dev, **kw)
+        except BaseException as e:  # re-raised in the caller's thread
+            box["error"] = e
+
+    worker = threading.Thread(target=run, name="near-correction", daemon=True)
+    worker.start()
+
+    def result() -> NearCorrection:
+        worker.join()
+        if "error" in box:
+            raise box["error"]
+        main.wait_stream(side)
+        return box["near"]
+
+    return result
+
+
+def panel_vertices_on(mesh: TriMesh, dev) -> Tensor:
+    """(N, 3, 3) FP64 panel vertices vertices[triangles], gathered on the device."""
+    V = torch.as_tensor(mesh.vertices, dtype=torch.float64).to(dev)
+    T = torch.as_tensor(np.asarray(mesh.triangles, dtype=np.int64)).to(dev)
+    return V[T].contiguous()
+
+
 def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtype, mixed: bool, mixed_rtol: float,
                 inner_restart: int, inner_expansion_order: Optional[int], operator: str, fmm_threshold: int,
                 use_graph: bool, self_integral: str, logger, fp64_arithmetic: str = "native",
@@ -218,15 +255,17 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
     linear solve with its retry and fallback chain, and the pass results.
     Returns {"error": msg} on a failure the reference reports as an error."""
     N = mesh.n_panels
-    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64)
-    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64)
-    PV = mesh.vertices[mesh.triangles]
+    # the mesh goes to the device once: centroids, areas, and the panels'
+    # vertices gathered there from the vertex and triangle arrays
+    C64 = torch.as_tensor(mesh.centroids, dtype=torch.float64).to(dev)
+    A64 = torch.as_tensor(mesh.areas, dtype=torch.float64).to(dev)
+    PV = panel_vertices_on(mesh, dev)
     depth_self, depth_near = quad_depths(spec)
     order = int(getattr(cfg, "near_quadrature_order", 2))
     use_quad = self_integral == "quadrature" or (self_integral == "auto" and (
         bool(getattr(cfg, "use_near_quadrature_matvec", False)) or bool(getattr(cfg, "use_near_quadrature", False))))
     if use_quad:
-        I_self = self_integrals(PV, mesh.centroids, order=order, depth=depth_self, device=dev)
+        I_self = self_integrals(PV, C64, order=order, depth=depth_self, device=dev)
     else:
         a = np.clip(mesh.areas, 0.0, None)
         I_self = torch.as_tensor(np.where(mesh.areas > 0, 2.0 * np.pi * K_E * np.sqrt(a / np.pi), 0.0),
@@ -236,12 +275,15 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
     self_corr = (I_self / A_dev.clamp_min(tiny)).to(dtype)
     want_near = bool(getattr(cfg, "use_near_quadrature_matvec", False)) and N > 1
     near = None
+    near_job = None
     if want_near:
-        near = NearCorrection(mesh.centroids, mesh.areas, PV,
-                              distance_factor=float(getattr(cfg, "near_quadrature_distance_factor", 1.5)),
-                              order=order, depth=depth_near, dtype=dtype, device=dev)
-    op = build_operator(C64, A64, self_corr, dtype=dtype, kind=operator, fmm_threshold=fmm_threshold, near=near,
-                        device=dev)
+        # the pair search and weights overlap the operator's tree and lists
+        near_job = _near_in_background(C64, A64, PV, dev,
+                                       distance_factor=float(getattr(cfg, "near_quadrature_distance_factor", 1.5)),
+                                       order=order, depth=depth_near, dtype=dtype)
+    op = build_operator(C64, A64, self_corr, dtype=dtype, kind=operator, fmm_threshold=fmm_threshold, device=dev)
+    if near_job is not None:
+        near = op.near = near_job()
     op32 = None
     if mixed:
         if isinstance(op.base, FmmOperator) and fp64_arithmetic != "native":
