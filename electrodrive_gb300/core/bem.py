@@ -694,6 +694,9 @@ def solve_mixed(op64, op32, b: Tensor, *, A_diag: Optional[Tensor] = None, x0: O
     FP32 operator: x0 is an estimate whose error is far above the FP32
     operator's (about 2e-7 of |A x0|), so the first correction needs no FP64
     application; every later residual, and the stopping test, is FP64.
+
+    On success the returned dict also holds ``residual``, the FP64 residual
+    b - A64 x at the returned x (the stopping test's own vector).
     """
     dev = b.device
     b64 = b.to(torch.float64)

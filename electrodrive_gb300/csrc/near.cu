@@ -270,22 +270,9 @@ __global__ void k_near_scan(const double *cent, const double *radii, int64_t n, 
                         const int j = items[k];
                         const double rj = radii[j];
                         if (!isfinite(rj)) continue;
-                        // d = |c_i - c_j| in numpy's order, kept iff 0 < d <= th; the
-                        // squared distance decides all but the pairs within a few
-                        // ulps of the threshold, which take the square root
-                        const V3 pj = ld3(cent + 3 * (int64_t)j);
-                        const double ex = __dsub_rn(pi.x, pj.x), ey = __dsub_rn(pi.y, pj.y),
-                                     ez = __dsub_rn(pi.z, pj.z);
-                        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+                        const double d = dist_np(pi, ld3(cent + 3 * (int64_t)j));
                         const double th = __dmul_rn(factor, __dadd_rn(radii[i], rj));
-                        const double t2 = th * th;
-                        bool keep;
-                        if (!(d2 > 0.0) || !isfinite(d2) || !(th >= 0.0)) keep = false;
-                        else if (!(t2 >= 1e-290) || !isfinite(t2)) keep = __dsqrt_rn(d2) <= th;
-                        else if (d2 < t2 * (1.0 - 1e-14)) keep = true;
-                        else if (d2 > t2 * (1.0 + 1e-14)) keep = false;
-                        else keep = __dsqrt_rn(d2) <= th;
-                        if (keep) {
+                        if (isfinite(d) && d > 0.0 && d <= th) {
                             if (pass) cols[base + cnt] = j;
                             ++cnt;
                         }
