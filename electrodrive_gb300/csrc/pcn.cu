@@ -8,10 +8,10 @@
 //   h2_i = relu(W2 h1_i + V2 g + b2)                  128 -> 128
 //   h3_i = relu(W3 h2_i + b3)                         128 -> 128
 //   y_i  = w4 . h3_i + b4                             128 -> 1
-// The three per-panel GEMMs run on the tensor cores (mma.sync m16n8k16,
-// BF16 inputs, FP32 accumulators); the context, output and weight-gradient
-// reductions run on the FP32 pipe with fixed reduction orders, so forward and
-// backward are deterministic.
+// The three per-panel GEMMs and the weight gradients' partial products run
+// on the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulators);
+// the context, output and bias reductions run on the FP32 pipe, and every
+// reduction has a fixed order, so forward and backward are deterministic.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -323,48 +323,77 @@ __global__ void k_pcn_head_grad(const __nv_bfloat16 *__restrict__ h3, const floa
     dz[i] = __float2bfloat16_rn(v);
 }
 
-// partial weight gradients over a block of rows:
+// partial weight gradients over a block of rows, on the tensor cores:
 //   part[p][o][k] = sum_{r in block p} D[r][o] X[r][k]     (o < 128, k < K)
 //   part[p][128*K + o] = sum_r D[r][o]                   (bias gradient)
+// The product D^T X has the rows r as its reduction dimension, so each stage
+// of RT rows is staged transposed in shared memory (Dt[o][r], Xt[k][r], padded
+// rows: conflict-free fragment loads) and warp w computes output rows
+// 16w..16w+15 against all K columns with mma.sync m16n8k16 (BF16 in, FP32
+// accumulate; the order of the additions is fixed, so the sums are
+// deterministic).  The bias sums run on the FP32 pipe in row order.
 template <int K>
 __global__ void __launch_bounds__(256) k_pcn_wgrad_part(const __nv_bfloat16 *__restrict__ D,
                                                         const __nv_bfloat16 *__restrict__ X, int64_t n,
                                                         float *__restrict__ part) {
-    constexpr int RT = 32;  // rows per shared tile
-    constexpr int PER = W * K / 256;  // outputs per thread
-    __shared__ float sd[RT][W + 1];
-    __shared__ float sx[RT][K + 1];
-    const int tid = threadIdx.x;
-    // thread -> output unit o and a run of PER consecutive k
-    const int o = (tid * PER) / K, kb = (tid * PER) % K;
-    float acc[PER];
+    constexpr int RT = 32;       // rows per stage (two MMA k-steps)
+    constexpr int LD = RT + 8;   // padded row stride of the transposed tiles (bf16 elements)
+    constexpr int NT = K / 8;    // n-tiles of 8 columns
+    __shared__ __align__(16) __nv_bfloat16 Dt[W * LD];
+    __shared__ __align__(16) __nv_bfloat16 Xt[K * LD];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int o0 = 16 * warp;
+    float acc[NT][4];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) acc[q] = 0.0f;
+    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
     float bsum = 0.0f;
     const int64_t r0 = (int64_t)blockIdx.x * kPartRows, r1 = (n < r0 + kPartRows) ? n : r0 + kPartRows;
     for (int64_t rt = r0; rt < r1; rt += RT) {
         const int rows = (int)((r1 - rt < RT) ? r1 - rt : RT);
         __syncthreads();
-        for (int i = tid; i < RT * W; i += 256) {
-            const int r = i / W, c = i % W;
-            sd[r][c] = r < rows ? __bfloat162float(D[(rt + r) * W + c]) : 0.0f;
+        // transpose RT x 128 of D and RT x K of X into Dt / Xt (pairs of
+        // columns per 32-bit global load; rows past the end are zeros)
+        for (int i = tid; i < RT * (W / 2); i += 256) {
+            const int r = i / (W / 2), c = 2 * (i % (W / 2));
+            __nv_bfloat162 v = __floats2bfloat162_rn(0.0f, 0.0f);
+            if (r < rows) v = *reinterpret_cast<const __nv_bfloat162 *>(D + (rt + r) * W + c);
+            Dt[c * LD + r] = v.x;
+            Dt[(c + 1) * LD + r] = v.y;
         }
-        for (int i = tid; i < RT * K; i += 256) {
-            const int r = i / K, c = i % K;
-            sx[r][c] = r < rows ? __bfloat162float(X[(rt + r) * K + c]) : 0.0f;
+        for (int i = tid; i < RT * (K / 2); i += 256) {
+            const int r = i / (K / 2), c = 2 * (i % (K / 2));
+            __nv_bfloat162 v = __floats2bfloat162_rn(0.0f, 0.0f);
+            if (r < rows) v = *reinterpret_cast<const __nv_bfloat162 *>(X + (rt + r) * K + c);
+            Xt[c * LD + r] = v.x;
+            Xt[(c + 1) * LD + r] = v.y;
         }
         __syncthreads();
-        for (int r = 0; r < rows; ++r) {
-            const float d = sd[r][o];
 #pragma unroll
-            for (int q = 0; q < PER; ++q) acc[q] += d * sx[r][kb + q];
+        for (int k0 = 0; k0 < RT; k0 += 16) {
+            uint32_t a[4];
+            a[0] = ld32(Dt + (o0 + g) * LD + k0 + 2 * t);
+            a[1] = ld32(Dt + (o0 + g + 8) * LD + k0 + 2 * t);
+            a[2] = ld32(Dt + (o0 + g) * LD + k0 + 2 * t + 8);
+            a[3] = ld32(Dt + (o0 + g + 8) * LD + k0 + 2 * t + 8);
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const __nv_bfloat16 *xr = Xt + (8 * j + g) * LD + k0 + 2 * t;
+                mma_bf16(acc[j], a, ld32(xr), ld32(xr + 8));
+            }
         }
         if (tid < W)
-            for (int r = 0; r < rows; ++r) bsum += sd[r][tid];
+            for (int r = 0; r < rows; ++r) bsum += __bfloat162float(Dt[tid * LD + r]);
     }
     float *pp = part + (int64_t)blockIdx.x * (W * K + W);
 #pragma unroll
-    for (int q = 0; q < PER; ++q) pp[o * K + kb + q] = acc[q];
+    for (int j = 0; j < NT; ++j) {
+        const int col = 8 * j + 2 * t;
+        pp[(o0 + g) * K + col] = acc[j][0];
+        pp[(o0 + g) * K + col + 1] = acc[j][1];
+        pp[(o0 + g + 8) * K + col] = acc[j][2];
+        pp[(o0 + g + 8) * K + col + 1] = acc[j][3];
+    }
     if (tid < W) pp[W * K + tid] = bsum;
 }
 
