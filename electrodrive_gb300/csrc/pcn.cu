@@ -93,48 +93,55 @@ Ws carve(void *base, int64_t n) {
 // ---------------------------------------------------------------------------
 // features
 // ---------------------------------------------------------------------------
-// stats: [0..2] mean centroid, [3] mean area, [4] rms rhs, [5] rms radius
-__global__ void __launch_bounds__(1024) k_pcn_stats(const double *__restrict__ c, const double *__restrict__ a,
-                                                    const double *__restrict__ b, int64_t n, double *stats) {
-    __shared__ double red[6][32];
+// stats: [0..2] mean centroid, [3] mean area, [4] rms rhs, [5] rms radius.
+// Two passes of kStatBlocks blocks (grid-stride partial sums, then one small
+// kernel that adds the blocks' partials in block order): the second pass
+// needs the mean centroid of the first.  The partition is fixed, so the
+// sums are deterministic.
+constexpr int kStatBlocks = 152;
+
+__global__ void __launch_bounds__(256) k_pcn_stats_part(const double *__restrict__ c, const double *__restrict__ a,
+                                                        const double *__restrict__ b, int64_t n,
+                                                        const double *__restrict__ mean, double *__restrict__ part) {
+    __shared__ double red[5][8];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     double s[5] = {0, 0, 0, 0, 0};
-    for (int64_t i = tid; i < n; i += blockDim.x) {
-        s[0] += c[3 * i];
-        s[1] += c[3 * i + 1];
-        s[2] += c[3 * i + 2];
-        s[3] += a[i];
-        s[4] += b[i] * b[i];
+    for (int64_t i = (int64_t)blockIdx.x * 256 + tid; i < n; i += (int64_t)gridDim.x * 256) {
+        if (mean) {
+            const double dx = c[3 * i] - mean[0], dy = c[3 * i + 1] - mean[1], dz = c[3 * i + 2] - mean[2];
+            s[0] += dx * dx + dy * dy + dz * dz;
+        } else {
+            s[0] += c[3 * i];
+            s[1] += c[3 * i + 1];
+            s[2] += c[3 * i + 2];
+            s[3] += a[i];
+            s[4] += b[i] * b[i];
+        }
     }
+#pragma unroll
     for (int q = 0; q < 5; ++q) {
         for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
         if (lane == 0) red[q][wid] = s[q];
     }
     __syncthreads();
-    if (tid == 0) {
-        double t[5] = {0, 0, 0, 0, 0};
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-            for (int q = 0; q < 5; ++q) t[q] += red[q][w];
-        const double inv = n > 0 ? 1.0 / (double)n : 0.0;
-        stats[0] = t[0] * inv;
-        stats[1] = t[1] * inv;
-        stats[2] = t[2] * inv;
-        stats[3] = t[3] * inv;
-        stats[4] = sqrt(t[4] * inv);
-    }
-    __syncthreads();
-    const double mx = stats[0], my = stats[1], mz = stats[2];
-    double r = 0;
-    for (int64_t i = tid; i < n; i += blockDim.x) {
-        const double dx = c[3 * i] - mx, dy = c[3 * i + 1] - my, dz = c[3 * i + 2] - mz;
-        r += dx * dx + dy * dy + dz * dz;
-    }
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-    if (lane == 0) red[5][wid] = r;
-    __syncthreads();
-    if (tid == 0) {
+    if (tid < 5) {
         double t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[5][w];
+        for (int w = 0; w < 8; ++w) t += red[tid][w];
+        part[(int64_t)blockIdx.x * 8 + tid] = t;
+    }
+}
+
+// pass 0: stats[0..4] from the first partials; pass 1: stats[5]
+__global__ void k_pcn_stats_fin(const double *__restrict__ part, int nb, int64_t n, int pass, double *stats) {
+    const int q = threadIdx.x;
+    if (pass == 0 && q < 5) {
+        double t = 0;
+        for (int k = 0; k < nb; ++k) t += part[(int64_t)k * 8 + q];
+        const double inv = n > 0 ? 1.0 / (double)n : 0.0;
+        stats[q] = q < 4 ? t * inv : sqrt(t * inv);
+    } else if (pass == 1 && q == 0) {
+        double t = 0;
+        for (int k = 0; k < nb; ++k) t += part[(int64_t)k * 8];
         stats[5] = sqrt(t / (double)(n > 0 ? n : 1));
     }
 }
@@ -508,8 +515,17 @@ extern "C" EDFMM_API int edfmm_pcn_features(const double *centroids_dev, const d
     Ws w = carve(ws_dev, n);
     if (ws_bytes < w.bytes) return fail(EDFMM_ERR_ARG, "edfmm_pcn_features: workspace too small");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    k_pcn_stats<<<1, 1024, 0, s>>>(centroids_dev, areas_dev, rhs_dev, n, w.stats);
-    EDFMM_LAUNCH_CHECK("k_pcn_stats");
+    // the stats partials borrow the weight-gradient partial buffer (at least
+    // W * W + W floats, far more than kStatBlocks * 8 doubles; not in use here)
+    double *sp = reinterpret_cast<double *>(w.part);
+    k_pcn_stats_part<<<kStatBlocks, 256, 0, s>>>(centroids_dev, areas_dev, rhs_dev, n, nullptr, sp);
+    EDFMM_LAUNCH_CHECK("k_pcn_stats_part");
+    k_pcn_stats_fin<<<1, 32, 0, s>>>(sp, kStatBlocks, n, 0, w.stats);
+    EDFMM_LAUNCH_CHECK("k_pcn_stats_fin");
+    k_pcn_stats_part<<<kStatBlocks, 256, 0, s>>>(centroids_dev, areas_dev, rhs_dev, n, w.stats, sp);
+    EDFMM_LAUNCH_CHECK("k_pcn_stats_part");
+    k_pcn_stats_fin<<<1, 32, 0, s>>>(sp, kStatBlocks, n, 1, w.stats);
+    EDFMM_LAUNCH_CHECK("k_pcn_stats_fin");
     k_pcn_features<<<nblk(n, 256), 256, 0, s>>>(centroids_dev, normals_dev, areas_dev, rhs_dev, n, w.stats,
                                                  features_dev);
     EDFMM_LAUNCH_CHECK("k_pcn_features");
