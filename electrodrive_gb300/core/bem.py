@@ -323,14 +323,18 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
 
     sigma = info = None
     r_sigma = None  # the mixed solve's FP64 residual b - A sigma at its sigma
+    N64 = None
     if mixed:
         xm0 = x0
         if warm_start is not None:
             # the learned start (features, network, one FP32 operator
             # application); the reference's chain below keeps x0 = b / I_self
-            from .warm_start import panel_geometry, warm_start as learned_start
+            from .warm_start import warm_start as learned_start
 
-            xs = learned_start(warm_start, panel_geometry(mesh, dev), b, op32)
+            # the network's panel data: the device copies this pass already holds
+            N64 = torch.as_tensor(mesh.normals, dtype=torch.float64).to(dev).contiguous()
+            geom = dict(centroids=C64.contiguous(), normals=N64, areas=A64.contiguous())
+            xs = learned_start(warm_start, geom, b, op32)
             if bool(torch.isfinite(xs).all()):
                 xm0 = xs.to(dtype)
         x, minfo = solve_mixed(op, op32, b, A_diag=diag if use_precond else None, x0=xm0, rtol=mixed_rtol,
@@ -373,7 +377,7 @@ def _solve_pass(spec: Any, cfg: BEMConfig, mesh: TriMesh, h: float, *, dev, dtyp
         V_tot = torch.nan_to_num(V_free + op(sigma).clone(), nan=0.0, posinf=0.0, neginf=0.0)
     bc_resid = float(torch.max(torch.abs(V_tot - bc)))
     energy = float(0.5 * torch.sum(V_tot.double() * torch.nan_to_num(sigma).double() * A_dev))
-    Nrm = torch.as_tensor(mesh.normals, dtype=dtype, device=dev)
+    Nrm = N64.to(dtype) if N64 is not None else torch.as_tensor(mesh.normals, dtype=dtype, device=dev)
     return {"pass_payload": {"h": h, "dof": N, "bc_resid_linf": bc_resid, "energy_A": energy, "gmres_info": dict(info),
                              "tile_size": int(getattr(cfg, "tile_size", 0) or 0),
                              "artifacts": (spec, C_dev, A_dev.to(dtype), Nrm, sigma, V_tot, mesh)},
