@@ -19,8 +19,10 @@ The Krylov arithmetic runs in libedfmm (``edfmm_gmres_*``): CGS2
 orthogonalisation with FP64 inner products, Hessenberg / Givens / triangular
 solve in FP64 on the device.  The host reads the device status once per
 cycle.  When the operator advertises ``capturable = True`` (the operators of
-``electrodrive_gb300.core.operators``) each full cycle is captured once as a
-CUDA graph and replayed.
+``electrodrive_gb300.core.operators``) a cycle's step sequence (or each
+early-exit chunk of it) is captured as a CUDA graph the second time it is
+asked for and replayed from then on; its first run launches the kernels
+directly.
 """
 from __future__ import annotations
 
