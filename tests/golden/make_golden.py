@@ -108,11 +108,11 @@ def save_tree_case(name, kind, n, seed, dtype, leaf, theta, max_depth=32):
     print(f"tree_{name}: N={n} nodes={tree.n_nodes} p2p={len(p2p)} m2l={len(m2l)} ({time.time() - t0:.1f}s)")
 
 
-def save_fmm_case(name, n, seed, dtype, leaf, theta, p):
+def save_fmm_case(name, n, seed, dtype, leaf, theta, p, kind="uniform"):
     from electrodrive.fmm3d.bem_fmm import make_laplace_fmm_backend
     from electrodrive.core.bem_kernel import bem_matvec_gpu
 
-    pts = gen_points("uniform", n, seed, dtype)
+    pts = gen_points(kind, n, seed, dtype)
     g = torch.Generator().manual_seed(seed + 200)
     sigma = (2 * torch.rand(n, generator=g, dtype=torch.float64) - 1).to(dtype)
     areas = (0.5 + torch.rand(n, generator=g, dtype=torch.float64)).to(dtype) * 1e-3
@@ -124,7 +124,7 @@ def save_fmm_case(name, n, seed, dtype, leaf, theta, p):
     v_dense = bem_matvec_gpu(sigma, pts, areas, tile_size=1024, self_integrals=self_int, backend="torch_tiled")
     np.savez_compressed(
         os.path.join(HERE, f"fmm_{name}.npz"),
-        n=n, seed=seed, leaf_size=leaf, theta=theta, p=p, dtype=str(dtype).replace("torch.", ""),
+        n=n, seed=seed, leaf_size=leaf, theta=theta, p=p, dtype=str(dtype).replace("torch.", ""), kind=kind,
         points=pts.numpy(), sigma=sigma.numpy(), areas=areas.numpy(), self_integrals=self_int.numpy(),
         v_fmm_reference=v_fmm.numpy(), v_dense_reference=v_dense.numpy(),
         reference_seconds_per_matvec=t1 - t0,
@@ -481,6 +481,11 @@ def main():
     if "fmm" in which:
         save_fmm_case("uniform512_f32", 512, 10, torch.float32, 64, 0.5, 8)
         save_fmm_case("uniform1024_f32", 1024, 11, torch.float32, 64, 0.5, 8)
+    if "fmm_shapes" in which:
+        # BEM-like and clustered point sets: points on the unit sphere, and two
+        # tight Gaussian clusters over a sparse background with smaller leaves
+        save_fmm_case("sphere1024_f32", 1024, 12, torch.float32, 64, 0.5, 8, kind="sphere")
+        save_fmm_case("clusters1200_leaf32_f32", 1200, 13, torch.float32, 32, 0.5, 8, kind="clusters")
 
 
 if __name__ == "__main__":
