@@ -71,6 +71,18 @@ def test_icosphere_has_5120_panels_on_the_unit_sphere():
     assert abs(m.areas.sum() - 4 * np.pi) < 2e-3 * 4 * np.pi
 
 
+def test_panel_vertices_gather_equals_host_gather():
+    """bem_solve's panel vertex triples, gathered from the vertex and triangle
+    arrays on the solve's device (here the CPU), equal vertices[triangles]."""
+    from electrodrive_gb300.core.bem import panel_vertices_on
+    from electrodrive_gb300.core.bem_mesh import icosphere, torus_mesh
+
+    for m in (icosphere(2), torus_mesh(1.0, 0.35, 20, 8)):
+        pv = panel_vertices_on(m, torch.device("cpu"))
+        assert pv.dtype == torch.float64 and pv.shape == (m.n_panels, 3, 3) and pv.is_contiguous()
+        assert np.array_equal(pv.numpy(), m.vertices[m.triangles])
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", NEAR_CASES)
 def test_gpu_near_field_matches_reference(cuda_lib, name):
